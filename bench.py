@@ -1,0 +1,361 @@
+#!/usr/bin/env python
+"""Plain HoughLine throughput on one GB300 (or N, one process per GPU).
+
+Workload: one 4096 x 4096 uint8 binary image per step -- 64 seeded segments of
+200-3000 px plus 2% salt (about 0.44 M edge points), theta step 0.25 deg
+(T = 720), rho step 1 px over [-5793, 5793] (R = 11587), threshold 300,
+top-256 lines: compaction -> vote -> peak NMS -> rank/merge, all on the GPU.
+
+  value : images/s with the image resident in HBM (device time per step,
+          CUDA events; L2 flushed between steps, flush not timed)
+  e2e   : images/s through the C ABI with host buffers: pinned H2D of the
+          image + hl_plain (which returns the LineParam records to the host)
+  roofline : the vote kernel against the measured shared-memory atomic
+          ceiling of this GPU (conflict-free int32 atomicAdd micro-kernel);
+          the whole pipeline against measured HBM bandwidth is reported
+          beside it
+  cpu_baseline : the C transcription of the reference's vote loop + host
+          tail (oracle/hough_oracle.c) on this host's cores
+
+--impl reference times that CPU transcription alone (the reference's path
+has no CPU implementation of its own; its GPU kernels are the K40-era code
+this project replaces).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "tests" / "golden"))
+
+METRIC = "images/s, Gvotes/s: proposal-guided vs plain Hough, 1 GB300, >=99% recall"
+DETHETA = math.pi / 720
+THRESHOLD = 300
+LINESMAX = 256
+W = H = 4096
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_images(rank: int, n: int):
+    import cases
+    return [cases.synth(2, 1234 + 1000 * rank + i, 0) for i in range(n)]
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text()), "measured"
+        except Exception:
+            pass
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the vote kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "vote_kernel_4096.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: str):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", gpu_index], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        for line in Path(self.f.name).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r)
+                          if v.lower().startswith("active")})
+        return {"sm_mhz": statistics.median(r[0] for r in rows),
+                "sm_max_mhz": max(r[1] for r in rows), "reasons": reasons,
+                "samples": len(rows)}
+
+
+def cpu_reference_images(imgs, budget_s: float, min_images: int = 1):
+    """The C transcription of the reference path on all host cores."""
+    from oracle import oracle as O
+    c, s = O.trig_libm(O.numtheta(DETHETA), DETHETA)
+    t0 = time.perf_counter()
+    n = votes = 0
+    while True:
+        img = imgs[n % len(imgs)]
+        O.houghline(img, c, s, DETHETA, 1.0, THRESHOLD, O.default_thresang(), 50,
+                    LINESMAX)
+        votes += int((img == 255).sum()) * O.numtheta(DETHETA)
+        n += 1
+        el = time.perf_counter() - t0
+        if n >= min_images and el >= budget_s:
+            break
+        if n >= min_images and el / n * (n + 1) > budget_s * 1.5:
+            break
+    return n, el, votes, O.max_threads()
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return 0
+    from opencuda_gb300 import build
+    build.build_oracle()
+    imgs = make_images(0, 2)
+    for _ in range(max(args.warmup, 0)):
+        cpu_reference_images(imgs, 0.0)
+    n, el, votes, cores = cpu_reference_images(imgs, 0.0, min_images=args.steps)
+    ips = n / el
+    line = {"impl": "reference", "metric": METRIC, "value": ips, "unit": "images/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": el / n * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32 votes, f32 rho", "data": "synthetic",
+            "gvotes_per_s": votes / el / 1e9,
+            "config": {"workload": "plain HoughLine 4096x4096, T=720, R=11587, thr 300, top-256",
+                       "images_per_step": 1, "parallelism": "replicas"},
+            "cpu_baseline": {"value": ips, "unit": "images/s", "cores": cores, "kind": "port",
+                             "sample": f"{n} full 4096x4096 images (vote + peaks + host tail), "
+                                       "OpenMP over theta columns"},
+            "e2e": {"value": ips, "unit": "images/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_gb300(args):
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    from opencuda_gb300 import _lib, build
+    build.build_library()
+    L = _lib.load()
+    from opencuda_gb300.houghline import HoughLine, Image
+
+    imgs_host = make_images(rank, 4)
+    hl = HoughLine(detheta=DETHETA, threshold=THRESHOLD)
+    g = hl.geometry(W, H)
+    T = g.numtheta
+    dimgs = [Image.from_host(im, device=dev) for im in imgs_host]
+    npts = [int((im == 255).sum()) for im in imgs_host]
+    stream = torch.cuda.current_stream(dev)
+    sp = C.c_void_p(stream.cuda_stream)
+    lines_dev = torch.empty(LINESMAX * 3, dtype=torch.int32, device=dev)
+    count_dev = torch.zeros(1, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def step(i):
+        d = dimgs[i % len(dimgs)].desc()
+        rc = L.hl_plain_async(hl.handle, C.byref(d), LINESMAX,
+                              C.c_void_p(lines_dev.data_ptr()),
+                              C.c_void_p(count_dev.data_ptr()), sp)
+        if rc != 0:
+            raise RuntimeError(f"hl_plain_async returned {rc}")
+
+    # warm-up (also grows the workspace once)
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize(dev)
+    st = C.c_int()
+    _lib.check(L.hl_last_status(hl.handle, C.byref(st), sp), "hl_last_status")
+    if st.value != 0:
+        raise RuntimeError(f"device status {st.value}")
+    launches_per_step = hl.last_launch_count()
+
+    # shared-memory atomic ceiling of this GPU (micro-kernel)
+    atom = C.c_double()
+    _lib.check(L.hl_measure_smem_atomic_peak(2000, C.byref(atom), sp), "atomic peak")
+
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    gpu_index = os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[local] \
+        if os.environ.get("CUDA_VISIBLE_DEVICES") else str(local)
+    clocks = ClockSampler(gpu_index)
+    _lib.check(L.hl_profile(hl.handle, 1), "hl_profile")
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    t_wall = time.perf_counter()
+    for i in range(args.steps):
+        flush.zero_()                       # L2 flush, outside the timed events
+        evs[i][0].record(stream)
+        step(i)
+        evs[i][1].record(stream)
+    torch.cuda.synchronize(dev)
+    if ws > 1:
+        torch.distributed.barrier()
+    t_wall = time.perf_counter() - t_wall
+    ck = clocks.stop()
+    stage = (C.c_double * 4)()
+    calls = C.c_int()
+    _lib.check(L.hl_profile_read(hl.handle, stage, C.byref(calls)), "hl_profile_read")
+    L.hl_profile(hl.handle, 0)
+    dev_ms = sum(a.elapsed_time(b) for a, b in evs)
+    votes = sum(npts[i % len(npts)] * T for i in range(args.steps))
+    # e2e: pinned host image -> device, hl_plain returns lines to the host
+    pinned = [torch.from_numpy(im).pin_memory() for im in imgs_host]
+    staging = torch.empty((H, W), dtype=torch.uint8, device=dev)
+    e2e_img = Image(staging)
+    lm = C.c_int()
+    out = (_lib.hl_line * LINESMAX)()
+    e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+    for i in range(args.steps + args.warmup):
+        flush.zero_()
+        j = i - args.warmup
+        if j >= 0:
+            e2e_ev[j][0].record(stream)
+        staging.copy_(pinned[i % len(pinned)], non_blocking=True)
+        lm.value = LINESMAX
+        d = e2e_img.desc()
+        rc = L.hl_plain(hl.handle, C.byref(d), C.byref(lm), out, sp)
+        if rc != 0:
+            raise RuntimeError(f"hl_plain returned {rc}")
+        if j >= 0:
+            e2e_ev[j][1].record(stream)
+    torch.cuda.synchronize(dev)
+    e2e_ms = sum(a.elapsed_time(b) for a, b in e2e_ev)
+
+    # max over ranks
+    t = torch.tensor([dev_ms, e2e_ms, stage[1], float(votes)], dtype=torch.float64, device=dev)
+    if ws > 1:
+        torch.distributed.all_reduce(t[:3], op=torch.distributed.ReduceOp.MAX)
+        vt = t[3:].clone()
+        torch.distributed.all_reduce(vt, op=torch.distributed.ReduceOp.SUM)
+        t[3] = vt[0]
+    dev_ms, e2e_ms, vote_ms, votes_all = (float(x) for x in t.tolist())
+    if rank != 0:
+        if ws > 1:
+            torch.distributed.destroy_process_group()
+        return 0
+
+    images = args.steps * ws
+    value = images / (dev_ms / 1e3)
+    peaks, peak_kind = measured_peaks()
+    n_avg = sum(npts[i % len(npts)] for i in range(args.steps)) / args.steps
+    vote_launch_s = vote_ms / 1e3 / max(calls.value, 1)
+    atomics_per_launch = n_avg * T
+    achieved_atom = atomics_per_launch / vote_launch_s
+    b_alg_step = W * H + 4.0 * T * g.numrho          # image once + accumulator once
+    pipe_s = dev_ms / 1e3 / args.steps
+    hbm_gbs = b_alg_step / pipe_s / 1e9
+    traffic = ncu_traffic()
+    line = {
+        "metric": METRIC, "value": value, "unit": "images/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int32 votes, f32 rho (bit-exact)", "data": "synthetic",
+        "gvotes_per_s": votes_all / (dev_ms / 1e3) / 1e9,
+        "config": {"workload": "plain HoughLine 4096x4096, T=720, R=11587, thr 300, top-256",
+                   "edge_points_avg": n_avg, "images_per_step_per_gpu": 1,
+                   "parallelism": f"replicas x{ws} (images sharded, no collective)",
+                   "l2": "flushed between steps (256 MiB write, not timed)"},
+        "stage_ms_avg": {"compact": stage[0] / max(calls.value, 1),
+                         "vote": stage[1] / max(calls.value, 1),
+                         "peaks": stage[2] / max(calls.value, 1),
+                         "finalize": stage[3] / max(calls.value, 1)},
+        "roofline": {"kernel": "hl_vote_kernel", "bound": "smem_atomic",
+                     "achieved": achieved_atom / 1e9, "peak": atom.value / 1e9,
+                     "unit": "Gatomic/s", "frac": achieved_atom / atom.value,
+                     "peak_source": "measured on this GPU: conflict-free shared int32 atomicAdd micro-kernel",
+                     "units_per_launch": atomics_per_launch,
+                     "traffic": traffic,
+                     "hbm": {"achieved": hbm_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                             "frac": hbm_gbs / peaks["hbm_gbs"], "peak_source": peak_kind,
+                             "bytes_per_step": b_alg_step, "scope": "whole pipeline"}},
+        "e2e": {"value": images / (e2e_ms / 1e3), "unit": "images/s",
+                "h2d_bytes_per_step": W * H,
+                "d2h_bytes_per_step": 16 + 12 * LINESMAX},
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": ck,
+        "wall_s_timed_loop": t_wall,
+    }
+    if ws == 1 and not args.no_cpu_baseline:
+        n, el, v, cores = cpu_reference_images(imgs_host, args.cpu_budget)
+        line["cpu_baseline"] = {"value": n / el, "unit": "images/s", "cores": cores,
+                                "kind": "port", "gvotes_per_s": v / el / 1e9,
+                                "sample": f"{n} full 4096x4096 images through the C "
+                                          "transcription of the reference vote loop + "
+                                          "host tail, OpenMP over theta columns"}
+    else:
+        line["cpu_baseline"] = None
+    print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,118 @@
+"""ctypes binding of libhoughline_gb300.so (the C ABI in include/houghline_gb300.h).
+
+The shared library is the product; this module only declares its symbols.
+Loading fails loudly when the library has not been built -- there is no
+Python or CPU fallback for any kernel.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_build" / "libhoughline_gb300.so"
+
+NO_ERROR = 0
+INVALID_DATA = -1
+NULL_POINTER = -2
+OP_OVERFLOW = -3
+NO_FILE = -4
+WRONG_FILE = -5
+OUT_OF_MEM = -6
+CUDA_ERROR = -7
+UNMATCH_IMG = -8
+UNIMPLEMENT = -998
+UNKNOW_ERROR = -999
+
+
+class hl_params(C.Structure):
+    _fields_ = [("detheta", C.c_double), ("derho", C.c_double),
+                ("threshold", C.c_int), ("thresang", C.c_float),
+                ("thresdis", C.c_int)]
+
+
+class hl_line(C.Structure):
+    _fields_ = [("angle", C.c_float), ("distance", C.c_int), ("votes", C.c_int)]
+
+    def as_tuple(self):
+        return (self.angle, self.distance, self.votes)
+
+
+class hl_image_desc(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("pitch", C.c_size_t),
+                ("width", C.c_int), ("height", C.c_int),
+                ("roi_x1", C.c_int), ("roi_y1", C.c_int),
+                ("roi_x2", C.c_int), ("roi_y2", C.c_int)]
+
+
+class hl_geom(C.Structure):
+    _fields_ = [("numtheta", C.c_int), ("theta_pad", C.c_int),
+                ("rho_min", C.c_int), ("numrho", C.c_int),
+                ("ref_numrho", C.c_int), ("tiles_x", C.c_int),
+                ("tiles_y", C.c_int)]
+
+
+class hl_scene_params(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("nseg", C.c_int),
+                ("len_min", C.c_int), ("len_max", C.c_int),
+                ("salt_ppm", C.c_int), ("nbezier", C.c_int),
+                ("seed", C.c_uint64)]
+
+
+H = C.c_void_p
+P = C.c_void_p
+I = C.c_int
+PI = C.POINTER(C.c_int)
+
+# name -> (restype, argtypes); every symbol include/houghline_gb300.h declares
+SIGNATURES = {
+    "hl_create": (I, [C.POINTER(H), C.POINTER(hl_params)]),
+    "hl_destroy": (I, [H]),
+    "hl_set_params": (I, [H, C.POINTER(hl_params)]),
+    "hl_get_params": (I, [H, C.POINTER(hl_params)]),
+    "hl_geometry": (I, [H, I, I, C.POINTER(hl_geom)]),
+    "hl_trig_table": (I, [H, P, P]),
+    "hl_plain": (I, [H, C.POINTER(hl_image_desc), PI, P, P]),
+    "hl_plain_async": (I, [H, C.POINTER(hl_image_desc), I, P, P, P]),
+    "hl_last_status": (I, [H, PI, P]),
+    "hl_plain_points": (I, [H, P, I, PI, P, P]),
+    "hl_compact": (I, [H, C.POINTER(hl_image_desc), P, P, P, P]),
+    "hl_accumulator": (I, [H, C.POINTER(hl_image_desc), P, P]),
+    "hl_accumulator_ref_layout": (I, [H, C.POINTER(hl_image_desc), P, P]),
+    "hl_lines_from_accumulator": (I, [H, P, I, I, PI, P, P]),
+    "hl_set_vote_shape": (I, [H, I, I]),
+    "hl_measure_smem_atomic_peak": (I, [I, C.POINTER(C.c_double), P]),
+    "hl_last_launch_count": (I, [H]),
+    "hl_profile": (I, [H, I]),
+    "hl_profile_read": (I, [H, C.POINTER(C.c_double), PI]),
+    "hl_synth_scene": (I, [C.POINTER(hl_scene_params), P, C.c_long]),
+    "hl_synth_spec": (I, [I, C.c_uint64, I, C.POINTER(hl_scene_params)]),
+}
+
+_lib = None
+
+
+def load(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Load (once) and return the native library; raises if it is missing."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(
+            f"{p} is missing: build the CUDA library first "
+            "(python -c 'import __graft_entry__ as g; g.build()')")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(rc: int, what: str = "call") -> None:
+    if rc != NO_ERROR:
+        raise RuntimeError(f"{what} failed with ErrorCode {rc}")

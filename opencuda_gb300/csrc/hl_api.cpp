@@ -1,0 +1,796 @@
+/*
+ * hl_api.cpp -- the C ABI: handle, workspace and the stage pipeline.
+ *
+ * hl_plain is HoughLine::houghLine (okano_3_0/HoughLine.cu:635-955) without
+ * its per-call cudaMalloc/cudaFree and without the two accumulator-sized
+ * device->host copies: four kernels run back to back on the caller's stream
+ *   compact (a) -> vote (b) -> peaks (c1) -> finalize (c2)
+ * and one small transfer brings back a header plus linesmax LineParam
+ * records.  The workspace is owned by the handle and grows only when a
+ * larger ROI arrives.
+ */
+#include <cuda_runtime.h>
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <new>
+
+#include "hl_internal.h"
+
+#ifndef M_PI
+#error "M_PI required: numtheta = (int)(M_PI / detheta)"
+#endif
+
+struct hl_handle {
+    hl_params p;
+    int T, Tp;
+    int device;
+    int sms;
+    float *d_cos, *d_sin;
+
+    uint32_t *d_pts;
+    size_t cap_pts;
+    unsigned long long *d_tile_state;
+    int *d_tile_off;
+    size_t cap_tiles;
+    int32_t *d_acc;
+    size_t cap_acc;
+    unsigned long long *d_keys;
+    size_t cap_keys;
+    int32_t *d_aux;          /* tight / reference layout staging */
+    size_t cap_aux;
+    unsigned char *d_result; /* hl_result_hdr + lines */
+    size_t cap_result;
+    unsigned char *h_result; /* pinned mirror */
+    /* counters: [0] ncand, [1] status, [2] points, [3] ticket, [4..7] bbox */
+    int *d_counters;
+
+    unsigned ticket_base;
+    unsigned epoch;
+    int win_rows_override, threads_override;
+    int last_launches;
+
+    /* per-stage CUDA-event timing (hl_profile) */
+    int prof;
+    int prof_open;
+    int prof_used;
+    cudaEvent_t *prof_ev;   /* HL_PROF_MAX x HL_NSTAGE+1 */
+};
+
+#define HL_NSTAGE 4
+#define HL_PROF_MAX 512
+
+/* Record the event that closes stage `st` (0 = before the first stage). */
+static void prof_mark(hl_handle *h, int st, cudaStream_t s)
+{
+    if (!h->prof || !h->prof_ev || h->prof_used >= HL_PROF_MAX)
+        return;
+    if (st == 0)
+        h->prof_open = 1;
+    else if (!h->prof_open)
+        return;   /* a call that did not start at stage (a) */
+    cudaEventRecord(h->prof_ev[h->prof_used * (HL_NSTAGE + 1) + st], s);
+    if (st == HL_NSTAGE) {
+        h->prof_used++;
+        h->prof_open = 0;
+    }
+}
+
+static int map_err(cudaError_t e)
+{
+    if (e == cudaSuccess)
+        return HL_NO_ERROR;
+    if (e == cudaErrorMemoryAllocation)
+        return HL_OUT_OF_MEM;
+    return HL_CUDA_ERROR;
+}
+
+#define CK(call)                                  \
+    do {                                          \
+        cudaError_t e__ = (call);                 \
+        if (e__ != cudaSuccess)                   \
+            return map_err(e__);                  \
+    } while (0)
+
+static int grow(void **ptr, size_t *cap, size_t need_bytes)
+{
+    if (*cap >= need_bytes && *ptr)
+        return HL_NO_ERROR;
+    size_t nb = std::max(need_bytes, (size_t)256);
+    nb = nb + nb / 4;   /* headroom for the next, slightly larger ROI */
+    if (*ptr) {
+        cudaFree(*ptr);   /* synchronises: nothing in flight uses it */
+        *ptr = nullptr;
+        *cap = 0;
+    }
+    cudaError_t e = cudaMalloc(ptr, nb);
+    if (e != cudaSuccess) {
+        *ptr = nullptr;
+        return e == cudaErrorMemoryAllocation ? HL_OUT_OF_MEM : HL_CUDA_ERROR;
+    }
+    *cap = nb;
+    return HL_NO_ERROR;
+}
+
+static int check_params(const hl_params *p)
+{
+    if (!(p->detheta > 0.0) || !(p->derho > 0.0))
+        return HL_INVALID_DATA;
+    double t = M_PI / p->detheta;
+    if (!(t >= 1.0) || t > 65536.0)
+        return HL_INVALID_DATA;
+    return HL_NO_ERROR;
+}
+
+static int build_table(hl_handle *h)
+{
+    h->T = (int)(M_PI / h->p.detheta);          /* okano_3_0/HoughLine.cu:671 */
+    h->Tp = (h->T + HL_SLICE - 1) / HL_SLICE * HL_SLICE;
+    if (h->d_cos)
+        cudaFree(h->d_cos);
+    if (h->d_sin)
+        cudaFree(h->d_sin);
+    h->d_cos = h->d_sin = nullptr;
+    CK(cudaMalloc(&h->d_cos, sizeof(float) * h->Tp));
+    CK(cudaMalloc(&h->d_sin, sizeof(float) * h->Tp));
+    CK(hl_launch_trig(h->d_cos, h->d_sin, h->T, h->Tp, h->p.detheta, 0));
+    CK(cudaStreamSynchronize(0));
+    return HL_NO_ERROR;
+}
+
+extern "C" int hl_create(hl_handle **out, const hl_params *params)
+{
+    if (!out)
+        return HL_NULL_POINTER;
+    *out = nullptr;
+    hl_params p;
+    if (params) {
+        p = *params;
+    } else {   /* okano_3_0/HoughLine.h:120-124 */
+        p.detheta = M_PI / 180;
+        p.derho = 1.0;
+        p.threshold = 90;
+        p.thresang = (float)(M_PI / 180 * 5.0f);
+        p.thresdis = 50;
+    }
+    int rc = check_params(&p);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    hl_handle *h = new (std::nothrow) hl_handle();
+    if (!h)
+        return HL_OUT_OF_MEM;
+    memset(h, 0, sizeof(*h));
+    h->p = p;
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount,
+                                   h->device);
+    if (e == cudaSuccess)
+        e = cudaMalloc(&h->d_counters, 16 * sizeof(int));
+    if (e == cudaSuccess)
+        e = cudaMemset(h->d_counters, 0, 16 * sizeof(int));
+    if (e != cudaSuccess) {
+        hl_destroy(h);
+        return map_err(e);
+    }
+    rc = build_table(h);
+    if (rc != HL_NO_ERROR) {
+        hl_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return HL_NO_ERROR;
+}
+
+extern "C" int hl_destroy(hl_handle *h)
+{
+    if (!h)
+        return HL_NULL_POINTER;
+    void *ptrs[] = {h->d_cos, h->d_sin, h->d_pts, h->d_tile_state,
+                    h->d_tile_off, h->d_acc, h->d_keys, h->d_aux,
+                    h->d_result, h->d_counters};
+    for (void *q : ptrs)
+        if (q)
+            cudaFree(q);
+    if (h->h_result)
+        cudaFreeHost(h->h_result);
+    if (h->prof_ev) {
+        for (int i = 0; i < HL_PROF_MAX * (HL_NSTAGE + 1); i++)
+            cudaEventDestroy(h->prof_ev[i]);
+        free(h->prof_ev);
+    }
+    delete h;
+    return HL_NO_ERROR;
+}
+
+extern "C" int hl_profile(hl_handle *h, int enable)
+{
+    if (!h)
+        return HL_NULL_POINTER;
+    if (enable && !h->prof_ev) {
+        int n = HL_PROF_MAX * (HL_NSTAGE + 1);
+        h->prof_ev = (cudaEvent_t *)calloc((size_t)n, sizeof(cudaEvent_t));
+        if (!h->prof_ev)
+            return HL_OUT_OF_MEM;
+        for (int i = 0; i < n; i++)
+            CK(cudaEventCreate(&h->prof_ev[i]));
+    }
+    h->prof = enable ? 1 : 0;
+    h->prof_used = 0;
+    return HL_NO_ERROR;
+}
+
+extern "C" int hl_profile_read(hl_handle *h, double *stage_ms, int *calls)
+{
+    if (!h || !stage_ms || !calls)
+        return HL_NULL_POINTER;
+    for (int s = 0; s < HL_NSTAGE; s++)
+        stage_ms[s] = 0.0;
+    *calls = h->prof_used;
+    for (int c = 0; c < h->prof_used; c++) {
+        cudaEvent_t *e = &h->prof_ev[c * (HL_NSTAGE + 1)];
+        CK(cudaEventSynchronize(e[HL_NSTAGE]));
+        for (int s = 0; s < HL_NSTAGE; s++) {
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, e[s], e[s + 1]));
+            stage_ms[s] += ms;
+        }
+    }
+    h->prof_used = 0;
+    return HL_NO_ERROR;
+}
+
+extern "C" int hl_set_params(hl_handle *h, const hl_params *params)
+{
+    if (!h || !params)
+        return HL_NULL_POINTER;
+    int rc = check_params(params);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    bool retable = params->detheta != h->p.detheta;
+    h->p = *params;
+    return retable ? build_table(h) : HL_NO_ERROR;
+}
+
+extern "C" int hl_get_params(const hl_handle *h, hl_params *params)
+{
+    if (!h || !params)
+        return HL_NULL_POINTER;
+    *params = h->p;
+    return HL_NO_ERROR;
+}
+
+static void layout(const hl_handle *h, double extent, int *rho_min, int *R)
+{
+    int d = (int)floor(extent / h->p.derho + 0.5);
+    *rho_min = -d;
+    *R = 2 * d + 1;
+}
+
+extern "C" int hl_geometry(const hl_handle *h, int w, int hh, hl_geom *g)
+{
+    if (!h || !g)
+        return HL_NULL_POINTER;
+    if (w <= 0 || hh <= 0 || w > HL_MAX_SIDE || hh > HL_MAX_SIDE)
+        return HL_INVALID_DATA;
+    g->numtheta = h->T;
+    g->theta_pad = h->Tp;
+    layout(h, sqrt((double)w * w + (double)hh * hh), &g->rho_min, &g->numrho);
+    /* okano_3_0/HoughLine.cu:670 */
+    g->ref_numrho = (int)((double)(int)((w + hh) * 2 + 1) / h->p.derho);
+    g->tiles_x = (w + HL_TILE_W - 1) / HL_TILE_W;
+    g->tiles_y = (hh + HL_TILE_H - 1) / HL_TILE_H;
+    if ((double)g->numrho * h->Tp >= 2147483647.0)
+        return HL_OP_OVERFLOW;
+    return HL_NO_ERROR;
+}
+
+extern "C" int hl_trig_table(hl_handle *h, float *cos_host, float *sin_host)
+{
+    if (!h || !cos_host || !sin_host)
+        return HL_NULL_POINTER;
+    CK(cudaMemcpy(cos_host, h->d_cos, sizeof(float) * h->T,
+                  cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(sin_host, h->d_sin, sizeof(float) * h->T,
+                  cudaMemcpyDeviceToHost));
+    return HL_NO_ERROR;
+}
+
+extern "C" int hl_set_vote_shape(hl_handle *h, int window_rows, int threads)
+{
+    if (!h)
+        return HL_NULL_POINTER;
+    if (window_rows < 0 || threads < 0 || threads > 1024 || (threads & 31))
+        return HL_INVALID_DATA;
+    if (window_rows > 0 && hl_vote_smem_bytes(window_rows) > 200 * 1024)
+        return HL_INVALID_DATA;
+    h->win_rows_override = window_rows;
+    h->threads_override = threads;
+    return HL_NO_ERROR;
+}
+
+extern "C" int hl_last_launch_count(const hl_handle *h)
+{
+    return h ? h->last_launches : 0;
+}
+
+/* Rho windows per theta slice: enough CTAs to give every SM two, never a
+ * window above 1536 rows (192 KB of shared memory) nor below 64 rows. */
+static void vote_shape(const hl_handle *h, int R, int *rows, int *nwin,
+                       int *threads)
+{
+    const int slices = h->Tp / HL_SLICE;
+    int nw;
+    if (h->win_rows_override > 0) {
+        nw = (R + h->win_rows_override - 1) / h->win_rows_override;
+    } else {
+        int nmin = (R + 1535) / 1536;
+        int want = (2 * std::max(h->sms, 1) + slices - 1) / slices;
+        int nmax = std::max(1, R / 64);
+        nw = std::max(nmin, std::min(want, nmax));
+    }
+    int r = (R + nw - 1) / nw;
+    r = (r + 7) / 8 * 8;
+    nw = (R + r - 1) / r;
+    *rows = r;
+    *nwin = nw;
+    *threads = h->threads_override > 0 ? h->threads_override : 512;
+}
+
+static int ensure_image(hl_handle *h, const hl_geom &g, int w, int hh)
+{
+    int rc;
+    size_t ntiles = (size_t)g.tiles_x * g.tiles_y;
+    if ((rc = grow((void **)&h->d_pts, &h->cap_pts,
+                   sizeof(uint32_t) * (size_t)w * hh)) != HL_NO_ERROR)
+        return rc;
+    if (h->cap_tiles < ntiles + 1 || !h->d_tile_state) {
+        size_t cap = 0;
+        if ((rc = grow((void **)&h->d_tile_state, &cap,
+                       sizeof(unsigned long long) * (ntiles + 1))) != HL_NO_ERROR)
+            return rc;
+        CK(cudaMemset(h->d_tile_state, 0, cap));
+        size_t cap2 = 0;
+        if ((rc = grow((void **)&h->d_tile_off, &cap2,
+                       sizeof(int) * (ntiles + 1))) != HL_NO_ERROR)
+            return rc;
+        h->cap_tiles = std::min(cap / sizeof(unsigned long long),
+                                cap2 / sizeof(int));
+    }
+    return HL_NO_ERROR;
+}
+
+static int ensure_acc(hl_handle *h, int R, int linesmax)
+{
+    int rc;
+    size_t bins = (size_t)R * h->Tp;
+    if ((rc = grow((void **)&h->d_acc, &h->cap_acc, sizeof(int32_t) * bins)) !=
+        HL_NO_ERROR)
+        return rc;
+    /* peaks never sit next to each other along theta: at most ceil(T/2)
+     * per rho row */
+    size_t maxpk = (size_t)R * ((h->T + 1) / 2) + 32;
+    if ((rc = grow((void **)&h->d_keys, &h->cap_keys,
+                   sizeof(unsigned long long) * maxpk)) != HL_NO_ERROR)
+        return rc;
+    size_t lm = (size_t)std::max(linesmax, 1);
+    size_t rbytes = sizeof(hl_result_hdr) + sizeof(hl_line) * lm;
+    if (h->cap_result < rbytes || !h->d_result) {
+        if ((rc = grow((void **)&h->d_result, &h->cap_result, rbytes)) !=
+            HL_NO_ERROR)
+            return rc;
+        if (h->h_result)
+            cudaFreeHost(h->h_result);
+        h->h_result = nullptr;
+        CK(cudaMallocHost(&h->h_result, h->cap_result));
+    }
+    return HL_NO_ERROR;
+}
+
+static int key_cap(const hl_handle *h)
+{
+    size_t c = h->cap_keys / sizeof(unsigned long long);
+    return (int)std::min(c, (size_t)0x7fffffff);
+}
+
+static int roi_of(const hl_image_desc *img, hl_roi *roi)
+{
+    if (!img || !img->data)
+        return HL_NULL_POINTER;
+    /* okano_3_0/Image.h:218-258: the ROI must lie inside the image */
+    if (img->width <= 0 || img->height <= 0 || img->pitch < (size_t)img->width)
+        return HL_INVALID_DATA;
+    if (img->roi_x1 < 0 || img->roi_y1 < 0 || img->roi_x2 > img->width ||
+        img->roi_y2 > img->height || img->roi_x2 <= img->roi_x1 ||
+        img->roi_y2 <= img->roi_y1)
+        return HL_INVALID_DATA;
+    roi->w = img->roi_x2 - img->roi_x1;
+    roi->h = img->roi_y2 - img->roi_y1;
+    if (roi->w > HL_MAX_SIDE || roi->h > HL_MAX_SIDE)
+        return HL_INVALID_DATA;
+    roi->base = img->data + (size_t)img->roi_y1 * img->pitch + img->roi_x1;
+    roi->pitch = (long)img->pitch;
+    return HL_NO_ERROR;
+}
+
+/* stages (a) + (b) into h->d_acc ([R][Tp]) */
+static int run_ab(hl_handle *h, const hl_roi &roi, const hl_geom &g,
+                  cudaStream_t s, int *launches)
+{
+    const int ntiles = g.tiles_x * g.tiles_y;
+    hl_compact_args ca;
+    ca.roi = roi;
+    ca.tiles_x = g.tiles_x;
+    ca.ntiles = ntiles;
+    ca.tile_state = h->d_tile_state;
+    ca.ticket = reinterpret_cast<unsigned *>(h->d_counters + 3);
+    ca.ticket_base = h->ticket_base;
+    if (++h->epoch >= (1u << 30)) {
+        CK(cudaMemsetAsync(h->d_tile_state, 0,
+                           sizeof(unsigned long long) * h->cap_tiles, s));
+        h->epoch = 1;
+    }
+    ca.epoch = h->epoch;
+    ca.pts = h->d_pts;
+    ca.tile_off = h->d_tile_off;
+    ca.count = h->d_counters + 2;
+    ca.status = h->d_counters + 1;
+    prof_mark(h, 0, s);
+    CK(hl_launch_compact(&ca, s));
+    h->ticket_base += (unsigned)ntiles;
+    (*launches)++;
+    prof_mark(h, 1, s);
+
+    hl_vote_args va;
+    va.pts = h->d_pts;
+    va.tile_off = h->d_tile_off;
+    va.ntiles = ntiles;
+    va.tiles_x = g.tiles_x;
+    va.w = roi.w;
+    va.h = roi.h;
+    va.cosv = h->d_cos;
+    va.sinv = h->d_sin;
+    va.T = h->T;
+    va.Tp = h->Tp;
+    va.rho_min = g.rho_min;
+    va.R = g.numrho;
+    int threads;
+    vote_shape(h, g.numrho, &va.win_rows, &va.nwin, &threads);
+    va.irho = (float)(1.0 / h->p.derho);   /* okano_3_0/HoughLine.cu:107 */
+    va.acc = h->d_acc;
+    va.status = h->d_counters + 1;
+    CK(hl_launch_vote(&va, threads, s));
+    (*launches)++;
+    prof_mark(h, 2, s);
+    return HL_NO_ERROR;
+}
+
+/* stage (c) over h->d_acc */
+static int run_c(hl_handle *h, const hl_geom &g, int linesmax,
+                 hl_line *lines_dev, int *count_dev, cudaStream_t s,
+                 int *launches)
+{
+    hl_peak_args pa;
+    pa.acc = h->d_acc;
+    pa.R = g.numrho;
+    pa.T = h->T;
+    pa.Tp = h->Tp;
+    pa.threshold = h->p.threshold;
+    pa.keys = h->d_keys;
+    pa.ncand = h->d_counters + 0;
+    pa.cap = key_cap(h);
+    pa.status = h->d_counters + 1;
+    CK(hl_launch_peaks(&pa, s));
+    (*launches)++;
+    prof_mark(h, 3, s);
+
+    hl_final_args fa;
+    fa.keys = h->d_keys;
+    fa.ncand = h->d_counters + 0;
+    fa.cap = pa.cap;
+    fa.T = h->T;
+    fa.rho_min = g.rho_min;
+    fa.ref_numrho = g.ref_numrho;
+    fa.detheta = h->p.detheta;
+    fa.thresdis = h->p.thresdis;
+    fa.thresang = h->p.thresang;
+    fa.linesmax = linesmax;
+    fa.hdr = reinterpret_cast<hl_result_hdr *>(h->d_result);
+    fa.lines = lines_dev ? lines_dev
+                         : reinterpret_cast<hl_line *>(h->d_result +
+                                                       sizeof(hl_result_hdr));
+    fa.status = h->d_counters + 1;
+    fa.count_out = count_dev;
+    CK(hl_launch_finalize(&fa, s));
+    (*launches)++;
+    prof_mark(h, 4, s);
+    return HL_NO_ERROR;
+}
+
+static int fetch_result(hl_handle *h, int *linesmax, hl_line *lines,
+                        cudaStream_t s)
+{
+    int lm = std::max(*linesmax, 0);
+    size_t bytes = sizeof(hl_result_hdr) + sizeof(hl_line) * (size_t)lm;
+    CK(cudaMemcpyAsync(h->h_result, h->d_result, bytes, cudaMemcpyDeviceToHost,
+                       s));
+    CK(cudaStreamSynchronize(s));
+    const hl_result_hdr *hdr = reinterpret_cast<const hl_result_hdr *>(h->h_result);
+    if (hdr->status != 0)
+        return HL_CUDA_ERROR;
+    int cnt = hdr->count;
+    if (cnt > 0 && lines)
+        memcpy(lines, h->h_result + sizeof(hl_result_hdr),
+               sizeof(hl_line) * (size_t)cnt);
+    *linesmax = cnt;
+    return HL_NO_ERROR;
+}
+
+static int plain_launch(hl_handle *h, const hl_image_desc *img, int linesmax,
+                        hl_line *lines_dev, int *count_dev, cudaStream_t s)
+{
+    hl_roi roi;
+    int rc = roi_of(img, &roi);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    hl_geom g;
+    if ((rc = hl_geometry(h, roi.w, roi.h, &g)) != HL_NO_ERROR)
+        return rc;
+    if ((rc = ensure_image(h, g, roi.w, roi.h)) != HL_NO_ERROR)
+        return rc;
+    if ((rc = ensure_acc(h, g.numrho, linesmax)) != HL_NO_ERROR)
+        return rc;
+    int launches = 0;
+    if ((rc = run_ab(h, roi, g, s, &launches)) != HL_NO_ERROR)
+        return rc;
+    rc = run_c(h, g, linesmax, lines_dev, count_dev, s, &launches);
+    h->last_launches = launches;
+    return rc;
+}
+
+extern "C" int hl_plain(hl_handle *h, const hl_image_desc *img, int *linesmax,
+                        hl_line *lines, void *stream)
+{
+    if (!h || !img || !linesmax)
+        return HL_NULL_POINTER;
+    if (*linesmax > 0 && !lines)
+        return HL_NULL_POINTER;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int rc = plain_launch(h, img, *linesmax, nullptr, nullptr, s);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    return fetch_result(h, linesmax, lines, s);
+}
+
+extern "C" int hl_plain_async(hl_handle *h, const hl_image_desc *img,
+                              int linesmax, hl_line *lines_dev, int *count_dev,
+                              void *stream)
+{
+    if (!h || !img)
+        return HL_NULL_POINTER;
+    if (linesmax > 0 && !lines_dev)
+        return HL_NULL_POINTER;
+    return plain_launch(h, img, linesmax, lines_dev, count_dev,
+                        reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int hl_last_status(hl_handle *h, int *status, void *stream)
+{
+    if (!h || !status)
+        return HL_NULL_POINTER;
+    hl_result_hdr hdr;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (!h->d_result) {
+        *status = 0;
+        return HL_NO_ERROR;
+    }
+    CK(cudaMemcpyAsync(&hdr, h->d_result, sizeof(hdr), cudaMemcpyDeviceToHost,
+                       s));
+    CK(cudaStreamSynchronize(s));
+    *status = hdr.status;
+    return HL_NO_ERROR;
+}
+
+extern "C" int hl_compact(hl_handle *h, const hl_image_desc *img,
+                          uint32_t *pts_dev, int *tile_off_dev, int *count_dev,
+                          void *stream)
+{
+    if (!h || !img || !pts_dev || !tile_off_dev || !count_dev)
+        return HL_NULL_POINTER;
+    hl_roi roi;
+    int rc = roi_of(img, &roi);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    hl_geom g;
+    if ((rc = hl_geometry(h, roi.w, roi.h, &g)) != HL_NO_ERROR)
+        return rc;
+    if ((rc = ensure_image(h, g, roi.w, roi.h)) != HL_NO_ERROR)
+        return rc;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const int ntiles = g.tiles_x * g.tiles_y;
+    hl_compact_args ca;
+    ca.roi = roi;
+    ca.tiles_x = g.tiles_x;
+    ca.ntiles = ntiles;
+    ca.tile_state = h->d_tile_state;
+    ca.ticket = reinterpret_cast<unsigned *>(h->d_counters + 3);
+    ca.ticket_base = h->ticket_base;
+    if (++h->epoch >= (1u << 30)) {
+        CK(cudaMemsetAsync(h->d_tile_state, 0,
+                           sizeof(unsigned long long) * h->cap_tiles, s));
+        h->epoch = 1;
+    }
+    ca.epoch = h->epoch;
+    ca.pts = pts_dev;
+    ca.tile_off = tile_off_dev;
+    ca.count = count_dev;
+    ca.status = h->d_counters + 1;
+    CK(hl_launch_compact(&ca, s));
+    h->ticket_base += (unsigned)ntiles;
+    h->last_launches = 1;
+    return HL_NO_ERROR;
+}
+
+extern "C" int hl_accumulator(hl_handle *h, const hl_image_desc *img,
+                              int32_t *acc_dev, void *stream)
+{
+    if (!h || !img || !acc_dev)
+        return HL_NULL_POINTER;
+    hl_roi roi;
+    int rc = roi_of(img, &roi);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    hl_geom g;
+    if ((rc = hl_geometry(h, roi.w, roi.h, &g)) != HL_NO_ERROR)
+        return rc;
+    if ((rc = ensure_image(h, g, roi.w, roi.h)) != HL_NO_ERROR)
+        return rc;
+    if ((rc = ensure_acc(h, g.numrho, 1)) != HL_NO_ERROR)
+        return rc;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int launches = 0;
+    if ((rc = run_ab(h, roi, g, s, &launches)) != HL_NO_ERROR)
+        return rc;
+    CK(hl_launch_to_tight(h->d_acc, g.numrho, h->T, h->Tp, acc_dev, s));
+    h->last_launches = launches + 1;
+    return HL_NO_ERROR;
+}
+
+extern "C" int hl_accumulator_ref_layout(hl_handle *h, const hl_image_desc *img,
+                                         int32_t *ref_dev, void *stream)
+{
+    if (!h || !img || !ref_dev)
+        return HL_NULL_POINTER;
+    hl_roi roi;
+    int rc = roi_of(img, &roi);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    hl_geom g;
+    if ((rc = hl_geometry(h, roi.w, roi.h, &g)) != HL_NO_ERROR)
+        return rc;
+    if ((rc = ensure_image(h, g, roi.w, roi.h)) != HL_NO_ERROR)
+        return rc;
+    if ((rc = ensure_acc(h, g.numrho, 1)) != HL_NO_ERROR)
+        return rc;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int launches = 0;
+    if ((rc = run_ab(h, roi, g, s, &launches)) != HL_NO_ERROR)
+        return rc;
+    CK(hl_launch_to_ref(h->d_acc, g.numrho, h->T, h->Tp, g.rho_min,
+                        g.ref_numrho, ref_dev, s));
+    h->last_launches = launches + 1;
+    return HL_NO_ERROR;
+}
+
+extern "C" int hl_lines_from_accumulator(hl_handle *h, const int32_t *acc_dev,
+                                         int w, int hh, int *linesmax,
+                                         hl_line *lines, void *stream)
+{
+    if (!h || !acc_dev || !linesmax)
+        return HL_NULL_POINTER;
+    if (*linesmax > 0 && !lines)
+        return HL_NULL_POINTER;
+    hl_geom g;
+    int rc = hl_geometry(h, w, hh, &g);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    if ((rc = ensure_acc(h, g.numrho, *linesmax)) != HL_NO_ERROR)
+        return rc;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    CK(hl_launch_from_tight(acc_dev, g.numrho, h->T, h->Tp, h->d_acc, s));
+    h->prof_open = 0;
+    int launches = 1;
+    if ((rc = run_c(h, g, *linesmax, nullptr, nullptr, s, &launches)) !=
+        HL_NO_ERROR)
+        return rc;
+    h->last_launches = launches;
+    return fetch_result(h, linesmax, lines, s);
+}
+
+extern "C" int hl_plain_points(hl_handle *h, const int *xy_dev, int n,
+                               int *linesmax, hl_line *lines, void *stream)
+{
+    if (!h || !xy_dev || !linesmax)
+        return HL_NULL_POINTER;
+    if (*linesmax > 0 && !lines)
+        return HL_NULL_POINTER;
+    if (n <= 0)
+        return HL_INVALID_DATA;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int init[4] = {0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000};
+    CK(cudaMemcpyAsync(h->d_counters + 4, init, sizeof(init),
+                       cudaMemcpyHostToDevice, s));
+    CK(hl_launch_bbox(xy_dev, n, h->d_counters + 4, s));
+    int bb[4];
+    CK(cudaMemcpyAsync(bb, h->d_counters + 4, sizeof(bb), cudaMemcpyDeviceToHost,
+                       s));
+    CK(cudaStreamSynchronize(s));
+    /* the reference's accumulator height uses the box extent,
+     * okano_3_0/HoughLine.cu:374-375,387 */
+    int w = bb[2] - bb[0], hh = bb[3] - bb[1];
+    double ax = std::max(fabs((double)bb[0]), fabs((double)bb[2]));
+    double ay = std::max(fabs((double)bb[1]), fabs((double)bb[3]));
+    hl_geom g;
+    g.numtheta = h->T;
+    g.theta_pad = h->Tp;
+    layout(h, sqrt(ax * ax + ay * ay) + 1.0, &g.rho_min, &g.numrho);
+    g.ref_numrho = (int)((double)(int)((w + hh) * 2 + 1) / h->p.derho);
+    if ((double)g.numrho * h->Tp >= 2147483647.0)
+        return HL_OP_OVERFLOW;
+    int rc = ensure_acc(h, g.numrho, *linesmax);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    int rows, nwin, threads;
+    vote_shape(h, g.numrho, &rows, &nwin, &threads);
+    CK(hl_launch_vote_points(xy_dev, n, h->d_cos, h->d_sin, h->T, h->Tp,
+                             g.rho_min, g.numrho, rows, nwin,
+                             (float)(1.0 / h->p.derho), h->d_acc, threads, s));
+    int launches = 2;
+    h->prof_open = 0;
+    if ((rc = run_c(h, g, *linesmax, nullptr, nullptr, s, &launches)) !=
+        HL_NO_ERROR)
+        return rc;
+    h->last_launches = launches;
+    return fetch_result(h, linesmax, lines, s);
+}
+
+extern "C" int hl_measure_smem_atomic_peak(int iters, double *atomics_per_s,
+                                           void *stream)
+{
+    if (!atomics_per_s)
+        return HL_NULL_POINTER;
+    if (iters <= 0)
+        return HL_INVALID_DATA;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int *sink = nullptr;
+    CK(cudaMalloc(&sink, sizeof(int)));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int blocks = 0, threads = 0;
+    cudaError_t e = hl_launch_atomic_bench(iters / 4 + 1, sink, s, &blocks,
+                                           &threads);   /* warm-up */
+    float best = 1e30f;
+    for (int rep = 0; rep < 3 && e == cudaSuccess; rep++) {
+        cudaEventRecord(e0, s);
+        e = hl_launch_atomic_bench(iters, sink, s, &blocks, &threads);
+        cudaEventRecord(e1, s);
+        if (e == cudaSuccess)
+            e = cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        best = std::min(best, ms);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    if (e != cudaSuccess)
+        return map_err(e);
+    double total = (double)blocks * threads * (double)iters * 8.0;
+    *atomics_per_s = total / (best * 1e-3);
+    return HL_NO_ERROR;
+}

@@ -1,0 +1,119 @@
+/*
+ * hl_internal.h -- kernel argument blocks and launchers shared by the
+ * translation units of libhoughline_gb300.so (not part of the C ABI).
+ */
+#ifndef HL_INTERNAL_H
+#define HL_INTERNAL_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "houghline_gb300.h"
+
+/* Compaction tiles: 128 x 32 pixels; one CTA of 256 threads reads one tile,
+ * 16 pixels (one 16-byte vector) per thread. */
+#define HL_TILE_W 128
+#define HL_TILE_H 32
+#define HL_COMPACT_THREADS 256
+/* Theta slice = one warp: lane i owns theta k0 + i. */
+#define HL_SLICE 32
+
+/* Bits of the device status word. */
+#define HL_ST_LOOKBACK_TIMEOUT 0x1
+#define HL_ST_CAND_OVERFLOW 0x2
+#define HL_ST_RHO_OUT_OF_RANGE 0x4
+#define HL_ST_MERGE_OVERFLOW 0x8
+
+/* Result block written by the finalize kernel (device) and copied to the
+ * host in one transfer. */
+typedef struct hl_result_hdr {
+    int count;    /* lines written = min(survivors, linesmax) */
+    int status;   /* HL_ST_* bits seen during this call */
+    int ncand;    /* peaks found */
+    int pad;
+} hl_result_hdr;
+
+typedef struct hl_roi {
+    const uint8_t *base;  /* ROI origin */
+    long pitch;
+    int w, h;
+} hl_roi;
+
+typedef struct hl_compact_args {
+    hl_roi roi;
+    int tiles_x, ntiles;
+    unsigned long long *tile_state;  /* [ntiles], epoch-tagged */
+    unsigned int *ticket;            /* monotonically increasing counter */
+    unsigned int ticket_base;        /* value of *ticket at launch */
+    unsigned int epoch;              /* 1..2^30-1, distinct per launch */
+    uint32_t *pts;                   /* out: packed x | y << 16 */
+    int *tile_off;                   /* out: [ntiles + 1] */
+    int *count;                      /* out: total points */
+    int *status;
+} hl_compact_args;
+
+typedef struct hl_vote_args {
+    const uint32_t *pts;
+    const int *tile_off;
+    int ntiles, tiles_x;
+    int w, h;                 /* ROI size (tile clipping) */
+    const float *cosv, *sinv; /* [theta_pad] */
+    int T, Tp;
+    int rho_min, R;
+    int win_rows, nwin;       /* rho window per CTA */
+    float irho;
+    int32_t *acc;             /* [R][Tp] */
+    int *status;
+} hl_vote_args;
+
+typedef struct hl_peak_args {
+    const int32_t *acc;       /* [R][Tp] */
+    int R, T, Tp;
+    int threshold;
+    unsigned long long *keys; /* votes << 32 | ~tight_index */
+    int *ncand;
+    int cap;
+    int *status;
+} hl_peak_args;
+
+typedef struct hl_final_args {
+    const unsigned long long *keys;
+    int *ncand;               /* read, then reset to 0 for the next call */
+    int cap;
+    int T, rho_min, ref_numrho;
+    double detheta;
+    int thresdis;
+    float thresang;
+    int linesmax;
+    hl_line *lines;           /* out: [linesmax] */
+    hl_result_hdr *hdr;       /* out */
+    int *status;              /* read, then reset to 0 */
+    int *count_out;           /* optional extra copy of hdr->count */
+} hl_final_args;
+
+/* launchers (return cudaGetLastError() after the launch) */
+cudaError_t hl_launch_trig(float *cosv, float *sinv, int T, int Tp,
+                           double detheta, cudaStream_t s);
+cudaError_t hl_launch_compact(const hl_compact_args *a, cudaStream_t s);
+cudaError_t hl_launch_vote(const hl_vote_args *a, int threads,
+                           cudaStream_t s);
+size_t hl_vote_smem_bytes(int win_rows);
+cudaError_t hl_launch_vote_points(const int *xy, int n, const float *cosv,
+                                  const float *sinv, int T, int Tp,
+                                  int rho_min, int R, int win_rows, int nwin,
+                                  float irho, int32_t *acc, int threads,
+                                  cudaStream_t s);
+cudaError_t hl_launch_peaks(const hl_peak_args *a, cudaStream_t s);
+cudaError_t hl_launch_finalize(const hl_final_args *a, cudaStream_t s);
+cudaError_t hl_launch_to_tight(const int32_t *acc, int R, int T, int Tp,
+                               int32_t *out, cudaStream_t s);
+cudaError_t hl_launch_to_ref(const int32_t *acc, int R, int T, int Tp,
+                             int rho_min, int ref_numrho, int32_t *ref,
+                             cudaStream_t s);
+cudaError_t hl_launch_from_tight(const int32_t *acc, int R, int T, int Tp,
+                                 int32_t *out, cudaStream_t s);
+cudaError_t hl_launch_bbox(const int *xy, int n, int *bbox, cudaStream_t s);
+cudaError_t hl_launch_atomic_bench(int iters, int *sink, cudaStream_t s,
+                                   int *blocks_out, int *threads_out);
+
+#endif

@@ -1,0 +1,415 @@
+/*
+ * hl_stage_c.cu -- stage (c): peak NMS + threshold, then rank, decode, merge
+ * and truncate, all on the device.
+ *
+ * The reference finds peaks with _findlocalMaxKer (okano_3_0/HoughLine.cu:
+ * 168-213, racy and unchecked at its edges), copies two accumulator-sized
+ * arrays to the host and ranks / merges there (:781-948).  Here:
+ *   hl_peaks_kernel   -- bounds-checked peak rule over acc[R][Tp], peaks
+ *                        appended as 64-bit keys (votes << 32 | ~index) with
+ *                        warp-aggregated atomics (HBM-bound: one read of acc);
+ *   hl_finalize_kernel -- one CTA: top-M selection (MSD radix select when the
+ *                        peaks exceed one chunk), bitonic sort of the chunk,
+ *                        the reference's float decode, and its greedy merge
+ *                        resolved in parallel; writes min(survivors,
+ *                        linesmax) LineParam records.
+ * Ranking is canonical: votes descending, then the reference raster index
+ * (rho-major, theta-minor) ascending -- the reference's Shell sort
+ * (:853-873) is unstable, so ties are ordered by index here.
+ */
+#include "hl_internal.h"
+
+#include <math.h>
+
+#define FULL 0xffffffffu
+#define FIN_THREADS 1024
+#define FIN_CHUNK 1024
+#define FIN_SCACHE 1024
+
+__global__ void hl_peaks_kernel(hl_peak_args a)
+{
+    const int lane = threadIdx.x;
+    const int k = blockIdx.x * 32 + lane;
+    const int row = blockIdx.y * blockDim.y + threadIdx.y;
+    bool is = false;
+    unsigned long long key = 0;
+    if (k < a.T && row < a.R) {
+        const int32_t *p = a.acc + (size_t)row * a.Tp + k;
+        const int v = __ldcs(p);
+        if (v > a.threshold) {
+            const int W = (k > 0) ? p[-1] : 0;
+            const int E = (k + 1 < a.T) ? p[1] : 0;
+            const int N = (row > 0) ? p[-a.Tp] : 0;
+            const int S = (row + 1 < a.R) ? p[a.Tp] : 0;
+            /* okano_3_0/HoughLine.cu:195-199 */
+            if (v > W && v >= E && v > N && v >= S) {
+                is = true;
+                const unsigned idx = (unsigned)row * (unsigned)a.T + (unsigned)k;
+                key = ((unsigned long long)(unsigned)v << 32) | (unsigned)(~idx);
+            }
+        }
+    }
+    const unsigned b = __ballot_sync(FULL, is);
+    if (b) {
+        const int leader = __ffs(b) - 1;
+        int base = 0;
+        if (lane == leader)
+            base = atomicAdd(a.ncand, __popc(b));
+        base = __shfl_sync(FULL, base, leader);
+        if (is) {
+            const int pos = base + __popc(b & ((1u << lane) - 1u));
+            if (pos < a.cap)
+                a.keys[pos] = key;
+            else
+                atomicOr(a.status, HL_ST_CAND_OVERFLOW);
+        }
+    }
+}
+
+cudaError_t hl_launch_peaks(const hl_peak_args *a, cudaStream_t s)
+{
+    dim3 block(32, 8);
+    dim3 grid((a->T + 31) / 32, (a->R + 7) / 8);
+    hl_peaks_kernel<<<grid, block, 0, s>>>(*a);
+    return cudaGetLastError();
+}
+
+/* ------------------------------------------------------------------ */
+/* finalize                                                             */
+
+struct FinSmem {
+    unsigned long long keys[FIN_CHUNK];
+    float ang[FIN_CHUNK];
+    int dist[FIN_CHUNK];
+    int votes[FIN_CHUNK];
+    unsigned mask[FIN_CHUNK][FIN_CHUNK / 32];   /* suppression rows */
+    unsigned removed[FIN_CHUNK / 32];
+    int surv[FIN_CHUNK];
+    float sang[FIN_SCACHE];
+    int sdist[FIN_SCACHE];
+    int hist[256];
+    int misc[8];
+};
+
+/* The merge predicate, okano_3_0/HoughLine.cu:909-920: the angle test is in
+ * float, the wrap-around angle M_PI - a - b in double, rounded to float. */
+__device__ __forceinline__ bool similar(float ai, int di, float aj, int dj,
+                                        int thresdis, float thresang)
+{
+    int dd = abs(di - dj);
+    if (dd < thresdis && fabsf(__fsub_rn(ai, aj)) < thresang)
+        return true;
+    int ds = abs(di + dj);
+    if (ds < thresdis) {
+        double t = __dsub_rn(__dsub_rn(3.14159265358979323846, (double)ai),
+                             (double)aj);
+        float da2 = __double2float_rn(fabs(t));
+        if (da2 < thresang)
+            return true;
+    }
+    return false;
+}
+
+/* Reference decode, okano_3_0/HoughLine.cu:882-897. */
+__device__ __forceinline__ void decode(unsigned long long key, int T,
+                                       int rho_min, int off, float scale,
+                                       double detheta, float *angle,
+                                       int *distance, int *votes)
+{
+    const unsigned idx = ~(unsigned)(key & 0xffffffffu);
+    const int row = (int)(idx / (unsigned)T), k = (int)(idx % (unsigned)T);
+    const int rho = row + rho_min;
+    const int ref_idx = (rho + off + 1) * (T + 2) + k + 1;
+    const int rr = __float2int_rz(__fmul_rn(__int2float_rn(ref_idx), scale)) - 1;
+    const int theta = ref_idx - (rr + 1) * (T + 2) - 1;
+    *angle = __double2float_rn(__dmul_rn((double)theta, detheta));
+    const int rel = rr - off;
+    const float half = (rr >= 0) ? -0.5f : 0.5f;
+    *distance = __float2int_rz(__fsub_rn(__int2float_rn(rel), half));
+    *votes = (int)(key >> 32);
+}
+
+__global__ void __launch_bounds__(FIN_THREADS)
+hl_finalize_kernel(hl_final_args a, float scale)
+{
+    extern __shared__ __align__(16) unsigned char fin_raw[];
+    FinSmem &sm = *reinterpret_cast<FinSmem *>(fin_raw);
+    const int tid = threadIdx.x;
+    const int ncand_raw = *a.ncand;
+    const int n = min(ncand_raw, a.cap);
+    const int K = a.linesmax;
+    const int off = (a.ref_numrho - 1) / 2;
+    int S = 0;          /* survivors written so far */
+    int taken = 0;
+    unsigned long long upper = ~0ull;
+
+    while (taken < n && S < K) {
+        const int m = min(FIN_CHUNK, n - taken);
+        if (n <= FIN_CHUNK) {
+            for (int i = tid; i < m; i += blockDim.x)
+                sm.keys[i] = a.keys[i];
+        } else {
+            /* MSD radix select of the m-th largest key below `upper` */
+            unsigned long long prefix = 0, pmask = 0;
+            int need = m;
+            for (int d = 7; d >= 0; d--) {
+                for (int i = tid; i < 256; i += blockDim.x)
+                    sm.hist[i] = 0;
+                __syncthreads();
+                for (int i = tid; i < n; i += blockDim.x) {
+                    unsigned long long kk = a.keys[i];
+                    if (kk < upper && (kk & pmask) == prefix)
+                        atomicAdd(&sm.hist[(kk >> (8 * d)) & 255], 1);
+                }
+                __syncthreads();
+                if (tid == 0) {
+                    int c = 0, bsel = 0;
+                    for (int bb = 255; bb >= 0; bb--) {
+                        if (c + sm.hist[bb] >= need) {
+                            bsel = bb;
+                            break;
+                        }
+                        c += sm.hist[bb];
+                    }
+                    sm.misc[0] = bsel;
+                    sm.misc[1] = need - c;
+                }
+                __syncthreads();
+                prefix |= (unsigned long long)sm.misc[0] << (8 * d);
+                pmask |= 255ull << (8 * d);
+                need = sm.misc[1];
+                __syncthreads();
+            }
+            if (tid == 0)
+                sm.misc[2] = 0;
+            __syncthreads();
+            for (int i = tid; i < n; i += blockDim.x) {
+                unsigned long long kk = a.keys[i];
+                if (kk < upper && kk >= prefix) {
+                    int pos = atomicAdd(&sm.misc[2], 1);
+                    if (pos < FIN_CHUNK)
+                        sm.keys[pos] = kk;
+                }
+            }
+            __syncthreads();
+        }
+        /* bitonic sort, descending, over P = next power of two >= m */
+        int P = 2;
+        while (P < m)
+            P <<= 1;
+        for (int i = m + tid; i < P; i += blockDim.x)
+            sm.keys[i] = 0ull;
+        __syncthreads();
+        for (int size = 2; size <= P; size <<= 1) {
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                for (int i = tid; i < P; i += blockDim.x) {
+                    int j = i ^ stride;
+                    if (j > i) {
+                        bool desc = (i & size) == 0;
+                        unsigned long long x = sm.keys[i], y = sm.keys[j];
+                        if ((x < y) == desc) {
+                            sm.keys[i] = y;
+                            sm.keys[j] = x;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        taken += m;
+        upper = sm.keys[m - 1];
+
+        /* decode; drop candidates similar to a survivor of an earlier chunk */
+        const int W = (m + 31) >> 5;
+        for (int i = tid; i < 32; i += blockDim.x)
+            sm.removed[i] = 0u;
+        __syncthreads();
+        for (int i = tid; i < m; i += blockDim.x) {
+            float ang;
+            int dist, vts;
+            decode(sm.keys[i], a.T, a.rho_min, off, scale, a.detheta, &ang,
+                   &dist, &vts);
+            sm.ang[i] = ang;
+            sm.dist[i] = dist;
+            sm.votes[i] = vts;
+            bool dead = false;
+            for (int q = 0; q < S && !dead; q++) {
+                float qa;
+                int qd;
+                if (q < FIN_SCACHE) {
+                    qa = sm.sang[q];
+                    qd = sm.sdist[q];
+                } else {
+                    qa = a.lines[q].angle;
+                    qd = a.lines[q].distance;
+                }
+                dead = similar(qa, qd, ang, dist, a.thresdis, a.thresang);
+            }
+            if (dead)
+                atomicOr(&sm.removed[i >> 5], 1u << (i & 31));
+        }
+        __syncthreads();
+        /* suppression bitmask: bit j of mask[i] <=> i < j and similar(i, j) */
+        for (int e = tid; e < m * W; e += blockDim.x) {
+            const int i = e / W, wd = e % W;
+            unsigned bits = 0u;
+            const int j0 = wd << 5;
+            if (j0 + 31 > i) {
+                const float ai = sm.ang[i];
+                const int di = sm.dist[i];
+                const int jlim = min(32, m - j0);
+                for (int b = 0; b < jlim; b++) {
+                    const int j = j0 + b;
+                    if (j > i && similar(ai, di, sm.ang[j], sm.dist[j],
+                                         a.thresdis, a.thresang))
+                        bits |= 1u << b;
+                }
+            }
+            sm.mask[i][wd] = bits;
+        }
+        __syncthreads();
+        /* the greedy pass of okano_3_0/HoughLine.cu:900-927 over the chunk:
+         * one warp jumps from survivor to survivor (lane w holds word w of
+         * the removed set), OR-ing each survivor's suppression row in */
+        if (tid < 32) {
+            const int lane = tid;
+            unsigned rem = (lane < W) ? sm.removed[lane] : 0xffffffffu;
+            if (lane == W - 1 && (m & 31))
+                rem |= ~((1u << (m & 31)) - 1u);
+            int ns = 0;
+            const int room = K - S;
+            while (ns < room) {
+                const unsigned avail = ~rem;
+                const unsigned lanes = __ballot_sync(FULL, avail != 0u);
+                if (!lanes)
+                    break;
+                const int wl = __ffs(lanes) - 1;
+                const unsigned wv = __shfl_sync(FULL, avail, wl);
+                const int i = (wl << 5) + __ffs(wv) - 1;
+                if (lane == 0)
+                    sm.surv[ns] = i;
+                ns++;
+                rem |= (lane < W) ? sm.mask[i][lane] : 0u;
+                if (lane == wl)
+                    rem |= 1u << (i & 31);
+            }
+            if (lane == 0)
+                sm.misc[3] = ns;
+        }
+        __syncthreads();
+        const int ns = sm.misc[3];
+        for (int q = tid; q < ns; q += blockDim.x) {
+            const int i = sm.surv[q];
+            const int o = S + q;
+            hl_line L;
+            L.angle = sm.ang[i];
+            L.distance = sm.dist[i];
+            L.votes = sm.votes[i];
+            a.lines[o] = L;
+            if (o < FIN_SCACHE) {
+                sm.sang[o] = L.angle;
+                sm.sdist[o] = L.distance;
+            }
+        }
+        S += ns;
+        __syncthreads();
+    }
+    if (tid == 0) {
+        int st = *a.status;
+        if (ncand_raw > a.cap)
+            st |= HL_ST_CAND_OVERFLOW;
+        a.hdr->count = (K > 0) ? S : K;
+        a.hdr->status = st;
+        a.hdr->ncand = ncand_raw;
+        if (a.count_out)
+            *a.count_out = (K > 0) ? S : K;
+        *a.ncand = 0;
+        *a.status = 0;
+    }
+}
+
+cudaError_t hl_launch_finalize(const hl_final_args *a, cudaStream_t s)
+{
+    const size_t smem = sizeof(FinSmem);
+    cudaError_t e = cudaFuncSetAttribute(
+        hl_finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    const float scale = (float)(1.0 / (a->T + 2));   /* :882-883 */
+    hl_finalize_kernel<<<1, FIN_THREADS, smem, s>>>(*a, scale);
+    return cudaGetLastError();
+}
+
+/* acc[R][Tp] -> acc[R][T] */
+__global__ void hl_to_tight_kernel(const int32_t *acc, int R, int T, int Tp,
+                                   int32_t *out)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t total = (size_t)R * T;
+    if (i >= total)
+        return;
+    size_t row = i / T, k = i % T;
+    out[i] = acc[row * Tp + k];
+}
+
+cudaError_t hl_launch_to_tight(const int32_t *acc, int R, int T, int Tp,
+                               int32_t *out, cudaStream_t s)
+{
+    size_t total = (size_t)R * T;
+    hl_to_tight_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(acc, R, T,
+                                                                     Tp, out);
+    return cudaGetLastError();
+}
+
+/* acc[R][Tp] -> reference layout (T+2) x (ref_numrho+2) with zero border,
+ * okano_3_0/HoughLine.cu:122-124. */
+__global__ void hl_to_ref_kernel(const int32_t *acc, int R, int T, int Tp,
+                                 int rho_min, int ref_numrho, int32_t *ref)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t total = (size_t)(T + 2) * (size_t)(ref_numrho + 2);
+    if (i >= total)
+        return;
+    int prow = (int)(i / (T + 2)), pcol = (int)(i % (T + 2));
+    int v = 0;
+    int k = pcol - 1, row_ref = prow - 1;
+    if (k >= 0 && k < T && row_ref >= 0 && row_ref < ref_numrho) {
+        int rho = row_ref - (ref_numrho - 1) / 2;
+        int row = rho - rho_min;
+        if (row >= 0 && row < R)
+            v = acc[(size_t)row * Tp + k];
+    }
+    ref[i] = v;
+}
+
+cudaError_t hl_launch_to_ref(const int32_t *acc, int R, int T, int Tp,
+                             int rho_min, int ref_numrho, int32_t *ref,
+                             cudaStream_t s)
+{
+    size_t total = (size_t)(T + 2) * (size_t)(ref_numrho + 2);
+    hl_to_ref_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(
+        acc, R, T, Tp, rho_min, ref_numrho, ref);
+    return cudaGetLastError();
+}
+
+/* acc[R][T] -> acc[R][Tp] (zero padding columns) */
+__global__ void hl_from_tight_kernel(const int32_t *acc, int R, int T, int Tp,
+                                     int32_t *out)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t total = (size_t)R * Tp;
+    if (i >= total)
+        return;
+    size_t row = i / Tp, k = i % Tp;
+    out[i] = (k < (size_t)T) ? acc[row * T + k] : 0;
+}
+
+cudaError_t hl_launch_from_tight(const int32_t *acc, int R, int T, int Tp,
+                                 int32_t *out, cudaStream_t s)
+{
+    size_t total = (size_t)R * Tp;
+    hl_from_tight_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(
+        acc, R, T, Tp, out);
+    return cudaGetLastError();
+}

@@ -1,0 +1,56 @@
+"""CPU tests of the C ABI boundary: the library loads and exports every
+symbol the public header declares; struct layouts match the reference's
+records.  No compute call is made (no GPU here)."""
+import ctypes as C
+import re
+from pathlib import Path
+
+from opencuda_gb300 import _lib
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_symbols():
+    text = (ROOT / "include" / "houghline_gb300.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(hl_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = C.CDLL(str(_lib.LIB_PATH))
+    syms = declared_symbols()
+    assert len(syms) >= 15
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert missing == []
+
+
+def test_binding_covers_header():
+    assert sorted(_lib.SIGNATURES) == declared_symbols()
+
+
+def test_struct_layouts():
+    # LineParam is 12 bytes: float angle, int distance, int votes
+    # (okano_3_0/HoughLine.h:70-74)
+    assert C.sizeof(_lib.hl_line) == 12
+    assert _lib.hl_line.distance.offset == 4
+    assert C.sizeof(_lib.hl_params) == 32
+
+
+def test_error_codes_match_reference():
+    # okano_3_0/ErrorCode.h:16-56
+    assert (_lib.NO_ERROR, _lib.INVALID_DATA, _lib.NULL_POINTER, _lib.OP_OVERFLOW,
+            _lib.OUT_OF_MEM, _lib.CUDA_ERROR, _lib.UNIMPLEMENT) == \
+        (0, -1, -2, -3, -6, -7, -998)
+    hdr = (ROOT / "include" / "houghline_gb300.h").read_text()
+    for name, val in [("HL_NO_ERROR", 0), ("HL_INVALID_DATA", -1),
+                      ("HL_NULL_POINTER", -2), ("HL_OUT_OF_MEM", -6),
+                      ("HL_CUDA_ERROR", -7)]:
+        assert re.search(rf"#define {name}\s+{val}\b", hdr)
+
+
+def test_null_arguments_rejected_without_gpu():
+    lib = _lib.load()
+    assert lib.hl_create(None, None) == _lib.NULL_POINTER
+    assert lib.hl_destroy(None) == _lib.NULL_POINTER
+    assert lib.hl_plain(None, None, None, None, None) == _lib.NULL_POINTER
+    assert lib.hl_set_vote_shape(None, 0, 0) == _lib.NULL_POINTER

@@ -1,0 +1,222 @@
+"""CPU tests of the oracle: known answers, the reference's quirks, and the
+golden accumulators recorded from the reference's own vote kernel."""
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import cases
+from oracle import oracle as O
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def _tables():
+    p = GOLDEN / "trig_tables.npz"
+    if not p.exists():
+        pytest.skip("golden trig tables not generated yet")
+    return np.load(p)
+
+
+def _table(det):
+    T = O.numtheta(det)
+    t = GOLDEN / "trig_tables.npz"
+    if t.exists():
+        z = np.load(t)
+        return z[f"cos_T{T}"], z[f"sin_T{T}"]
+    return O.trig_libm(T, det)
+
+
+def test_numtheta_uses_glibc_pi():
+    # okano_3_0/HoughLine.cu:671 with M_PI from <cmath>
+    assert O.numtheta(math.pi / 180) == 180
+    assert O.numtheta(math.pi / 720) == 720
+    assert O.numtheta(math.pi / 360) == 360
+    # the header's fallback literal would give 179 (okano_3_0/HoughLine.h:62)
+    assert int(math.pi / (3.14159265359 / 180)) == 179
+
+
+def test_layouts():
+    assert O.layout(512, 512) == (-724, 1449)
+    assert O.layout(4096, 4096) == (-5793, 11587)
+    assert O.ref_numrho(512, 512) == 2049      # okano_3_0/HoughLine.cu:670
+    assert O.ref_numrho(4096, 4096) == 16385
+    assert O.ref_numrho(512, 512, 2.0) == 1024
+
+
+@pytest.mark.parametrize("name,k,rho,votes", [
+    ("vertical", 0, 20, 48),       # x = 20: theta 0, rho 20
+    ("diag45", 135, 0, 36),        # y = x: normal at 135 deg through 0
+])
+def test_kat_peak(name, k, rho, votes):
+    img = cases.kat(name)
+    c, s = _table(math.pi / 180)
+    acc, rho_min, dropped = O.vote_image(img, c, s)
+    assert dropped == 0
+    assert acc[rho - rho_min, k] == votes
+    assert acc[:, k].max() == votes
+    # every edge point votes once per theta
+    assert acc.sum() == (img == 255).sum() * 180
+
+
+def test_kat_horizontal_truncation_split():
+    """y = 30 at theta = 90 deg: cosf((float)(pi/2)) is about -4.4e-8, not 0,
+    so x*cos + 30 drops just below 30 once x*4.4e-8 exceeds half an ulp of 30
+    and the reference's truncation (okano_3_0/HoughLine.cu:119) sends the rest
+    of the line to rho 29."""
+    img = cases.kat("horizontal")
+    c, s = _table(math.pi / 180)
+    acc, rho_min, _ = O.vote_image(img, c, s)
+    col = acc[:, 90]
+    assert col[30 - rho_min] + col[29 - rho_min] == 64
+    xs = np.arange(64, dtype=np.float32)
+    v = (xs * np.float32(c[90])).astype(np.float32) + np.float32(30.0) * np.float32(s[90])
+    assert col[30 - rho_min] == int((np.trunc(v.astype(np.float32)) == 30).sum())
+
+
+def test_kat_empty_and_gray():
+    c, s = _table(math.pi / 180)
+    acc, _, _ = O.vote_image(cases.kat("empty"), c, s)
+    assert acc.sum() == 0
+    img = cases.kat("gray")
+    acc, _, _ = O.vote_image(img, c, s)
+    assert acc.sum() == 48 * 180     # only the 255 column votes
+
+
+def test_negative_rho_decode_quirk():
+    # okano_3_0/HoughLine.cu:891: negative rho bins are reported one higher
+    w = h = 64
+    T = 180
+    rho_min, R = O.layout(w, h)
+    nref = O.ref_numrho(w, h)
+    g = O.geom(T, rho_min, R, nref, math.pi / 180, 50, O.default_thresang())
+    off = (nref - 1) // 2
+    for rho, want in [(5, 5), (0, 0), (-1, 0), (-3, -2), (-40, -39)]:
+        k = 17
+        ref_idx = (rho + off + 1) * (T + 2) + k + 1
+        row, kk, ang, dist = O.decode_ref(g, ref_idx)
+        assert kk == k and dist == want
+        assert row == rho - rho_min
+        assert ang == np.float32(k * (math.pi / 180))
+
+
+def test_peak_rule_strictness():
+    # v > W, v >= E, v > N, v >= S (okano_3_0/HoughLine.cu:195-199)
+    acc = np.zeros((5, 6), np.int32)
+    acc[2, 2] = 10
+    acc[2, 3] = 10       # equal east neighbour: (2,2) is a peak, (2,3) is not
+    acc[3, 2] = 10       # equal south neighbour: still a peak
+    pk = O.peaks(acc, 5)
+    assert list(pk) == [2 * 6 + 2]
+    acc2 = np.zeros((3, 3), np.int32)
+    acc2[0, 0] = 7       # border bins compare against the zero border
+    assert list(O.peaks(acc2, 0)) == [0]
+    assert len(O.peaks(acc2, 7)) == 0     # threshold is strict
+
+
+def _geom_for(acc, rho_min, w, h, det=math.pi / 180, thresdis=50):
+    R, T = acc.shape
+    return O.geom(T, rho_min, R, O.ref_numrho(w, h), det, thresdis,
+                  O.default_thresang())
+
+
+def test_merge_wraparound():
+    # a line at ~1 deg with rho d and one at ~179 deg with rho -d are the same
+    # line (okano_3_0/HoughLine.cu:913-919)
+    w = h = 100
+    rho_min, R = O.layout(w, h)
+    acc = np.zeros((R, 180), np.int32)
+    acc[30 - rho_min, 1] = 50
+    acc[-30 - rho_min, 179] = 40
+    acc[80 - rho_min, 90] = 45
+    g = _geom_for(acc, rho_min, w, h)
+    idx = O.peaks(acc, 10)
+    lines, linenum, n = O.rank_merge(acc, g, idx, 8)
+    assert linenum == 2
+    assert [l[2] for l in lines] == [50, 45]
+
+
+def test_rank_ties_canonical_vs_shell():
+    rho_min, R = O.layout(200, 200)
+    acc = np.zeros((R, 180), np.int32)
+    # equal votes, far apart so no merging
+    pos = [(10, 5), (100, 40), (-50, 90), (150, 130), (60, 170)]
+    for r, k in pos:
+        acc[r - rho_min, k] = 30
+    g = _geom_for(acc, rho_min, 200, 200, thresdis=5)
+    idx = O.peaks(acc, 10)
+    can, _, _ = O.rank_merge(acc, g, idx, 8, O.RANK_CANONICAL)
+    # canonical: raster order (rho-major, theta-minor)
+    want = sorted(pos)
+    assert [(d, round(a / (math.pi / 180))) for a, d, v in can] == \
+        [(r if r >= 0 else r + 1, k) for r, k in want]
+    shell, _, _ = O.rank_merge(acc, g, idx, 8, O.RANK_REF_SHELL)
+    assert sorted(x[2] for x in shell) == sorted(x[2] for x in can)
+
+
+def test_linesmax_truncation():
+    rho_min, R = O.layout(200, 200)
+    acc = np.zeros((R, 180), np.int32)
+    for i, (r, k) in enumerate([(10, 5), (100, 40), (-50, 90), (150, 130)]):
+        acc[r - rho_min, k] = 30 + i
+    g = _geom_for(acc, rho_min, 200, 200, thresdis=5)
+    idx = O.peaks(acc, 10)
+    lines, linenum, n = O.rank_merge(acc, g, idx, 2)
+    assert linenum == 4 and n == 2 and [l[2] for l in lines] == [33, 32]
+    lines, linenum, n = O.rank_merge(acc, g, idx, 0)
+    assert n == 0 and lines == []
+
+
+def _golden():
+    p = GOLDEN / "golden.json"
+    if not p.exists():
+        pytest.skip("golden.json not generated yet")
+    return json.loads(p.read_text())
+
+
+@pytest.mark.parametrize("name", cases.CPU_CASES)
+def test_oracle_matches_reference_kernel(name):
+    """The oracle's accumulator, put in the reference layout, hashes to what
+    the reference's own _houghlineImgKer produced on a GB300."""
+    g = _golden()
+    if name not in g["cases"]:
+        pytest.skip(f"{name} not in golden set")
+    rec = g["cases"][name]
+    case = cases.CASES[name]
+    img = cases.image(case)
+    assert O.fnv1a(img) == rec["fnv_image"], "scene generator drifted"
+    x1, y1, x2, y2 = cases.roi_of(case, img)
+    roi = img[y1:y2, x1:x2]
+    c, s = _table(case["detheta"])
+    acc, rho_min, dropped = O.vote_image(roi, c, s, case["derho"])
+    assert dropped == 0
+    ref = O.to_ref_layout(acc, rho_min, rec["ref_numrho"])
+    assert int(ref.sum(dtype=np.int64)) == rec["sum"]
+    assert O.fnv1a(ref) == rec["fnv_ref_acc"]
+
+
+@pytest.mark.parametrize("name", ["points_deg1", "points_deg05"])
+def test_oracle_points_match_reference_kernel(name):
+    g = _golden()
+    if name not in g["cases"]:
+        pytest.skip(f"{name} not in golden set")
+    rec = g["cases"][name]
+    xy = cases.point_set()
+    assert O.fnv1a(xy) == rec["fnv_points"]
+    c, s = _table(rec["detheta"])
+    nref = rec["ref_numrho"]
+    off = (nref - 1) // 2
+    acc, dropped = O.vote_points(xy, c, s, -off, nref)
+    assert dropped == 0
+    assert O.fnv1a(O.to_ref_layout(acc, -off, nref)) == rec["fnv_ref_acc"]
+
+
+def test_trig_tables_recorded():
+    g = _golden()
+    z = _tables()
+    for T in (180, 360, 720):
+        rec = g["tables"][f"T{T}"]
+        assert O.fnv1a(z[f"cos_T{T}"]) == rec["fnv_cos"]
+        assert O.fnv1a(z[f"sin_T{T}"]) == rec["fnv_sin"]
