@@ -159,6 +159,31 @@ int hl_profile_read(hl_handle *h, double *stage_ms, int *calls);
 /* Number of kernels the last hl_plain / hl_plain_async call launched. */
 int hl_last_launch_count(const hl_handle *h);
 
+/* HoughLine::houghLineImg (okano_3_0/HoughLine.cu:958-1345) on DEVICE
+ * images: both ROIs are cut to the smaller width and height (:1101-1109),
+ * the lines are found as in hl_plain (records to the HOST array `lines`),
+ * then drawn into the output ROI: a pixel becomes 255 where
+ * (int)(fl(c*cos a) + fl(r*sin a)) equals a line's distance (:216-249);
+ * other output pixels are left as they are.  Synchronises `stream`. */
+int hl_plain_draw(hl_handle *h, const hl_image_desc *in,
+                  const hl_image_desc *out, int *linesmax, hl_line *lines,
+                  void *stream);
+
+/* The drawing step of houghLineImg alone: nlines HOST records drawn into the
+ * ROI of a DEVICE image (_houghoutKer, okano_3_0/HoughLine.cu:216-249).
+ * Synchronises `stream`. */
+int hl_draw_lines(hl_handle *h, const hl_image_desc *out,
+                  const hl_line *lines, int nlines, void *stream);
+
+/* HoughLine::realLine (okano_3_0/HoughLine.cu:1377-1462): counts the ROI's
+ * 255-pixels inside the segment's bounding box grown by (int)threshold whose
+ * distance to the line through (x1,y1)-(x2,y2) is below (int)threshold;
+ * *is_real = count > (int)|segment| * thresperc.  Coordinates are ROI-local.
+ * pointnum (optional) receives the count.  Synchronises `stream`. */
+int hl_real_line(hl_handle *h, const hl_image_desc *img, int x1, int y1,
+                 int x2, int y2, float threshold, float thresperc,
+                 int *is_real, int *pointnum, void *stream);
+
 /* Synthetic scenes (seeded, integer-only; identical on every host). */
 typedef struct hl_scene_params {
     int width, height;

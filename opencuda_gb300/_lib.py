@@ -86,6 +86,10 @@ SIGNATURES = {
     "hl_last_launch_count": (I, [H]),
     "hl_profile": (I, [H, I]),
     "hl_profile_read": (I, [H, C.POINTER(C.c_double), PI]),
+    "hl_plain_draw": (I, [H, C.POINTER(hl_image_desc), C.POINTER(hl_image_desc), PI, P, P]),
+    "hl_draw_lines": (I, [H, C.POINTER(hl_image_desc), P, I, P]),
+    "hl_real_line": (I, [H, C.POINTER(hl_image_desc), I, I, I, I, C.c_float, C.c_float,
+                         PI, PI, P]),
     "hl_synth_scene": (I, [C.POINTER(hl_scene_params), P, C.c_long]),
     "hl_synth_spec": (I, [I, C.c_uint64, I, C.POINTER(hl_scene_params)]),
 }

@@ -531,7 +531,8 @@ static int fetch_result(hl_handle *h, int *linesmax, hl_line *lines,
 }
 
 static int plain_launch(hl_handle *h, const hl_image_desc *img, int linesmax,
-                        hl_line *lines_dev, int *count_dev, cudaStream_t s)
+                        hl_line *lines_dev, int *count_dev, cudaStream_t s,
+                        int ref_numrho_override = 0)
 {
     hl_roi roi;
     int rc = roi_of(img, &roi);
@@ -540,6 +541,8 @@ static int plain_launch(hl_handle *h, const hl_image_desc *img, int linesmax,
     hl_geom g;
     if ((rc = hl_geometry(h, roi.w, roi.h, &g)) != HL_NO_ERROR)
         return rc;
+    if (ref_numrho_override > 0)
+        g.ref_numrho = ref_numrho_override;
     if ((rc = ensure_image(h, g, roi.w, roi.h)) != HL_NO_ERROR)
         return rc;
     if ((rc = ensure_acc(h, g.numrho, linesmax)) != HL_NO_ERROR)
@@ -792,5 +795,112 @@ extern "C" int hl_measure_smem_atomic_peak(int iters, double *atomics_per_s,
         return map_err(e);
     double total = (double)blocks * threads * (double)iters * 8.0;
     *atomics_per_s = total / (best * 1e-3);
+    return HL_NO_ERROR;
+}
+
+extern "C" int hl_plain_draw(hl_handle *h, const hl_image_desc *in,
+                             const hl_image_desc *out, int *linesmax,
+                             hl_line *lines, void *stream)
+{
+    if (!h || !in || !out || !linesmax || !out->data)
+        return HL_NULL_POINTER;
+    if (*linesmax > 0 && !lines)
+        return HL_NULL_POINTER;
+    hl_roi rin, rout;
+    int rc = roi_of(in, &rin);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    if ((rc = roi_of(out, &rout)) != HL_NO_ERROR)
+        return rc;
+    /* okano_3_0/HoughLine.cu:1101-1109: both ROIs shrink to the smaller
+     * width and height; the accumulator height still comes from the input
+     * ROI (:670), which only the decode sees */
+    const int ref_nrho = (int)((double)(int)((rin.w + rin.h) * 2 + 1) / h->p.derho);
+    const int w = std::min(rin.w, rout.w), hh = std::min(rin.h, rout.h);
+    hl_image_desc vin = *in;
+    vin.roi_x2 = vin.roi_x1 + w;
+    vin.roi_y2 = vin.roi_y1 + hh;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    rc = plain_launch(h, &vin, *linesmax, nullptr, nullptr, s, ref_nrho);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    const int launches = h->last_launches;
+    rc = fetch_result(h, linesmax, lines, s);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    if (*linesmax > 0) {
+        /* the drawing kernel reads the records still held in the device
+         * result block */
+        const hl_line *dl = reinterpret_cast<const hl_line *>(h->d_result +
+                                                              sizeof(hl_result_hdr));
+        int derho_i = (int)h->p.derho;   /* _houghoutKer takes an int derho */
+        if (derho_i == 0)
+            return HL_INVALID_DATA;
+        CK(hl_launch_draw(const_cast<uint8_t *>(rout.base), rout.pitch, w, hh, dl,
+                          *linesmax, derho_i, s));
+        CK(cudaStreamSynchronize(s));
+        h->last_launches = launches + (*linesmax + 1023) / 1024;
+    }
+    return HL_NO_ERROR;
+}
+
+extern "C" int hl_draw_lines(hl_handle *h, const hl_image_desc *out,
+                             const hl_line *lines, int nlines, void *stream)
+{
+    if (!h || !out)
+        return HL_NULL_POINTER;
+    if (nlines <= 0)
+        return HL_NO_ERROR;
+    if (!lines)
+        return HL_NULL_POINTER;
+    hl_roi r;
+    int rc = roi_of(out, &r);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    int derho_i = (int)h->p.derho;
+    if (derho_i == 0)
+        return HL_INVALID_DATA;
+    size_t bytes = sizeof(hl_result_hdr) + sizeof(hl_line) * (size_t)nlines;
+    if ((rc = grow((void **)&h->d_aux, &h->cap_aux, bytes)) != HL_NO_ERROR)
+        return rc;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    CK(cudaMemcpyAsync(h->d_aux, lines, sizeof(hl_line) * (size_t)nlines,
+                       cudaMemcpyHostToDevice, s));
+    CK(hl_launch_draw(const_cast<uint8_t *>(r.base), r.pitch, r.w, r.h,
+                      reinterpret_cast<const hl_line *>(h->d_aux), nlines,
+                      derho_i, s));
+    CK(cudaStreamSynchronize(s));
+    h->last_launches = (nlines + 1023) / 1024;
+    return HL_NO_ERROR;
+}
+
+extern "C" int hl_real_line(hl_handle *h, const hl_image_desc *img, int x1,
+                            int y1, int x2, int y2, float threshold,
+                            float thresperc, int *is_real, int *pointnum,
+                            void *stream)
+{
+    if (!h || !img || !is_real)
+        return HL_NULL_POINTER;
+    hl_roi roi;
+    int rc = roi_of(img, &roi);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int *cnt = h->d_counters + 8;
+    CK(cudaMemsetAsync(cnt, 0, sizeof(int), s));
+    /* okano_3_0/HoughLine.cu:1436-1443: the float threshold is passed to an
+     * int parameter (truncation) */
+    CK(hl_launch_real_line(roi.base, roi.pitch, roi.w, roi.h, x1, y1, x2, y2,
+                           (int)threshold, cnt, s));
+    int n = 0;
+    CK(cudaMemcpyAsync(&n, cnt, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    /* :1405: int pointnumfull = sqrt(0.0 + dx*dx + dy*dy) */
+    const int full = (int)sqrt(0.0 + (double)(x1 - x2) * (x1 - x2) +
+                               (double)(y1 - y2) * (y1 - y2));
+    *is_real = ((float)n > (float)full * thresperc) ? 1 : 0;
+    if (pointnum)
+        *pointnum = n;
+    h->last_launches = 1;
     return HL_NO_ERROR;
 }

@@ -113,6 +113,12 @@ cudaError_t hl_launch_to_ref(const int32_t *acc, int R, int T, int Tp,
 cudaError_t hl_launch_from_tight(const int32_t *acc, int R, int T, int Tp,
                                  int32_t *out, cudaStream_t s);
 cudaError_t hl_launch_bbox(const int *xy, int n, int *bbox, cudaStream_t s);
+cudaError_t hl_launch_draw(uint8_t *out, long pitch, int w, int h,
+                           const hl_line *lines, int nlines, int derho,
+                           cudaStream_t s);
+cudaError_t hl_launch_real_line(const uint8_t *img, long pitch, int w, int h,
+                                int x1, int y1, int x2, int y2, int delta,
+                                int *count, cudaStream_t s);
 cudaError_t hl_launch_atomic_bench(int iters, int *sink, cudaStream_t s,
                                    int *blocks_out, int *threads_out);
 

@@ -346,6 +346,36 @@ void ho_draw_lines(uint8_t *out, long pitch, int w, int h,
     }
 }
 
+int ho_real_line(const uint8_t *roi, long pitch, int w, int h, int x1, int y1,
+                 int x2, int y2, float threshold, float thresperc,
+                 int *is_real)
+{
+    int delta = (int)threshold;                 /* float -> int parameter */
+    int xmax = x1 > x2 ? x1 : x2, xmin = x1 > x2 ? x2 : x1;
+    int ymax = y1 > y2 ? y1 : y2, ymin = y1 > y2 ? y2 : y1;
+    double len = sqrt((double)((x2 - x1) * (x2 - x1)) * 1.0 +
+                      (double)((y2 - y1) * (y2 - y1)));
+    int count = 0;
+    for (int ry = 0; ry < h; ry++) {
+        for (int cx = 0; cx < w; cx++) {
+            if (!(cx <= xmax + delta && cx >= xmin - delta &&
+                  ry <= ymax + delta && ry >= ymin - delta))
+                continue;
+            if (roi[(long)ry * pitch + cx] != 255)
+                continue;
+            int cr = abs((x2 - x1) * (ry - y1) - (cx - x1) * (y2 - y1));
+            float dis = (float)((double)cr / len);
+            if (dis < (float)delta)
+                count++;
+        }
+    }
+    int full = (int)sqrt(0.0 + (double)((x1 - x2) * (x1 - x2)) +
+                         (double)((y1 - y2) * (y1 - y2)));   /* :1405 */
+    if (is_real)
+        *is_real = (float)count > (float)full * thresperc;
+    return count;
+}
+
 uint64_t ho_fnv1a(const void *p, size_t n)
 {
     const uint8_t *b = (const uint8_t *)p;

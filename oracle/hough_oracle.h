@@ -129,6 +129,14 @@ void ho_draw_lines(uint8_t *out, long pitch, int w, int h,
                    const float *cosl, const float *sinl, const int *dist,
                    int nlines);
 
+/* realLine's count, okano_3_0/HoughLine.cu:252-284 and :1377-1462: 255-pixels
+ * of the w x h ROI inside the segment's box grown by delta = (int)threshold
+ * whose distance |cross| / |segment| (double, stored as float) is below
+ * delta.  Returns the count; *is_real = count > (int)|segment| * thresperc. */
+int ho_real_line(const uint8_t *roi, long pitch, int w, int h, int x1, int y1,
+                 int x2, int y2, float threshold, float thresperc,
+                 int *is_real);
+
 /* 64-bit FNV-1a of a byte range (fixture hashing). */
 uint64_t ho_fnv1a(const void *p, size_t n);
 

@@ -65,6 +65,9 @@ def lib() -> C.CDLL:
         L.ho_fnv1a.argtypes = [P, C.c_size_t]
         L.ho_fnv1a.restype = C.c_uint64
         L.ho_max_threads.restype = C.c_int
+        L.ho_real_line.argtypes = [P, C.c_long, C.c_int, C.c_int, C.c_int, C.c_int,
+                                   C.c_int, C.c_int, C.c_float, C.c_float, P]
+        L.ho_real_line.restype = C.c_int
         _lib = L
     return _lib
 
@@ -191,6 +194,16 @@ def houghline(roi: np.ndarray, cosv, sinv, detheta: float, derho: float,
     g = geom(T, rho_min, R, ref_numrho(w, h, derho), detheta, thresdis,
              np.float32(thresang))
     return rank_merge(acc, g, pk, linesmax, mode)
+
+
+def real_line(roi: np.ndarray, x1, y1, x2, y2, threshold: float, thresperc: float):
+    """(count, is_real) of realLine's rule on an ROI."""
+    roi = np.ascontiguousarray(roi, np.uint8)
+    h, w = roi.shape
+    flag = C.c_int()
+    n = lib().ho_real_line(_p(roi), w, w, h, x1, y1, x2, y2, threshold, thresperc,
+                           C.byref(flag))
+    return n, bool(flag.value)
 
 
 def max_threads() -> int:
