@@ -16,8 +16,8 @@
 #include <string.h>
 
 #include <algorithm>
-#include <mutex>
 #include <new>
+#include <vector>
 
 #include "hl_internal.h"
 
@@ -53,6 +53,14 @@ struct hl_handle {
     unsigned epoch;
     int win_rows_override, threads_override;
     int last_launches;
+
+    /* vote work items: heaviest-first order (cached per geometry) and the
+     * persistent-CTA counter base */
+    int *order_dev;
+    size_t cap_order;
+    int order_w, order_h, order_rows, order_R, order_T;
+    double order_derho;
+    unsigned work_base;
 
     /* per-stage CUDA-event timing (hl_profile) */
     int prof;
@@ -192,7 +200,7 @@ extern "C" int hl_destroy(hl_handle *h)
         return HL_NULL_POINTER;
     void *ptrs[] = {h->d_cos, h->d_sin, h->d_pts, h->d_tile_state,
                     h->d_tile_off, h->d_acc, h->d_keys, h->d_aux,
-                    h->d_result, h->d_counters};
+                    h->d_result, h->d_counters, h->order_dev};
     for (void *q : ptrs)
         if (q)
             cudaFree(q);
@@ -306,7 +314,7 @@ extern "C" int hl_set_vote_shape(hl_handle *h, int window_rows, int threads)
         return HL_NULL_POINTER;
     if (window_rows < 0 || threads < 0 || threads > 1024 || (threads & 31))
         return HL_INVALID_DATA;
-    if (window_rows > 0 && hl_vote_smem_bytes(window_rows) > 200 * 1024)
+    if (window_rows > 0 && hl_vote_smem_bytes(window_rows) > 226 * 1024)
         return HL_INVALID_DATA;
     h->win_rows_override = window_rows;
     h->threads_override = threads;
@@ -320,6 +328,9 @@ extern "C" int hl_last_launch_count(const hl_handle *h)
 
 /* Rho windows per theta slice: enough CTAs to give every SM two, never a
  * window above 1536 rows (192 KB of shared memory) nor below 64 rows. */
+/* Rho-window rows per work item: at most 1408 (one CTA of 1024 threads per
+ * SM) and small enough that the heaviest window (the centre of the rho
+ * range) is no more than about a third of one SM's share of the image. */
 static void vote_shape(const hl_handle *h, int R, int *rows, int *nwin,
                        int *threads)
 {
@@ -328,9 +339,9 @@ static void vote_shape(const hl_handle *h, int R, int *rows, int *nwin,
     if (h->win_rows_override > 0) {
         nw = (R + h->win_rows_override - 1) / h->win_rows_override;
     } else {
-        int nmin = (R + 1535) / 1536;
-        int want = (2 * std::max(h->sms, 1) + slices - 1) / slices;
-        int nmax = std::max(1, R / 64);
+        int nmin = (R + 1407) / 1408;
+        int want = (3 * std::max(h->sms, 1) + slices - 1) / slices;
+        int nmax = std::max(1, R / 256);
         nw = std::max(nmin, std::min(want, nmax));
     }
     int r = (R + nw - 1) / nw;
@@ -338,7 +349,60 @@ static void vote_shape(const hl_handle *h, int R, int *rows, int *nwin,
     nw = (R + r - 1) / r;
     *rows = r;
     *nwin = nw;
-    *threads = h->threads_override > 0 ? h->threads_override : 512;
+    *threads = h->threads_override > 0 ? h->threads_override : 1024;
+}
+
+/* Heaviest-first order of the (slice, window) items: the share of the ROI
+ * whose rho at the slice's middle angle falls in the window, estimated on a
+ * 64 x 64 grid of cell centres.  Cached per geometry. */
+static int item_order(hl_handle *h, int w, int hh, int rho_min, int R,
+                      int rows, int nwin, const int **dev_order)
+{
+    const int slices = h->Tp / HL_SLICE;
+    const int nitems = slices * nwin;
+    if (h->order_dev && h->order_w == w && h->order_h == hh &&
+        h->order_rows == rows && h->order_R == R && h->order_T == h->T &&
+        h->order_derho == h->p.derho) {
+        *dev_order = h->order_dev;
+        return HL_NO_ERROR;
+    }
+    std::vector<double> wt((size_t)nitems, 0.0);
+    const int G = 64;
+    for (int sl = 0; sl < slices; sl++) {
+        const int k0 = sl * HL_SLICE;
+        const int k1 = std::min(k0 + HL_SLICE, h->T) - 1;
+        if (k0 >= h->T)
+            continue;
+        const double th = 0.5 * (k0 + k1) * h->p.detheta;
+        const double c = cos(th), s = sin(th);
+        for (int gy = 0; gy < G; gy++) {
+            const double y = (gy + 0.5) * hh / G;
+            for (int gx = 0; gx < G; gx++) {
+                const double x = (gx + 0.5) * w / G;
+                const int row = (int)floor((x * c + y * s) / h->p.derho) - rho_min;
+                const int wn = std::min(std::max(row / rows, 0), nwin - 1);
+                wt[(size_t)sl + (size_t)slices * wn] += (k1 - k0 + 1);
+            }
+        }
+    }
+    std::vector<int> ord((size_t)nitems);
+    for (int i = 0; i < nitems; i++)
+        ord[i] = i;
+    std::stable_sort(ord.begin(), ord.end(),
+                     [&](int a, int b) { return wt[a] > wt[b]; });
+    int rc = grow((void **)&h->order_dev, &h->cap_order, sizeof(int) * (size_t)nitems);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    CK(cudaMemcpy(h->order_dev, ord.data(), sizeof(int) * (size_t)nitems,
+                  cudaMemcpyHostToDevice));
+    h->order_w = w;
+    h->order_h = hh;
+    h->order_rows = rows;
+    h->order_R = R;
+    h->order_T = h->T;
+    h->order_derho = h->p.derho;
+    *dev_order = h->order_dev;
+    return HL_NO_ERROR;
 }
 
 static int ensure_image(hl_handle *h, const hl_geom &g, int w, int hh)
@@ -346,7 +410,7 @@ static int ensure_image(hl_handle *h, const hl_geom &g, int w, int hh)
     int rc;
     size_t ntiles = (size_t)g.tiles_x * g.tiles_y;
     if ((rc = grow((void **)&h->d_pts, &h->cap_pts,
-                   sizeof(uint32_t) * (size_t)w * hh)) != HL_NO_ERROR)
+                   sizeof(uint32_t) * ((size_t)w * hh + 16))) != HL_NO_ERROR)
         return rc;
     if (h->cap_tiles < ntiles + 1 || !h->d_tile_state) {
         size_t cap = 0;
@@ -463,7 +527,21 @@ static int run_ab(hl_handle *h, const hl_roi &roi, const hl_geom &g,
     va.irho = (float)(1.0 / h->p.derho);   /* okano_3_0/HoughLine.cu:107 */
     va.acc = h->d_acc;
     va.status = h->d_counters + 1;
-    CK(hl_launch_vote(&va, threads, s));
+    va.nitems = (h->Tp / HL_SLICE) * va.nwin;
+    int rc = item_order(h, roi.w, roi.h, g.rho_min, g.numrho, va.win_rows,
+                        va.nwin, &va.item_order);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    /* persistent CTAs: as many as fit (one per SM at 1024 threads) */
+    const size_t smem = hl_vote_smem_bytes(va.win_rows);
+    const int per_sm = std::max(1, std::min(2048 / threads,
+                                            (int)((228u * 1024u) / (smem + 1024))));
+    const int grid = std::min(va.nitems, std::max(h->sms, 1) * per_sm);
+    va.work = reinterpret_cast<unsigned *>(h->d_counters + 9);
+    va.work_base = h->work_base;
+    CK(hl_launch_vote(&va, threads, grid, s));
+    /* every CTA takes one ticket per item plus one that finds no item */
+    h->work_base += (unsigned)(va.nitems + grid);
     (*launches)++;
     prof_mark(h, 2, s);
     return HL_NO_ERROR;
@@ -511,6 +589,16 @@ static int run_c(hl_handle *h, const hl_geom &g, int linesmax,
     return HL_NO_ERROR;
 }
 
+/* After a device-side failure the ticket / work counters may not have
+ * advanced by what the host expects: zero them and their bases. */
+static void reset_counters(hl_handle *h, cudaStream_t s)
+{
+    cudaMemsetAsync(h->d_counters, 0, 16 * sizeof(int), s);
+    cudaStreamSynchronize(s);
+    h->ticket_base = 0;
+    h->work_base = 0;
+}
+
 static int fetch_result(hl_handle *h, int *linesmax, hl_line *lines,
                         cudaStream_t s)
 {
@@ -520,8 +608,10 @@ static int fetch_result(hl_handle *h, int *linesmax, hl_line *lines,
                        s));
     CK(cudaStreamSynchronize(s));
     const hl_result_hdr *hdr = reinterpret_cast<const hl_result_hdr *>(h->h_result);
-    if (hdr->status != 0)
+    if (hdr->status != 0) {
+        reset_counters(h, s);
         return HL_CUDA_ERROR;
+    }
     int cnt = hdr->count;
     if (cnt > 0 && lines)
         memcpy(lines, h->h_result + sizeof(hl_result_hdr),
@@ -595,6 +685,8 @@ extern "C" int hl_last_status(hl_handle *h, int *status, void *stream)
                        s));
     CK(cudaStreamSynchronize(s));
     *status = hdr.status;
+    if (hdr.status != 0)
+        reset_counters(h, s);
     return HL_NO_ERROR;
 }
 

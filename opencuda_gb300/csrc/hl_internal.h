@@ -23,6 +23,7 @@
 #define HL_ST_CAND_OVERFLOW 0x2
 #define HL_ST_RHO_OUT_OF_RANGE 0x4
 #define HL_ST_MERGE_OVERFLOW 0x8
+#define HL_ST_VOTE_TIMEOUT 0x10
 
 /* Result block written by the finalize kernel (device) and copied to the
  * host in one transfer. */
@@ -60,11 +61,22 @@ typedef struct hl_vote_args {
     const float *cosv, *sinv; /* [theta_pad] */
     int T, Tp;
     int rho_min, R;
-    int win_rows, nwin;       /* rho window per CTA */
+    int win_rows, nwin;       /* rho window per work item */
     float irho;
     int32_t *acc;             /* [R][Tp] */
     int *status;
+    /* persistent scheduling: items (slice, window) are taken in the order
+     * item_order[] (heaviest first) from a monotonically increasing counter */
+    const int *item_order;    /* [nitems] = slice + nslices * window */
+    int nitems;
+    unsigned *work;           /* counter */
+    unsigned work_base;       /* its value at launch */
 } hl_vote_args;
+
+/* Vote-kernel staging: points per TMA batch and pieces per batch. */
+#define HL_VOTE_CHUNK 1024
+#define HL_VOTE_PIECES 16
+#define HL_VOTE_TG 1024       /* tiles per coarse-filter group */
 
 typedef struct hl_peak_args {
     const int32_t *acc;       /* [R][Tp] */
@@ -95,9 +107,10 @@ typedef struct hl_final_args {
 cudaError_t hl_launch_trig(float *cosv, float *sinv, int T, int Tp,
                            double detheta, cudaStream_t s);
 cudaError_t hl_launch_compact(const hl_compact_args *a, cudaStream_t s);
-cudaError_t hl_launch_vote(const hl_vote_args *a, int threads,
+cudaError_t hl_launch_vote(const hl_vote_args *a, int threads, int grid,
                            cudaStream_t s);
 size_t hl_vote_smem_bytes(int win_rows);
+size_t hl_vote_points_smem_bytes(int win_rows);
 cudaError_t hl_launch_vote_points(const int *xy, int n, const float *cosv,
                                   const float *sinv, int T, int Tp,
                                   int rho_min, int R, int win_rows, int nwin,

@@ -21,56 +21,83 @@
 
 #include <math.h>
 
+#include <algorithm>
+
 #define FULL 0xffffffffu
 #define FIN_THREADS 1024
 #define FIN_CHUNK 1024
 #define FIN_SCACHE 1024
 
-__global__ void hl_peaks_kernel(hl_peak_args a)
+/* append one peak key (warp-aggregated: one global atomic per warp) */
+__device__ __forceinline__ void push_key(bool is, unsigned long long key,
+                                         const hl_peak_args &a)
 {
-    const int lane = threadIdx.x;
-    const int k = blockIdx.x * 32 + lane;
-    const int row = blockIdx.y * blockDim.y + threadIdx.y;
-    bool is = false;
-    unsigned long long key = 0;
-    if (k < a.T && row < a.R) {
-        const int32_t *p = a.acc + (size_t)row * a.Tp + k;
-        const int v = __ldcs(p);
-        if (v > a.threshold) {
-            const int W = (k > 0) ? p[-1] : 0;
-            const int E = (k + 1 < a.T) ? p[1] : 0;
-            const int N = (row > 0) ? p[-a.Tp] : 0;
-            const int S = (row + 1 < a.R) ? p[a.Tp] : 0;
-            /* okano_3_0/HoughLine.cu:195-199 */
-            if (v > W && v >= E && v > N && v >= S) {
-                is = true;
-                const unsigned idx = (unsigned)row * (unsigned)a.T + (unsigned)k;
-                key = ((unsigned long long)(unsigned)v << 32) | (unsigned)(~idx);
-            }
-        }
-    }
+    const int lane = threadIdx.x & 31;
     const unsigned b = __ballot_sync(FULL, is);
-    if (b) {
-        const int leader = __ffs(b) - 1;
-        int base = 0;
-        if (lane == leader)
-            base = atomicAdd(a.ncand, __popc(b));
-        base = __shfl_sync(FULL, base, leader);
-        if (is) {
-            const int pos = base + __popc(b & ((1u << lane) - 1u));
-            if (pos < a.cap)
-                a.keys[pos] = key;
-            else
-                atomicOr(a.status, HL_ST_CAND_OVERFLOW);
+    if (!b)
+        return;
+    const int leader = __ffs(b) - 1;
+    int base = 0;
+    if (lane == leader)
+        base = atomicAdd(a.ncand, __popc(b));
+    base = __shfl_sync(FULL, base, leader);
+    if (is) {
+        const int pos = base + __popc(b & ((1u << lane) - 1u));
+        if (pos < a.cap)
+            a.keys[pos] = key;
+        else
+            atomicOr(a.status, HL_ST_CAND_OVERFLOW);
+    }
+}
+
+/* One thread per 4 consecutive bins of a row (one 16-byte streaming load);
+ * the neighbours are read only for bins above the threshold, which are rare,
+ * so the kernel is one pass over the accumulator at HBM speed. */
+__global__ void __launch_bounds__(256) hl_peaks_kernel(hl_peak_args a)
+{
+    const int q4 = a.Tp >> 2;
+    const size_t total = (size_t)a.R * q4;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+         e - threadIdx.x < total; e += (size_t)gridDim.x * blockDim.x) {
+        int4 v = make_int4(0, 0, 0, 0);
+        const int row = (e < total) ? (int)(e / q4) : 0;
+        const int k4 = (e < total) ? (int)(e % q4) * 4 : 0;
+        if (e < total)
+            v = __ldcs(reinterpret_cast<const int4 *>(a.acc) + e);
+        const int vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int k = k4 + q;
+            bool is = false;
+            unsigned long long key = 0;
+            if (e < total && k < a.T && vv[q] > a.threshold) {
+                const int32_t *p = a.acc + (size_t)row * a.Tp + k;
+                const int W = (k > 0) ? p[-1] : 0;
+                const int E = (k + 1 < a.T) ? p[1] : 0;
+                const int N = (row > 0) ? p[-a.Tp] : 0;
+                const int S = (row + 1 < a.R) ? p[a.Tp] : 0;
+                const int x = vv[q];
+                /* okano_3_0/HoughLine.cu:195-199 */
+                if (x > W && x >= E && x > N && x >= S) {
+                    is = true;
+                    const unsigned idx = (unsigned)row * (unsigned)a.T + (unsigned)k;
+                    key = ((unsigned long long)(unsigned)x << 32) | (unsigned)(~idx);
+                }
+            }
+            push_key(is, key, a);
         }
     }
 }
 
 cudaError_t hl_launch_peaks(const hl_peak_args *a, cudaStream_t s)
 {
-    dim3 block(32, 8);
-    dim3 grid((a->T + 31) / 32, (a->R + 7) / 8);
-    hl_peaks_kernel<<<grid, block, 0, s>>>(*a);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t total = (size_t)a->R * (a->Tp >> 2);
+    size_t blocks = (total + 255) / 256;
+    blocks = std::min(blocks, (size_t)sms * 8);
+    hl_peaks_kernel<<<(unsigned)std::max(blocks, (size_t)1), 256, 0, s>>>(*a);
     return cudaGetLastError();
 }
 
@@ -249,23 +276,29 @@ hl_finalize_kernel(hl_final_args a, float scale)
                 atomicOr(&sm.removed[i >> 5], 1u << (i & 31));
         }
         __syncthreads();
-        /* suppression bitmask: bit j of mask[i] <=> i < j and similar(i, j) */
-        for (int e = tid; e < m * W; e += blockDim.x) {
-            const int i = e / W, wd = e % W;
-            unsigned bits = 0u;
-            const int j0 = wd << 5;
-            if (j0 + 31 > i) {
-                const float ai = sm.ang[i];
-                const int di = sm.dist[i];
-                const int jlim = min(32, m - j0);
-                for (int b = 0; b < jlim; b++) {
-                    const int j = j0 + b;
-                    if (j > i && similar(ai, di, sm.ang[j], sm.dist[j],
-                                         a.thresdis, a.thresang))
-                        bits |= 1u << b;
+        /* suppression bitmask: bit j of mask[i] <=> i < j and similar(i, j).
+         * Warp w owns the 32 candidates j of word w: it walks the rows i
+         * below them (broadcast shared loads) and ballots one word per row;
+         * rows at or past the word are zero. */
+        {
+            const int wd = tid >> 5, lane = tid & 31;
+            if (wd < W) {
+                const int j = (wd << 5) + lane;
+                const bool jv = j < m;
+                const float aj = jv ? sm.ang[j] : 0.f;
+                const int dj = jv ? sm.dist[j] : 0;
+                const int ilim = min(m, (wd << 5) + 32);
+                for (int i = 0; i < ilim; i++) {
+                    const bool hit = jv && j > i &&
+                                     similar(sm.ang[i], sm.dist[i], aj, dj,
+                                             a.thresdis, a.thresang);
+                    const unsigned bits = __ballot_sync(FULL, hit);
+                    if (lane == 0)
+                        sm.mask[i][wd] = bits;
                 }
+                for (int i = ilim + lane; i < m; i += 32)
+                    sm.mask[i][wd] = 0u;
             }
-            sm.mask[i][wd] = bits;
         }
         __syncthreads();
         /* the greedy pass of okano_3_0/HoughLine.cu:900-927 over the chunk:

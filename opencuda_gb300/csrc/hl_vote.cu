@@ -3,26 +3,40 @@
  *
  * Vote rule (okano_3_0/HoughLine.cu:86-130): an edge point (x, y) adds one
  * to bin (k, trunc(fl(x*cos_k) + fl(y*sin_k))) for every k.  The products and
- * the sum are rounded separately (__fmul_rn/__fadd_rn: no FMA contraction),
- * the float is truncated toward zero (the reference's +-0.5 step after the
- * (int) cast is a no-op), and cos_k/sin_k come from the GPU-evaluated table.
+ * the sum are rounded separately (no FMA contraction: packed mul.rn.f32x2 /
+ * add.rn.f32x2, each rounded on its own), the float is truncated toward zero
+ * (the reference's +-0.5 step after the (int) cast is a no-op), and
+ * cos_k/sin_k come from the GPU-evaluated table.
  *
- * Work decomposition.  A CTA owns a (theta slice, rho window) block of the
- * accumulator in shared memory: 32 thetas (one per lane) x win_rows rho bins,
- * laid out acc[row][lane].  A warp takes one point at a time; its 32 lanes
- * add to 32 different thetas of the same point, i.e. 32 different banks, so
- * every shared atomic instruction is conflict-free and no two lanes ever hit
- * one address (the aggregation a warp-aggregated atomic would buy is built
- * into the layout).  Points arrive tile-major from stage (a); a CTA whose
- * window does not cover the whole rho range skips tiles whose rho interval
- * over the slice misses its window.  Each CTA finally stores its block with
- * coalesced 128-byte rows into acc[R][Tp] -- every bin is written exactly
- * once, so the global accumulator needs no clearing.
+ * Work decomposition.  A work item is one (theta slice, rho window) block of
+ * the accumulator, held in shared memory as acc[row][lane]: 32 thetas (one
+ * per lane) x win_rows rho bins.  A warp takes two points per step; its 32
+ * lanes add to 32 different thetas of the same point -- 32 different banks --
+ * so every shared atomic instruction is conflict-free and no two lanes ever
+ * hit one address (the aggregation a warp-aggregated atomic would buy is built
+ * into the layout).
+ *
+ * Persistent CTAs take items heaviest-first from a global counter.  For an
+ * item, a coarse filter marks the 128x32 compaction tiles whose rho interval
+ * over the slice meets the window; runs of marked tiles are contiguous in the
+ * tile-major point list, and thread 0 streams them into shared memory with
+ * cp.async.bulk (TMA bulk copies of 16-byte aligned supersets of each run)
+ * completing on an mbarrier, two batches in flight.  All threads then unpack
+ * each batch, drop points whose own rho interval over the slice misses the
+ * window, and vote.  At the end of the item the block is stored with
+ * coalesced 128-byte rows into acc[R][Tp]; every bin is written exactly once,
+ * so the global accumulator needs no clearing.
+ *
+ * Bounds: the rho row of every vote is checked against the window (a point
+ * whose interval straddles the window votes only its in-window lanes), lanes
+ * beyond T never vote, mbarrier waits are bounded (status bit on time-out,
+ * then every thread leaves together).
  */
 #include "hl_internal.h"
 
 #define FULL 0xffffffffu
-#define LIST_CAP 1024
+#define RAWCAP (HL_VOTE_CHUNK + 6 * HL_VOTE_PIECES + 32)
+#define MBAR_SPIN_LIMIT (1 << 22)
 
 template <bool UNIT>
 __device__ __forceinline__ int rho_of(float x, float y, float c, float s,
@@ -37,12 +51,106 @@ __device__ __forceinline__ int rho_of(float x, float y, float c, float s,
     return __float2int_rz(__fadd_rn(a, b));
 }
 
+/* ---- packed f32x2 arithmetic (sm_100+), each operation rounded alone ---- */
+__device__ __forceinline__ unsigned long long pk2(float a, float b)
+{
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void up2(unsigned long long v, float &a, float &b)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long mul2(unsigned long long a,
+                                                   unsigned long long b)
+{
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long add2(unsigned long long a,
+                                                   unsigned long long b)
+{
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+
+/* rho values of the two points (x0, y0), (x1, y1) of a pair record
+ * {x0, x1, y0, y1} for this lane's (c, s) */
+template <bool UNIT>
+__device__ __forceinline__ void rho_pair(const float4 &q, unsigned long long cc,
+                                         unsigned long long ss,
+                                         unsigned long long ii, int &r0,
+                                         int &r1)
+{
+    unsigned long long a = mul2(pk2(q.x, q.y), cc);
+    unsigned long long b = mul2(pk2(q.z, q.w), ss);
+    if (!UNIT) {
+        a = mul2(a, ii);
+        b = mul2(b, ii);
+    }
+    float v0, v1;
+    up2(add2(a, b), v0, v1);
+    r0 = __float2int_rz(v0);
+    r1 = __float2int_rz(v1);
+}
+
+/* ---- mbarrier + bulk copy ---------------------------------------------- */
+__device__ __forceinline__ unsigned smem_u32(const void *p)
+{
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned n)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(n)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar,
+                                               unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                     smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src,
+                                         unsigned bytes,
+                                         unsigned long long *bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+        "[%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+/* bounded wait for the phase with the given parity; false on time-out */
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar,
+                                          unsigned parity)
+{
+    const unsigned a = smem_u32(bar);
+    for (int i = 0; i < MBAR_SPIN_LIMIT; i++) {
+        unsigned ok;
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], "
+            "%2; selp.u32 %0, 1, 0, p; }"
+            : "=r"(ok)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (ok)
+            return true;
+    }
+    return false;
+}
+
 /* Conservative test: can any point of tile t vote into rho bins
- * [lo_bin, hi_bin] for a theta in [k0, k1]?  rho(x, y, th) is linear in
+ * [lo_bin, hi_bin] for a theta in [th0, th1]?  rho(x, y, th) is linear in
  * (x, y) for fixed th, so its extremes over the tile lie at the corners; over
  * th in [th0, th1] (within [0, pi)) a corner's value |p| cos(th - phi), phi in
- * [0, pi/2], has no interior minimum and an interior maximum |p| only when
- * phi lies between th0 and th1.  Two bins of slack cover float rounding. */
+ * [0, pi/2], has no interior minimum and an interior maximum |p| <= x + y only
+ * when phi lies between th0 and th1.  Three bins of slack cover rounding. */
 __device__ __forceinline__ bool tile_hits(int t, int tiles_x, int w, int h,
                                           float c0, float s0, float c1,
                                           float s1, float lo_bin,
@@ -64,7 +172,7 @@ __device__ __forceinline__ bool tile_hits(int t, int tiles_x, int w, int h,
         float hi = fmaxf(f0, f1);
         float tol = 1e-3f * (x + y) + 1e-3f;
         if (c0 * y - s0 * x >= -tol && x * s1 - y * c1 >= -tol)
-            hi = fmaxf(hi, sqrtf(x * x + y * y) + 1.0f);
+            hi = fmaxf(hi, x + y);
         mx = fmaxf(mx, hi);
     }
     mn = mn * irho - 3.0f;
@@ -72,97 +180,314 @@ __device__ __forceinline__ bool tile_hits(int t, int tiles_x, int w, int h,
     return mn <= hi_bin && mx >= lo_bin;
 }
 
+struct VoteSmem {
+    unsigned long long mbar[2];
+    int item;
+    int nruns;
+    int nconv[3];
+    int np[2];
+    int total[2];
+    int timeout;
+    int pc_src[2][HL_VOTE_PIECES];    /* first point copied (multiple of 4) */
+    int pc_roff[2][HL_VOTE_PIECES];   /* offset in raw[slot] */
+    int pc_skip[2][HL_VOTE_PIECES];   /* leading points copied but not used */
+    int pc_base[2][HL_VOTE_PIECES + 1];
+    unsigned mask[HL_VOTE_TG / 32];
+    int run_s[HL_VOTE_TG / 2 + 1];
+    int run_e[HL_VOTE_TG / 2 + 1];
+    alignas(16) unsigned raw[2][RAWCAP];
+    alignas(16) float4 conv[2][HL_VOTE_CHUNK / 2 + 1];
+};
+
+#define VOTE_FIXED ((sizeof(VoteSmem) + 127) / 128 * 128)
+
+size_t hl_vote_smem_bytes(int win_rows)
+{
+    return VOTE_FIXED + (size_t)win_rows * HL_SLICE * sizeof(int);
+}
+
+/* Producer (thread 0): form the next batch of up to HL_VOTE_CHUNK points from
+ * the run list and start its bulk copies into raw[slot].  State: run index r
+ * and point cursor pos.  Source and destination of every copy are 16-byte
+ * aligned (whole groups of 4 points) and the point list is allocated with at
+ * least 4 entries of slack, so the rounded-up tail stays in bounds. */
+__device__ void produce(VoteSmem &sm, int slot, const uint32_t *pts, int &r,
+                        int &pos)
+{
+    int total = 0, np = 0, roff = 0;
+    const int nruns = sm.nruns;
+    while (np < HL_VOTE_PIECES && total < HL_VOTE_CHUNK && r < nruns) {
+        if (pos >= sm.run_e[r]) {
+            r++;
+            if (r < nruns)
+                pos = sm.run_s[r];
+            continue;
+        }
+        const int take = min(sm.run_e[r] - pos, HL_VOTE_CHUNK - total);
+        const int a0 = pos & ~3;
+        const int a1 = (pos + take + 3) & ~3;
+        sm.pc_src[slot][np] = a0;
+        sm.pc_roff[slot][np] = roff;
+        sm.pc_skip[slot][np] = pos - a0;
+        sm.pc_base[slot][np] = total;
+        roff += a1 - a0;
+        total += take;
+        pos += take;
+        np++;
+    }
+    sm.pc_base[slot][np] = total;
+    sm.np[slot] = np;
+    sm.total[slot] = total;
+    if (total > 0) {
+        mbar_expect_tx(&sm.mbar[slot], (unsigned)roff * 4u);
+        for (int p = 0; p < np; p++) {
+            const int end = (p + 1 < np) ? sm.pc_roff[slot][p + 1] : roff;
+            const int nb = end - sm.pc_roff[slot][p];
+            bulk_g2s(&sm.raw[slot][sm.pc_roff[slot][p]], pts + sm.pc_src[slot][p],
+                     (unsigned)nb * 4u, &sm.mbar[slot]);
+        }
+    }
+}
+
 template <bool UNIT>
 __global__ void __launch_bounds__(1024, 1)
 hl_vote_kernel(hl_vote_args a)
 {
-    extern __shared__ __align__(16) int s_acc[];   /* win_rows * 32 */
-    __shared__ int s_list[LIST_CAP];
-    __shared__ int s_nlist, s_next;
+    extern __shared__ __align__(128) unsigned char vote_raw[];
+    VoteSmem &sm = *reinterpret_cast<VoteSmem *>(vote_raw);
+    int *s_acc = reinterpret_cast<int *>(vote_raw + VOTE_FIXED);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nthr = blockDim.x, nwarps = nthr >> 5;
+    const int nslices = a.Tp / HL_SLICE;
+    const unsigned long long ii = pk2(a.irho, a.irho);
 
-    const int tid = threadIdx.x, lane = tid & 31;
-    const int slice = blockIdx.x, win = blockIdx.y;
-    const int k0 = slice * HL_SLICE;
-    const int k = k0 + lane;
-    const bool kvalid = k < a.T;
-    const float c = a.cosv[k], s = a.sinv[k];   /* table padded to Tp */
-    const int w0 = win * a.win_rows;
-    const int rows = min(a.win_rows, a.R - w0);
-    const int row_base = a.rho_min + w0;        /* rho bin of local row 0 */
+    if (tid == 0) {
+        mbar_init(&sm.mbar[0], 1);
+        mbar_init(&sm.mbar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        sm.nconv[0] = sm.nconv[1] = sm.nconv[2] = 0;
+        sm.timeout = 0;
+    }
+    unsigned use0 = 0u, use1 = 0u;   /* completed phases of mbar[0], mbar[1] */
+    __syncthreads();
 
-    for (int i = tid; i < rows * HL_SLICE; i += blockDim.x)
-        s_acc[i] = 0;
-
-    const int klast = min(k0 + HL_SLICE - 1, a.T - 1);
-    const float c0 = a.cosv[k0], s0 = a.sinv[k0];
-    const float c1 = a.cosv[klast], s1 = a.sinv[klast];
-    const float lo_bin = (float)row_base, hi_bin = (float)(row_base + rows - 1);
-
-    for (int t0 = 0; t0 < a.ntiles; t0 += LIST_CAP) {
+    while (true) {
         if (tid == 0) {
-            s_nlist = 0;
-            s_next = 0;
+            const unsigned t = atomicAdd(a.work, 1u) - a.work_base;
+            sm.item = (t < (unsigned)a.nitems) ? a.item_order[t] : -1;
         }
         __syncthreads();
-        const int t1 = min(a.ntiles, t0 + LIST_CAP);
-        for (int t = t0 + tid; t < t1; t += blockDim.x) {
-            if (a.tile_off[t + 1] == a.tile_off[t])
-                continue;
-            if (a.nwin == 1 ||
-                tile_hits(t, a.tiles_x, a.w, a.h, c0, s0, c1, s1, lo_bin,
-                          hi_bin, a.irho)) {
-                int pos = atomicAdd(&s_nlist, 1);
-                s_list[pos] = t;
+        const int item = sm.item;
+        if (item < 0 || sm.timeout)
+            break;
+        const int slice = item % nslices, win = item / nslices;
+        const int k0 = slice * HL_SLICE, k = k0 + lane;
+        const float c = a.cosv[k], s = a.sinv[k];   /* table padded to Tp */
+        const int w0 = win * a.win_rows;
+        const int rows = min(a.win_rows, a.R - w0);
+        const int row_base = a.rho_min + w0;       /* rho bin of local row 0 */
+        const unsigned lrows = (k < a.T) ? (unsigned)rows : 0u;
+        const int klast = min(k0 + HL_SLICE - 1, a.T - 1);
+        const float c0 = a.cosv[k0], s0 = a.sinv[k0];
+        const float c1 = a.cosv[klast], s1 = a.sinv[klast];
+        const float lo_bin = (float)row_base;
+        const float hi_bin = (float)(row_base + rows - 1);
+        const bool filter = a.nwin > 1;
+        const unsigned long long cc = pk2(c, c), ss = pk2(s, s);
+        int *accl = s_acc + lane;
+/* one vote of rho bin r, if it lies in the window and the lane has a theta */
+#define VOTE(r)                                                     \
+    do {                                                            \
+        const unsigned rl__ = (unsigned)((r) - row_base);           \
+        if (rl__ < lrows)                                           \
+            atomicAdd(accl + rl__ * HL_SLICE, 1);                   \
+    } while (0)
+
+        {
+            int4 *z = reinterpret_cast<int4 *>(s_acc);
+            const int4 zero = make_int4(0, 0, 0, 0);
+            for (int i = tid; i < rows * (HL_SLICE / 4); i += nthr)
+                z[i] = zero;
+        }
+
+        for (int tg = 0; tg < a.ntiles; tg += HL_VOTE_TG) {
+            const int tg_n = min(HL_VOTE_TG, a.ntiles - tg);
+            /* coarse filter: one bit per tile of the group */
+            for (int wd = warp; wd < HL_VOTE_TG / 32; wd += nwarps) {
+                const int tl = wd * 32 + lane;
+                bool hit = false;
+                if (tl < tg_n)
+                    hit = !filter || tile_hits(tg + tl, a.tiles_x, a.w, a.h, c0,
+                                               s0, c1, s1, lo_bin, hi_bin,
+                                               a.irho);
+                const unsigned m = __ballot_sync(FULL, hit);
+                if (lane == 0)
+                    sm.mask[wd] = m;
             }
-        }
-        __syncthreads();
-        const int nl = s_nlist;
-        while (true) {
-            int item = 0;
-            if (lane == 0)
-                item = atomicAdd(&s_next, 1);
-            item = __shfl_sync(FULL, item, 0);
-            if (item >= nl)
-                break;
-            const int t = s_list[item];
-            const int beg = a.tile_off[t], end = a.tile_off[t + 1];
-            for (int b = beg; b < end; b += 32) {
-                const int i = b + lane;
-                const uint32_t pk = (i < end) ? __ldg(&a.pts[i]) : 0u;
-                const float xf = (float)(pk & 0xffffu);
-                const float yf = (float)(pk >> 16);
-                const int nb = min(32, end - b);
-                for (int j = 0; j < nb; j++) {
-                    const float x = __shfl_sync(FULL, xf, j);
-                    const float y = __shfl_sync(FULL, yf, j);
-                    const int row = rho_of<UNIT>(x, y, c, s, a.irho) - row_base;
-                    if (kvalid && (unsigned)row < (unsigned)rows)
-                        atomicAdd(&s_acc[row * HL_SLICE + lane], 1);
+            __syncthreads();
+            /* runs of marked tiles -> point ranges (warp 0) */
+            if (warp == 0) {
+                const unsigned m = sm.mask[lane];
+                const unsigned prev = __shfl_up_sync(FULL, m, 1);
+                const unsigned next = __shfl_down_sync(FULL, m, 1);
+                const unsigned carry_in = (lane > 0) ? (prev >> 31) : 0u;
+                const unsigned carry_out = (lane < 31) ? (next & 1u) : 0u;
+                unsigned starts = m & ~((m << 1) | carry_in);
+                unsigned ends = m & ~((m >> 1) | (carry_out << 31));
+                const int ns = __popc(starts), ne = __popc(ends);
+                int bs = ns, be = ne;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t1 = __shfl_up_sync(FULL, bs, o);
+                    const int t2 = __shfl_up_sync(FULL, be, o);
+                    if (lane >= o) {
+                        bs += t1;
+                        be += t2;
+                    }
+                }
+                bs -= ns;
+                be -= ne;
+                while (starts) {
+                    const int b = __ffs(starts) - 1;
+                    starts &= starts - 1;
+                    sm.run_s[bs++] = a.tile_off[tg + lane * 32 + b];
+                }
+                while (ends) {
+                    const int b = __ffs(ends) - 1;
+                    ends &= ends - 1;
+                    sm.run_e[be++] = a.tile_off[tg + lane * 32 + b + 1];
+                }
+                if (lane == 31)
+                    sm.nruns = bs;
+            }
+            __syncthreads();
+
+            /* stream the runs through shared memory, two batches in flight */
+            int r = 0, pos = (sm.nruns > 0) ? sm.run_s[0] : 0;
+            if (tid == 0) {
+                sm.nconv[0] = sm.nconv[1] = sm.nconv[2] = 0;
+                produce(sm, 0, a.pts, r, pos);
+                produce(sm, 1, a.pts, r, pos);
+            }
+            __syncthreads();
+            for (int b = 0;; b++) {
+                const int slot = b & 1;
+                const int total = sm.total[slot];
+                if (total == 0)
+                    break;
+                const unsigned par = (slot ? use1 : use0) & 1u;
+                const bool ok = mbar_wait(&sm.mbar[slot], par);
+                if (slot)
+                    use1++;
+                else
+                    use0++;
+                if (!ok && lane == 0) {
+                    /* the batch never arrived: flag it and carry on with the
+                     * same barriers (votes stay inside the window, so the
+                     * result is only wrong, and the call reports it) */
+                    sm.timeout = 1;
+                    atomicOr(a.status, HL_ST_VOTE_TIMEOUT);
+                }
+                /* unpack + per-point window filter -> conv[slot] */
+                const int np = sm.np[slot];
+                const int cnt_i = b % 3;       /* kept-point counter of batch b */
+                float *cv = reinterpret_cast<float *>(sm.conv[slot]);
+                for (int j0 = 0; j0 < total; j0 += nthr) {
+                    const int j = j0 + tid;
+                    bool keep = false;
+                    float x = 0.f, y = 0.f;
+                    if (j < total) {
+                        int p = 0;
+                        while (p + 1 < np && sm.pc_base[slot][p + 1] <= j)
+                            p++;
+                        const unsigned u =
+                            sm.raw[slot][sm.pc_roff[slot][p] + sm.pc_skip[slot][p] +
+                                         (j - sm.pc_base[slot][p])];
+                        x = (float)(u & 0xffffu);
+                        y = (float)(u >> 16);
+                        keep = true;
+                        if (filter) {
+                            /* the point's own rho interval over the slice */
+                            const float f0 = x * c0 + y * s0;
+                            const float f1 = x * c1 + y * s1;
+                            const float lo = fminf(f0, f1);
+                            float hi = fmaxf(f0, f1);
+                            const float tol = 1e-3f * (x + y) + 1e-3f;
+                            if (c0 * y - s0 * x >= -tol && x * s1 - y * c1 >= -tol)
+                                hi = fmaxf(hi, x + y);
+                            keep = (lo * a.irho - 3.0f <= hi_bin) &&
+                                   (hi * a.irho + 3.0f >= lo_bin);
+                        }
+                    }
+                    const unsigned bm = __ballot_sync(FULL, keep);
+                    if (bm) {
+                        const int leader = __ffs(bm) - 1;
+                        int base = 0;
+                        if (lane == leader)
+                            base = atomicAdd(&sm.nconv[cnt_i], __popc(bm));
+                        base = __shfl_sync(FULL, base, leader);
+                        if (keep) {
+                            const int q = base + __popc(bm & ((1u << lane) - 1u));
+                            cv[(q >> 1) * 4 + (q & 1)] = x;
+                            cv[(q >> 1) * 4 + 2 + (q & 1)] = y;
+                        }
+                    }
+                }
+                __syncthreads();
+                const int n = sm.nconv[cnt_i];
+                if (tid == 0) {
+                    /* counter of batch b + 2: last read (for batch b - 1)
+                     * before this step's barrier by every thread */
+                    sm.nconv[(b + 2) % 3] = 0;
+                    produce(sm, slot, a.pts, r, pos);
+                }
+                /* vote: each warp takes pairs of points, 2 pairs per step */
+                const int npairs = n >> 1;
+                const float4 *c4 = sm.conv[slot];
+                int p = warp;
+                for (; p + nwarps < npairs; p += 2 * nwarps) {
+                    const float4 qa = c4[p];
+                    const float4 qb = c4[p + nwarps];
+                    int ra0, ra1, rb0, rb1;
+                    rho_pair<UNIT>(qa, cc, ss, ii, ra0, ra1);
+                    rho_pair<UNIT>(qb, cc, ss, ii, rb0, rb1);
+                    VOTE(ra0);
+                    VOTE(ra1);
+                    VOTE(rb0);
+                    VOTE(rb1);
+                }
+                if (p < npairs) {
+                    const float4 qa = c4[p];
+                    int ra0, ra1;
+                    rho_pair<UNIT>(qa, cc, ss, ii, ra0, ra1);
+                    VOTE(ra0);
+                    VOTE(ra1);
+                }
+                if ((n & 1) && warp == nwarps - 1) {
+                    const float4 qa = c4[npairs];
+                    const int ra = rho_of<UNIT>(qa.x, qa.z, c, s, a.irho);
+                    VOTE(ra);
                 }
             }
+            __syncthreads();
+        }
+
+        /* store the block: row i of the window -> acc[(w0 + i) * Tp + k0 ..] */
+        int4 *dst4 = reinterpret_cast<int4 *>(a.acc);
+        const int4 *src4 = reinterpret_cast<const int4 *>(s_acc);
+        const int tp4 = a.Tp >> 2;
+        for (int i = tid; i < rows * (HL_SLICE / 4); i += nthr) {
+            const int rr = i >> 3, q = i & 7;
+            dst4[(size_t)(w0 + rr) * tp4 + (k0 >> 2) + q] = src4[i];
         }
         __syncthreads();
     }
-
-    /* store the block: row r of the window -> acc[(w0 + r) * Tp + k0 ..] */
-    int4 *dst4 = reinterpret_cast<int4 *>(a.acc);
-    const int4 *src4 = reinterpret_cast<const int4 *>(s_acc);
-    const int tp4 = a.Tp >> 2;
-    for (int i = tid; i < rows * (HL_SLICE / 4); i += blockDim.x) {
-        int r = i >> 3, q = i & 7;
-        dst4[(size_t)(w0 + r) * tp4 + (k0 >> 2) + q] = src4[i];
-    }
 }
 
-size_t hl_vote_smem_bytes(int win_rows)
+cudaError_t hl_launch_vote(const hl_vote_args *a, int threads, int grid,
+                           cudaStream_t s)
 {
-    return (size_t)win_rows * HL_SLICE * sizeof(int);
-}
-
-cudaError_t hl_launch_vote(const hl_vote_args *a, int threads, cudaStream_t s)
-{
-    dim3 grid(a->Tp / HL_SLICE, a->nwin);
-    size_t smem = hl_vote_smem_bytes(a->win_rows);
+    const size_t smem = hl_vote_smem_bytes(a->win_rows);
     cudaError_t e;
     if (a->irho == 1.0f) {
         e = cudaFuncSetAttribute(hl_vote_kernel<true>,
@@ -182,6 +507,11 @@ cudaError_t hl_launch_vote(const hl_vote_args *a, int threads, cudaStream_t s)
     return cudaGetLastError();
 }
 
+size_t hl_vote_points_smem_bytes(int win_rows)
+{
+    return (size_t)win_rows * HL_SLICE * sizeof(int);
+}
+
 /* Voting over an interleaved int (x, y) list (the guidingset path,
  * okano_3_0/HoughLine.cu:133-165).  No tile order here, so every window
  * reads every point; the per-vote row test keeps it exact. */
@@ -191,7 +521,7 @@ hl_vote_points_kernel(const int2 *xy, int n, const float *cosv,
                       const float *sinv, int T, int Tp, int rho_min, int R,
                       int win_rows, float irho, int32_t *acc)
 {
-    extern __shared__ __align__(16) int s_acc[];
+    extern __shared__ __align__(16) int s_pacc[];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nwarps = blockDim.x >> 5;
     const int k0 = blockIdx.x * HL_SLICE, k = k0 + lane;
@@ -201,7 +531,7 @@ hl_vote_points_kernel(const int2 *xy, int n, const float *cosv,
     const int rows = min(win_rows, R - w0);
     const int row_base = rho_min + w0;
     for (int i = tid; i < rows * HL_SLICE; i += blockDim.x)
-        s_acc[i] = 0;
+        s_pacc[i] = 0;
     __syncthreads();
     for (int b = warp * 32; b < n; b += nwarps * 32) {
         const int i = b + lane;
@@ -213,12 +543,12 @@ hl_vote_points_kernel(const int2 *xy, int n, const float *cosv,
             const float y = __shfl_sync(FULL, yf, j);
             const int row = rho_of<UNIT>(x, y, c, s, irho) - row_base;
             if (kvalid && (unsigned)row < (unsigned)rows)
-                atomicAdd(&s_acc[row * HL_SLICE + lane], 1);
+                atomicAdd(&s_pacc[row * HL_SLICE + lane], 1);
         }
     }
     __syncthreads();
     int4 *dst4 = reinterpret_cast<int4 *>(acc);
-    const int4 *src4 = reinterpret_cast<const int4 *>(s_acc);
+    const int4 *src4 = reinterpret_cast<const int4 *>(s_pacc);
     const int tp4 = Tp >> 2;
     for (int i = tid; i < rows * (HL_SLICE / 4); i += blockDim.x) {
         int r = i >> 3, q = i & 7;
@@ -233,7 +563,7 @@ cudaError_t hl_launch_vote_points(const int *xy, int n, const float *cosv,
                                   cudaStream_t s)
 {
     dim3 grid(Tp / HL_SLICE, nwin);
-    size_t smem = hl_vote_smem_bytes(win_rows);
+    size_t smem = hl_vote_points_smem_bytes(win_rows);
     cudaError_t e;
     if (irho == 1.0f) {
         e = cudaFuncSetAttribute(hl_vote_points_kernel<true>,

@@ -95,7 +95,7 @@ def test_full_4096_against_golden_and_oracle(hl_mod):
     assert [l.astuple() for l in lines] == wl
 
 
-@pytest.mark.parametrize("rows,threads", [(64, 256), (200, 512), (1000, 1024), (1536, 512)])
+@pytest.mark.parametrize("rows,threads", [(64, 256), (200, 512), (1000, 1024), (1400, 512)])
 def test_vote_shapes_agree(hl_mod, rows, threads):
     """Rho windows narrower than the rho range exercise the tile filter."""
     HoughLine, Image = hl_mod
