@@ -3,10 +3,9 @@
  *
  * Vote rule (okano_3_0/HoughLine.cu:86-130): an edge point (x, y) adds one
  * to bin (k, trunc(fl(x*cos_k) + fl(y*sin_k))) for every k.  The products and
- * the sum are rounded separately (no FMA contraction: packed mul.rn.f32x2 /
- * add.rn.f32x2, each rounded on its own), the float is truncated toward zero
- * (the reference's +-0.5 step after the (int) cast is a no-op), and
- * cos_k/sin_k come from the GPU-evaluated table.
+ * the sum are rounded separately (__fmul_rn / __fadd_rn: no FMA contraction),
+ * the float is truncated toward zero (the reference's +-0.5 step after the
+ * (int) cast is a no-op), and cos_k/sin_k come from the GPU-evaluated table.
  *
  * Work decomposition.  A work item is one (theta slice, rho window) block of
  * the accumulator, held in shared memory as acc[row][lane]: 32 thetas (one
@@ -29,8 +28,9 @@
  *
  * Bounds: the rho row of every vote is checked against the window (a point
  * whose interval straddles the window votes only its in-window lanes), lanes
- * beyond T never vote, mbarrier waits are bounded (status bit on time-out,
- * then every thread leaves together).
+ * beyond T never vote, mbarrier waits are bounded (a time-out sets a status
+ * bit that the host reads with the result; the CTA keeps the same barrier
+ * sequence and stops taking items).
  */
 #include "hl_internal.h"
 
@@ -51,50 +51,14 @@ __device__ __forceinline__ int rho_of(float x, float y, float c, float s,
     return __float2int_rz(__fadd_rn(a, b));
 }
 
-/* ---- packed f32x2 arithmetic (sm_100+), each operation rounded alone ---- */
-__device__ __forceinline__ unsigned long long pk2(float a, float b)
-{
-    unsigned long long r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-__device__ __forceinline__ void up2(unsigned long long v, float &a, float &b)
-{
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-}
-__device__ __forceinline__ unsigned long long mul2(unsigned long long a,
-                                                   unsigned long long b)
-{
-    unsigned long long r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ unsigned long long add2(unsigned long long a,
-                                                   unsigned long long b)
-{
-    unsigned long long r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-
 /* rho values of the two points (x0, y0), (x1, y1) of a pair record
  * {x0, x1, y0, y1} for this lane's (c, s) */
 template <bool UNIT>
-__device__ __forceinline__ void rho_pair(const float4 &q, unsigned long long cc,
-                                         unsigned long long ss,
-                                         unsigned long long ii, int &r0,
-                                         int &r1)
+__device__ __forceinline__ void rho_pair(const float4 &q, float c, float s,
+                                         float irho, int &r0, int &r1)
 {
-    unsigned long long a = mul2(pk2(q.x, q.y), cc);
-    unsigned long long b = mul2(pk2(q.z, q.w), ss);
-    if (!UNIT) {
-        a = mul2(a, ii);
-        b = mul2(b, ii);
-    }
-    float v0, v1;
-    up2(add2(a, b), v0, v1);
-    r0 = __float2int_rz(v0);
-    r1 = __float2int_rz(v1);
+    r0 = rho_of<UNIT>(q.x, q.z, c, s, irho);
+    r1 = rho_of<UNIT>(q.y, q.w, c, s, irho);
 }
 
 /* ---- mbarrier + bulk copy ---------------------------------------------- */
@@ -259,7 +223,6 @@ hl_vote_kernel(hl_vote_args a)
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nthr = blockDim.x, nwarps = nthr >> 5;
     const int nslices = a.Tp / HL_SLICE;
-    const unsigned long long ii = pk2(a.irho, a.irho);
 
     if (tid == 0) {
         mbar_init(&sm.mbar[0], 1);
@@ -293,7 +256,6 @@ hl_vote_kernel(hl_vote_args a)
         const float lo_bin = (float)row_base;
         const float hi_bin = (float)(row_base + rows - 1);
         const bool filter = a.nwin > 1;
-        const unsigned long long cc = pk2(c, c), ss = pk2(s, s);
         int *accl = s_acc + lane;
 /* one vote of rho bin r, if it lies in the window and the lane has a theta */
 #define VOTE(r)                                                     \
@@ -449,8 +411,8 @@ hl_vote_kernel(hl_vote_args a)
                     const float4 qa = c4[p];
                     const float4 qb = c4[p + nwarps];
                     int ra0, ra1, rb0, rb1;
-                    rho_pair<UNIT>(qa, cc, ss, ii, ra0, ra1);
-                    rho_pair<UNIT>(qb, cc, ss, ii, rb0, rb1);
+                    rho_pair<UNIT>(qa, c, s, a.irho, ra0, ra1);
+                    rho_pair<UNIT>(qb, c, s, a.irho, rb0, rb1);
                     VOTE(ra0);
                     VOTE(ra1);
                     VOTE(rb0);
@@ -459,7 +421,7 @@ hl_vote_kernel(hl_vote_args a)
                 if (p < npairs) {
                     const float4 qa = c4[p];
                     int ra0, ra1;
-                    rho_pair<UNIT>(qa, cc, ss, ii, ra0, ra1);
+                    rho_pair<UNIT>(qa, c, s, a.irho, ra0, ra1);
                     VOTE(ra0);
                     VOTE(ra1);
                 }
