@@ -123,6 +123,20 @@ int hl_plain_points(hl_handle *h, const int *xy_dev, int n, int *linesmax,
 int hl_compact(hl_handle *h, const hl_image_desc *img, uint32_t *pts_dev,
                int *tile_off_dev, int *count_dev, void *stream);
 
+/* Stage (a) without allocating: the same compaction as hl_compact, for
+ * callers that may not call cudaMalloc after start-up (their device memory is
+ * owned by another memory manager or fixed by a budget, or an allocation
+ * would stall a latency-bound loop).  No counterpart in the reference.  The
+ * look-back scratch lives in a static device array of this library (about
+ * 512 KiB on every device that loads it, kept until exit), so the ROI may
+ * cover at most 65536 tiles of 128 x 32 pixels (HL_OP_OVERFLOW beyond).  The
+ * first call on a device looks up that array's device address and should
+ * come before any stream capture.  No handle is needed; every call shares
+ * the one array and clears what it uses, so calls that overlap on the GPU
+ * (two streams at once) race.  Asynchronous on `stream`. */
+int hl_compact_noalloc(const hl_image_desc *img, uint32_t *pts_dev,
+                       int *tile_off_dev, int *count_dev, void *stream);
+
 /* Stages (a)+(b): the int32 accumulator of the ROI in the tight layout
  * acc[(rho - rho_min) * T + k] (R * T ints, DEVICE), for parity checks. */
 int hl_accumulator(hl_handle *h, const hl_image_desc *img, int32_t *acc_dev,

@@ -42,7 +42,8 @@ def _run(cmd: list[str]) -> None:
         raise RuntimeError(f"build step failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
 
 
-CU_SOURCES = ["hl_stage_a.cu", "hl_vote.cu", "hl_stage_c.cu", "hl_stage_f.cu"]
+CU_SOURCES = ["hl_stage_a.cu", "hl_vote.cu", "hl_stage_c.cu", "hl_stage_f.cu",
+              "hl_noalloc.cu"]
 CXX_SOURCES = ["hl_api.cpp", "HoughLine.cpp", "Image.cpp"]
 C_SOURCES = ["synth.c"]
 

@@ -73,6 +73,9 @@ typedef struct hl_vote_args {
     unsigned work_base;       /* its value at launch */
 } hl_vote_args;
 
+/* Tiles the allocation-free compaction entry point can serve. */
+#define HL_NOALLOC_MAX_TILES 65536
+
 /* Vote-kernel staging: points per TMA batch and pieces per batch. */
 #define HL_VOTE_CHUNK 1024
 #define HL_VOTE_PIECES 16
