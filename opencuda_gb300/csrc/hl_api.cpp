@@ -505,7 +505,7 @@ static int run_ab(hl_handle *h, const hl_roi &roi, const hl_geom &g,
     ca.status = h->d_counters + 1;
     prof_mark(h, 0, s);
     CK(hl_launch_compact(&ca, s));
-    h->ticket_base += (unsigned)ntiles;
+    h->ticket_base += (unsigned)((ntiles + HL_COMPACT_GROUP - 1) / HL_COMPACT_GROUP);
     (*launches)++;
     prof_mark(h, 1, s);
 
@@ -725,7 +725,7 @@ extern "C" int hl_compact(hl_handle *h, const hl_image_desc *img,
     ca.count = count_dev;
     ca.status = h->d_counters + 1;
     CK(hl_launch_compact(&ca, s));
-    h->ticket_base += (unsigned)ntiles;
+    h->ticket_base += (unsigned)((ntiles + HL_COMPACT_GROUP - 1) / HL_COMPACT_GROUP);
     h->last_launches = 1;
     return HL_NO_ERROR;
 }

@@ -15,6 +15,8 @@
 #define HL_TILE_W 128
 #define HL_TILE_H 32
 #define HL_COMPACT_THREADS 256
+/* Tiles per compaction CTA (one look-back per group). */
+#define HL_COMPACT_GROUP 4
 /* Theta slice = one warp: lane i owns theta k0 + i. */
 #define HL_SLICE 32
 

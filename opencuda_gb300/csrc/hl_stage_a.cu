@@ -3,9 +3,10 @@
  *
  * Compaction replaces the flag / ScanArray / scatter chain of
  * ImgConvert::imgConvertToCst (okano_3_0/ImgConvert.cu:142-353,
- * okano_3_0/ScanArray.cu:1351+) with ONE pass: every CTA reads one
- * 128 x 32 tile with 16-byte vector loads, counts its 255-pixels, obtains the
- * tile's exclusive prefix by decoupled look-back over its predecessors'
+ * okano_3_0/ScanArray.cu:1351+) with ONE pass: every CTA reads a group of
+ * four 128 x 32 tiles with 16-byte vector loads (all four issued before any
+ * is used), counts their 255-pixels with one packed block scan, obtains the
+ * group's exclusive prefix by decoupled look-back over its predecessors'
  * published aggregates, and scatters packed coordinates.  The predicate is
  * the vote kernel's `pixel == 255` (okano_3_0/HoughLine.cu:125), not
  * ImgConvert's `>= 128`.
@@ -143,87 +144,125 @@ __device__ int lookback(unsigned long long *state, int tile, int total,
     return excl;
 }
 
+/* Tiles per CTA: one look-back and four 16-byte loads in flight per thread
+ * for every 16 KB of image. */
+#define CT_GROUP HL_COMPACT_GROUP
+
 __global__ void __launch_bounds__(HL_COMPACT_THREADS)
 hl_compact_kernel(hl_compact_args a)
 {
-    __shared__ int s_tile;
-    __shared__ int s_wsum[HL_COMPACT_THREADS / 32];
-    __shared__ int s_base;
+    __shared__ int s_grp;
+    __shared__ unsigned long long s_wsum[HL_COMPACT_THREADS / 32];
+    __shared__ int s_tbase[CT_GROUP];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int ngroups = (a.ntiles + CT_GROUP - 1) / CT_GROUP;
 
-    /* Tiles are taken in ticket order, so every predecessor of a tile is
-     * already resident when the tile looks back: the waits always end. */
+    /* Groups are taken in ticket order, so every predecessor of a group is
+     * already resident when the group looks back: the waits always end. */
     if (tid == 0)
-        s_tile = (int)(atomicAdd(a.ticket, 1u) - a.ticket_base);
+        s_grp = (int)(atomicAdd(a.ticket, 1u) - a.ticket_base);
     __syncthreads();
-    const int tile = s_tile;
-    if (tile < 0 || tile >= a.ntiles)
+    const int grp = s_grp;
+    if (grp < 0 || grp >= ngroups)
         return;
-    const int tx = tile % a.tiles_x, ty = tile / a.tiles_x;
     const int r = tid >> 3, ch = tid & 7;
-    const int y = ty * HL_TILE_H + r;
-    const int x0 = tx * HL_TILE_W + ch * 16;
 
-    uint32_t m = 0;
-    if (y < a.roi.h && x0 < a.roi.w) {
-        const uint8_t *p = a.roi.base + (size_t)y * (size_t)a.roi.pitch + x0;
-        if (x0 + 16 <= a.roi.w && (((uintptr_t)p) & 15u) == 0) {
-            uint4 v = __ldcs((const uint4 *)p);
-            m = eq255x4(v.x) | (eq255x4(v.y) << 4) | (eq255x4(v.z) << 8) |
-                (eq255x4(v.w) << 12);
-        } else {
-            int lim = min(16, a.roi.w - x0);
-            for (int i = 0; i < lim; i++)
-                m |= (uint32_t)(p[i] == 255) << i;
-        }
+    /* all loads first */
+    uint4 v[CT_GROUP];
+    int yq[CT_GROUP], xq[CT_GROUP];
+    bool vec[CT_GROUP], any[CT_GROUP];
+#pragma unroll
+    for (int q = 0; q < CT_GROUP; q++) {
+        const int tile = grp * CT_GROUP + q;
+        const int tx = tile % a.tiles_x, ty = tile / a.tiles_x;
+        yq[q] = ty * HL_TILE_H + r;
+        xq[q] = tx * HL_TILE_W + ch * 16;
+        any[q] = tile < a.ntiles && yq[q] < a.roi.h && xq[q] < a.roi.w;
+        const uint8_t *p = a.roi.base + (size_t)yq[q] * (size_t)a.roi.pitch + xq[q];
+        vec[q] = any[q] && xq[q] + 16 <= a.roi.w && (((uintptr_t)p) & 15u) == 0;
+        v[q] = vec[q] ? __ldcs((const uint4 *)p) : make_uint4(0, 0, 0, 0);
     }
-    const int cnt = __popc(m);
-    int incl = cnt;
+    uint32_t m[CT_GROUP];
+    unsigned long long cnt4 = 0;   /* four 16-bit counts, tile q in bits 16q */
+#pragma unroll
+    for (int q = 0; q < CT_GROUP; q++) {
+        uint32_t mm = 0;
+        if (vec[q]) {
+            mm = eq255x4(v[q].x) | (eq255x4(v[q].y) << 4) |
+                 (eq255x4(v[q].z) << 8) | (eq255x4(v[q].w) << 12);
+        } else if (any[q]) {
+            const uint8_t *p = a.roi.base + (size_t)yq[q] * (size_t)a.roi.pitch + xq[q];
+            const int lim = min(16, a.roi.w - xq[q]);
+            for (int i = 0; i < lim; i++)
+                mm |= (uint32_t)(p[i] == 255) << i;
+        }
+        m[q] = mm;
+        cnt4 |= (unsigned long long)__popc(mm) << (16 * q);
+    }
+    /* block scan of the packed counts (no field exceeds 4096) */
+    unsigned long long incl = cnt4;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        int v = __shfl_up_sync(FULL, incl, o);
+        const unsigned long long t = __shfl_up_sync(FULL, incl, o);
         if (lane >= o)
-            incl += v;
+            incl += t;
     }
     if (lane == 31)
         s_wsum[warp] = incl;
     __syncthreads();
     if (warp == 0) {
         const int nw = HL_COMPACT_THREADS / 32;
-        int ws = lane < nw ? s_wsum[lane] : 0;
-        int wi = ws;
+        const unsigned long long ws = lane < nw ? s_wsum[lane] : 0ull;
+        unsigned long long wi = ws;
 #pragma unroll
         for (int o = 1; o < nw; o <<= 1) {
-            int v = __shfl_up_sync(FULL, wi, o);
+            const unsigned long long t = __shfl_up_sync(FULL, wi, o);
             if (lane >= o)
-                wi += v;
+                wi += t;
         }
-        const int total = __shfl_sync(FULL, wi, nw - 1);
+        const unsigned long long tot4 = __shfl_sync(FULL, wi, nw - 1);
         if (lane < nw)
             s_wsum[lane] = wi - ws;
-        const int excl = lookback(a.tile_state, tile, total, a.epoch, a.status);
+        int total = 0;
+#pragma unroll
+        for (int q = 0; q < CT_GROUP; q++)
+            total += (int)((tot4 >> (16 * q)) & 0xffffu);
+        const int excl = lookback(a.tile_state, grp, total, a.epoch, a.status);
         if (lane == 0) {
-            s_base = excl;
-            a.tile_off[tile] = excl;
-            if (tile == a.ntiles - 1) {
-                a.tile_off[a.ntiles] = excl + total;
-                *a.count = excl + total;
+            int run = excl;
+#pragma unroll
+            for (int q = 0; q < CT_GROUP; q++) {
+                const int tile = grp * CT_GROUP + q;
+                s_tbase[q] = run;
+                if (tile < a.ntiles)
+                    a.tile_off[tile] = run;
+                run += (int)((tot4 >> (16 * q)) & 0xffffu);
+            }
+            if (grp == ngroups - 1) {
+                a.tile_off[a.ntiles] = run;
+                *a.count = run;
             }
         }
     }
     __syncthreads();
-    int pos = s_base + s_wsum[warp] + incl - cnt;
-    const uint32_t yy = (uint32_t)y << 16;
-    while (m) {
-        int b = __ffs(m) - 1;
-        m &= m - 1;
-        a.pts[pos++] = (uint32_t)(x0 + b) | yy;
+    const unsigned long long ex4 = s_wsum[warp] + incl - cnt4;
+#pragma unroll
+    for (int q = 0; q < CT_GROUP; q++) {
+        uint32_t mm = m[q];
+        int pos = s_tbase[q] + (int)((ex4 >> (16 * q)) & 0xffffu);
+        const uint32_t yy = (uint32_t)yq[q] << 16;
+        while (mm) {
+            const int bb = __ffs(mm) - 1;
+            mm &= mm - 1;
+            a.pts[pos++] = (uint32_t)(xq[q] + bb) | yy;
+        }
     }
 }
 
 cudaError_t hl_launch_compact(const hl_compact_args *a, cudaStream_t s)
 {
-    hl_compact_kernel<<<a->ntiles, HL_COMPACT_THREADS, 0, s>>>(*a);
+    const int ngroups = (a->ntiles + CT_GROUP - 1) / CT_GROUP;
+    hl_compact_kernel<<<ngroups, HL_COMPACT_THREADS, 0, s>>>(*a);
     return cudaGetLastError();
 }
 

@@ -9,10 +9,11 @@
  *                        appended as 64-bit keys (votes << 32 | ~index) with
  *                        warp-aggregated atomics (HBM-bound: one read of acc);
  *   hl_finalize_kernel -- one CTA: top-M selection (MSD radix select when the
- *                        peaks exceed one chunk), bitonic sort of the chunk,
- *                        the reference's float decode, and its greedy merge
- *                        resolved in parallel; writes min(survivors,
- *                        linesmax) LineParam records.
+ *                        peaks exceed one 1024-key chunk), rank sort of the
+ *                        chunk (keys are unique), the reference's float
+ *                        decode, the pairwise suppression bitmask, and the
+ *                        greedy merge as one warp's walk over that bitmask;
+ *                        writes min(survivors, linesmax) LineParam records.
  * Ranking is canonical: votes descending, then the reference raster index
  * (rho-major, theta-minor) ascending -- the reference's Shell sort
  * (:853-873) is unstable, so ties are ordered by index here.
@@ -106,6 +107,7 @@ cudaError_t hl_launch_peaks(const hl_peak_args *a, cudaStream_t s)
 
 struct FinSmem {
     unsigned long long keys[FIN_CHUNK];
+    unsigned long long sorted[FIN_CHUNK];
     float ang[FIN_CHUNK];
     int dist[FIN_CHUNK];
     int votes[FIN_CHUNK];
@@ -220,31 +222,25 @@ hl_finalize_kernel(hl_final_args a, float scale)
             }
             __syncthreads();
         }
-        /* bitonic sort, descending, over P = next power of two >= m */
-        int P = 2;
-        while (P < m)
-            P <<= 1;
-        for (int i = m + tid; i < P; i += blockDim.x)
-            sm.keys[i] = 0ull;
+        /* descending order by rank: keys are unique (the bin index is part of
+         * every key), so a key's rank is the number of larger keys; every
+         * thread ranks its keys against all m with broadcast reads, no
+         * barrier inside */
         __syncthreads();
-        for (int size = 2; size <= P; size <<= 1) {
-            for (int stride = size >> 1; stride > 0; stride >>= 1) {
-                for (int i = tid; i < P; i += blockDim.x) {
-                    int j = i ^ stride;
-                    if (j > i) {
-                        bool desc = (i & size) == 0;
-                        unsigned long long x = sm.keys[i], y = sm.keys[j];
-                        if ((x < y) == desc) {
-                            sm.keys[i] = y;
-                            sm.keys[j] = x;
-                        }
-                    }
-                }
-                __syncthreads();
-            }
+        for (int i = tid; i < m; i += blockDim.x) {
+            const unsigned long long ki = sm.keys[i];
+            int rank = 0;
+            int j = 0;
+            for (; j + 4 <= m; j += 4)
+                rank += (sm.keys[j] > ki) + (sm.keys[j + 1] > ki) +
+                        (sm.keys[j + 2] > ki) + (sm.keys[j + 3] > ki);
+            for (; j < m; j++)
+                rank += sm.keys[j] > ki;
+            sm.sorted[rank] = ki;
         }
+        __syncthreads();
         taken += m;
-        upper = sm.keys[m - 1];
+        upper = sm.sorted[m - 1];
 
         /* decode; drop candidates similar to a survivor of an earlier chunk */
         const int W = (m + 31) >> 5;
@@ -254,7 +250,7 @@ hl_finalize_kernel(hl_final_args a, float scale)
         for (int i = tid; i < m; i += blockDim.x) {
             float ang;
             int dist, vts;
-            decode(sm.keys[i], a.T, a.rho_min, off, scale, a.detheta, &ang,
+            decode(sm.sorted[i], a.T, a.rho_min, off, scale, a.detheta, &ang,
                    &dist, &vts);
             sm.ang[i] = ang;
             sm.dist[i] = dist;
@@ -277,28 +273,27 @@ hl_finalize_kernel(hl_final_args a, float scale)
         }
         __syncthreads();
         /* suppression bitmask: bit j of mask[i] <=> i < j and similar(i, j).
-         * Warp w owns the 32 candidates j of word w: it walks the rows i
-         * below them (broadcast shared loads) and ballots one word per row;
-         * rows at or past the word are zero. */
-        {
-            const int wd = tid >> 5, lane = tid & 31;
-            if (wd < W) {
-                const int j = (wd << 5) + lane;
-                const bool jv = j < m;
-                const float aj = jv ? sm.ang[j] : 0.f;
-                const int dj = jv ? sm.dist[j] : 0;
-                const int ilim = min(m, (wd << 5) + 32);
-                for (int i = 0; i < ilim; i++) {
-                    const bool hit = jv && j > i &&
-                                     similar(sm.ang[i], sm.dist[i], aj, dj,
+         * One thread per (row i, word w), word-major so a warp's threads share
+         * w and read the word's 32 candidates with broadcast loads; the 32
+         * tests of a word are independent (no serial chain). */
+        for (int e = tid; e < m * W; e += blockDim.x) {
+            const int wd = e / m, i = e - wd * m;
+            const int j0 = wd << 5;
+            unsigned bits = 0u;
+            if (j0 + 31 > i) {
+                const float ai = sm.ang[i];
+                const int di = sm.dist[i];
+                const int jn = min(32, m - j0);
+#pragma unroll 8
+                for (int b = 0; b < 32; b++) {
+                    const int j = j0 + b;
+                    const bool hit = b < jn && j > i &&
+                                     similar(ai, di, sm.ang[j], sm.dist[j],
                                              a.thresdis, a.thresang);
-                    const unsigned bits = __ballot_sync(FULL, hit);
-                    if (lane == 0)
-                        sm.mask[i][wd] = bits;
+                    bits |= (unsigned)hit << b;
                 }
-                for (int i = ilim + lane; i < m; i += 32)
-                    sm.mask[i][wd] = 0u;
             }
+            sm.mask[i][wd] = bits;
         }
         __syncthreads();
         /* the greedy pass of okano_3_0/HoughLine.cu:900-927 over the chunk:

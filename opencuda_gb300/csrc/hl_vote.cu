@@ -26,11 +26,17 @@
  * coalesced 128-byte rows into acc[R][Tp]; every bin is written exactly once,
  * so the global accumulator needs no clearing.
  *
- * Bounds: the rho row of every vote is checked against the window (a point
- * whose interval straddles the window votes only its in-window lanes), lanes
- * beyond T never vote, mbarrier waits are bounded (a time-out sets a status
- * bit that the host reads with the result; the CTA keeps the same barrier
- * sequence and stops taking items).
+ * Bounds: a point votes without per-vote checks only when its rho interval
+ * over the slice lies, with three bins of slack, inside the window; a point
+ * that straddles the window checks every vote (predicated red.shared), lanes
+ * beyond T add into a private sink word, and mbarrier waits are bounded (a
+ * time-out sets a status bit that the host reads with the result; the CTA
+ * keeps the same barrier sequence and stops taking items).
+ *
+ * Instruction budget per point and warp on the interior path: one shared
+ * load per two points, two multiplies, one add, one float->int truncation,
+ * one address multiply-add and one red.shared -- the truncation (16 per
+ * SM-clock) is the binding pipe, about half the measured red.shared rate.
  */
 #include "hl_internal.h"
 
@@ -148,7 +154,8 @@ struct VoteSmem {
     unsigned long long mbar[2];
     int item;
     int nruns;
-    int nconv[3];
+    int nin[3];                       /* interior points kept, per batch */
+    int nst[3];                       /* straddling points kept, per batch */
     int np[2];
     int total[2];
     int timeout;
@@ -159,8 +166,11 @@ struct VoteSmem {
     unsigned mask[HL_VOTE_TG / 32];
     int run_s[HL_VOTE_TG / 2 + 1];
     int run_e[HL_VOTE_TG / 2 + 1];
+    int sink[HL_SLICE];               /* votes of lanes past the last theta */
     alignas(16) unsigned raw[2][RAWCAP];
-    alignas(16) float4 conv[2][HL_VOTE_CHUNK / 2 + 1];
+    /* unpacked points as pair records {x0, x1, y0, y1} */
+    alignas(16) float4 cin[2][HL_VOTE_CHUNK / 2 + 1];
+    alignas(16) float4 cst[2][HL_VOTE_CHUNK / 2 + 1];
 };
 
 #define VOTE_FIXED ((sizeof(VoteSmem) + 127) / 128 * 128)
@@ -168,6 +178,20 @@ struct VoteSmem {
 size_t hl_vote_smem_bytes(int win_rows)
 {
     return VOTE_FIXED + (size_t)win_rows * HL_SLICE * sizeof(int);
+}
+
+/* one vote: shared-memory reduction without a returned value */
+__device__ __forceinline__ void red_smem(unsigned addr)
+{
+    asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(addr));
+}
+/* one vote if the window-relative row rl is below lim */
+__device__ __forceinline__ void red_smem_if(unsigned addr, unsigned rl,
+                                            unsigned lim)
+{
+    asm volatile("{ .reg .pred p; setp.lt.u32 p, %1, %2; "
+                 "@p red.shared.add.u32 [%0], 1; }" ::"r"(addr),
+                 "r"(rl), "r"(lim));
 }
 
 /* Producer (thread 0): form the next batch of up to HL_VOTE_CHUNK points from
@@ -213,6 +237,26 @@ __device__ void produce(VoteSmem &sm, int slot, const uint32_t *pts, int &r,
     }
 }
 
+/* append a point to a pair-record list with a warp-aggregated counter */
+__device__ __forceinline__ void append_point(bool take, float x, float y,
+                                             int *counter, float *list)
+{
+    const int lane = threadIdx.x & 31;
+    const unsigned bm = __ballot_sync(FULL, take);
+    if (!bm)
+        return;
+    const int leader = __ffs(bm) - 1;
+    int base = 0;
+    if (lane == leader)
+        base = atomicAdd(counter, __popc(bm));
+    base = __shfl_sync(FULL, base, leader);
+    if (take) {
+        const int q = base + __popc(bm & ((1u << lane) - 1u));
+        list[(q >> 1) * 4 + (q & 1)] = x;
+        list[(q >> 1) * 4 + 2 + (q & 1)] = y;
+    }
+}
+
 template <bool UNIT>
 __global__ void __launch_bounds__(1024, 1)
 hl_vote_kernel(hl_vote_args a)
@@ -228,7 +272,6 @@ hl_vote_kernel(hl_vote_args a)
         mbar_init(&sm.mbar[0], 1);
         mbar_init(&sm.mbar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        sm.nconv[0] = sm.nconv[1] = sm.nconv[2] = 0;
         sm.timeout = 0;
     }
     unsigned use0 = 0u, use1 = 0u;   /* completed phases of mbar[0], mbar[1] */
@@ -249,21 +292,21 @@ hl_vote_kernel(hl_vote_args a)
         const int w0 = win * a.win_rows;
         const int rows = min(a.win_rows, a.R - w0);
         const int row_base = a.rho_min + w0;       /* rho bin of local row 0 */
-        const unsigned lrows = (k < a.T) ? (unsigned)rows : 0u;
+        const bool kv = k < a.T;
+        const unsigned lrows = kv ? (unsigned)rows : 0u;
         const int klast = min(k0 + HL_SLICE - 1, a.T - 1);
         const float c0 = a.cosv[k0], s0 = a.sinv[k0];
         const float c1 = a.cosv[klast], s1 = a.sinv[klast];
         const float lo_bin = (float)row_base;
         const float hi_bin = (float)(row_base + rows - 1);
         const bool filter = a.nwin > 1;
-        int *accl = s_acc + lane;
-/* one vote of rho bin r, if it lies in the window and the lane has a theta */
-#define VOTE(r)                                                     \
-    do {                                                            \
-        const unsigned rl__ = (unsigned)((r) - row_base);           \
-        if (rl__ < lrows)                                           \
-            atomicAdd(accl + rl__ * HL_SLICE, 1);                   \
-    } while (0)
+        /* shared addresses: bin row rl of this lane is acc_l + rl * 128;
+         * interior votes index by rho directly (base folded), and lanes past
+         * the last theta vote into their own sink word */
+        const unsigned acc_l = smem_u32(s_acc) + 4u * lane;
+        const unsigned in_mul = kv ? 128u : 0u;
+        const unsigned in_base = kv ? acc_l - 128u * (unsigned)row_base
+                                    : smem_u32(&sm.sink[lane]);
 
         {
             int4 *z = reinterpret_cast<int4 *>(s_acc);
@@ -327,7 +370,8 @@ hl_vote_kernel(hl_vote_args a)
             /* stream the runs through shared memory, two batches in flight */
             int r = 0, pos = (sm.nruns > 0) ? sm.run_s[0] : 0;
             if (tid == 0) {
-                sm.nconv[0] = sm.nconv[1] = sm.nconv[2] = 0;
+                sm.nin[0] = sm.nin[1] = sm.nin[2] = 0;
+                sm.nst[0] = sm.nst[1] = sm.nst[2] = 0;
                 produce(sm, 0, a.pts, r, pos);
                 produce(sm, 1, a.pts, r, pos);
             }
@@ -350,13 +394,16 @@ hl_vote_kernel(hl_vote_args a)
                     sm.timeout = 1;
                     atomicOr(a.status, HL_ST_VOTE_TIMEOUT);
                 }
-                /* unpack + per-point window filter -> conv[slot] */
+                /* unpack; each point's own rho interval over the slice sorts
+                 * it into interior (every vote inside the window), straddling
+                 * (some inside) or dropped */
                 const int np = sm.np[slot];
-                const int cnt_i = b % 3;       /* kept-point counter of batch b */
-                float *cv = reinterpret_cast<float *>(sm.conv[slot]);
+                const int cnt_i = b % 3;
+                float *lin = reinterpret_cast<float *>(sm.cin[slot]);
+                float *lst = reinterpret_cast<float *>(sm.cst[slot]);
                 for (int j0 = 0; j0 < total; j0 += nthr) {
                     const int j = j0 + tid;
-                    bool keep = false;
+                    bool inner = false, strad = false;
                     float x = 0.f, y = 0.f;
                     if (j < total) {
                         int p = 0;
@@ -367,68 +414,76 @@ hl_vote_kernel(hl_vote_args a)
                                          (j - sm.pc_base[slot][p])];
                         x = (float)(u & 0xffffu);
                         y = (float)(u >> 16);
-                        keep = true;
-                        if (filter) {
-                            /* the point's own rho interval over the slice */
-                            const float f0 = x * c0 + y * s0;
-                            const float f1 = x * c1 + y * s1;
-                            const float lo = fminf(f0, f1);
-                            float hi = fmaxf(f0, f1);
-                            const float tol = 1e-3f * (x + y) + 1e-3f;
-                            if (c0 * y - s0 * x >= -tol && x * s1 - y * c1 >= -tol)
-                                hi = fmaxf(hi, x + y);
-                            keep = (lo * a.irho - 3.0f <= hi_bin) &&
-                                   (hi * a.irho + 3.0f >= lo_bin);
-                        }
+                        const float f0 = x * c0 + y * s0;
+                        const float f1 = x * c1 + y * s1;
+                        float lo = fminf(f0, f1), hi = fmaxf(f0, f1);
+                        const float tol = 1e-3f * (x + y) + 1e-3f;
+                        if (c0 * y - s0 * x >= -tol && x * s1 - y * c1 >= -tol)
+                            hi = fmaxf(hi, x + y);
+                        lo = lo * a.irho;
+                        hi = hi * a.irho;
+                        inner = (lo - 3.0f >= lo_bin) && (hi + 3.0f <= hi_bin);
+                        strad = !inner && (lo - 3.0f <= hi_bin) && (hi + 3.0f >= lo_bin);
                     }
-                    const unsigned bm = __ballot_sync(FULL, keep);
-                    if (bm) {
-                        const int leader = __ffs(bm) - 1;
-                        int base = 0;
-                        if (lane == leader)
-                            base = atomicAdd(&sm.nconv[cnt_i], __popc(bm));
-                        base = __shfl_sync(FULL, base, leader);
-                        if (keep) {
-                            const int q = base + __popc(bm & ((1u << lane) - 1u));
-                            cv[(q >> 1) * 4 + (q & 1)] = x;
-                            cv[(q >> 1) * 4 + 2 + (q & 1)] = y;
-                        }
-                    }
+                    append_point(inner, x, y, &sm.nin[cnt_i], lin);
+                    append_point(strad, x, y, &sm.nst[cnt_i], lst);
                 }
                 __syncthreads();
-                const int n = sm.nconv[cnt_i];
+                const int n_in = sm.nin[cnt_i], n_st = sm.nst[cnt_i];
                 if (tid == 0) {
-                    /* counter of batch b + 2: last read (for batch b - 1)
+                    /* counters of batch b + 2: last read (for batch b - 1)
                      * before this step's barrier by every thread */
-                    sm.nconv[(b + 2) % 3] = 0;
+                    sm.nin[(b + 2) % 3] = 0;
+                    sm.nst[(b + 2) % 3] = 0;
                     produce(sm, slot, a.pts, r, pos);
                 }
-                /* vote: each warp takes pairs of points, 2 pairs per step */
-                const int npairs = n >> 1;
-                const float4 *c4 = sm.conv[slot];
-                int p = warp;
-                for (; p + nwarps < npairs; p += 2 * nwarps) {
-                    const float4 qa = c4[p];
-                    const float4 qb = c4[p + nwarps];
-                    int ra0, ra1, rb0, rb1;
-                    rho_pair<UNIT>(qa, c, s, a.irho, ra0, ra1);
-                    rho_pair<UNIT>(qb, c, s, a.irho, rb0, rb1);
-                    VOTE(ra0);
-                    VOTE(ra1);
-                    VOTE(rb0);
-                    VOTE(rb1);
+                /* interior points: every vote lands in the window */
+                {
+                    const int npairs = n_in >> 1;
+                    const float4 *c4 = sm.cin[slot];
+                    int p = warp;
+                    for (; p + nwarps < npairs; p += 2 * nwarps) {
+                        const float4 qa = c4[p];
+                        const float4 qb = c4[p + nwarps];
+                        int r0, r1, r2, r3;
+                        rho_pair<UNIT>(qa, c, s, a.irho, r0, r1);
+                        rho_pair<UNIT>(qb, c, s, a.irho, r2, r3);
+                        red_smem((unsigned)r0 * in_mul + in_base);
+                        red_smem((unsigned)r1 * in_mul + in_base);
+                        red_smem((unsigned)r2 * in_mul + in_base);
+                        red_smem((unsigned)r3 * in_mul + in_base);
+                    }
+                    if (p < npairs) {
+                        int r0, r1;
+                        rho_pair<UNIT>(c4[p], c, s, a.irho, r0, r1);
+                        red_smem((unsigned)r0 * in_mul + in_base);
+                        red_smem((unsigned)r1 * in_mul + in_base);
+                    }
+                    if ((n_in & 1) && warp == nwarps - 1) {
+                        const float4 q = c4[npairs];
+                        const int r0 = rho_of<UNIT>(q.x, q.z, c, s, a.irho);
+                        red_smem((unsigned)r0 * in_mul + in_base);
+                    }
                 }
-                if (p < npairs) {
-                    const float4 qa = c4[p];
-                    int ra0, ra1;
-                    rho_pair<UNIT>(qa, c, s, a.irho, ra0, ra1);
-                    VOTE(ra0);
-                    VOTE(ra1);
-                }
-                if ((n & 1) && warp == nwarps - 1) {
-                    const float4 qa = c4[npairs];
-                    const int ra = rho_of<UNIT>(qa.x, qa.z, c, s, a.irho);
-                    VOTE(ra);
+                /* straddling points: only the lanes inside the window vote */
+                {
+                    const int npairs = n_st >> 1;
+                    const float4 *c4 = sm.cst[slot];
+                    int p = nwarps - 1 - warp;   /* other end of the warp range */
+                    for (; p < npairs; p += nwarps) {
+                        int r0, r1;
+                        rho_pair<UNIT>(c4[p], c, s, a.irho, r0, r1);
+                        const unsigned l0 = (unsigned)(r0 - row_base);
+                        const unsigned l1 = (unsigned)(r1 - row_base);
+                        red_smem_if(acc_l + 128u * l0, l0, lrows);
+                        red_smem_if(acc_l + 128u * l1, l1, lrows);
+                    }
+                    if ((n_st & 1) && warp == 0) {
+                        const float4 q = c4[npairs];
+                        const int r0 = rho_of<UNIT>(q.x, q.z, c, s, a.irho);
+                        const unsigned l0 = (unsigned)(r0 - row_base);
+                        red_smem_if(acc_l + 128u * l0, l0, lrows);
+                    }
                 }
             }
             __syncthreads();
