@@ -56,9 +56,10 @@ struct hl_handle {
 
     /* vote work items: heaviest-first order (cached per geometry) and the
      * persistent-CTA counter base */
-    int *order_dev;
+    int2 *order_dev;
     size_t cap_order;
-    int order_w, order_h, order_rows, order_R, order_T;
+    int order_w, order_h, order_rows, order_R, order_T, order_ctas;
+    int order_n, order_split;
     double order_derho;
     unsigned work_base;
 
@@ -314,8 +315,8 @@ extern "C" int hl_set_vote_shape(hl_handle *h, int window_rows, int threads)
         return HL_NULL_POINTER;
     if (window_rows < 0 || threads < 0 || threads > 1024 || (threads & 31))
         return HL_INVALID_DATA;
-    if (window_rows > 0 && hl_vote_smem_bytes(window_rows) > 226 * 1024)
-        return HL_INVALID_DATA;
+    if (window_rows > 65535 || (threads > 0 && threads < 64))
+        return HL_INVALID_DATA;   /* rows above the shared-memory limit are clamped */
     h->win_rows_override = window_rows;
     h->threads_override = threads;
     return HL_NO_ERROR;
@@ -326,21 +327,22 @@ extern "C" int hl_last_launch_count(const hl_handle *h)
     return h ? h->last_launches : 0;
 }
 
-/* Rho windows per theta slice: enough CTAs to give every SM two, never a
- * window above 1536 rows (192 KB of shared memory) nor below 64 rows. */
-/* Rho-window rows per work item: at most 1408 (one CTA of 1024 threads per
- * SM) and small enough that the heaviest window (the centre of the rho
- * range) is no more than about a third of one SM's share of the image. */
+/* Rho-window rows per work item: at most what one CTA holds next to its
+ * staging ring (one CTA of 1024 threads per SM), and enough windows that
+ * there are about two items per SM (the heaviest-first order then balances
+ * the tail), but no window below 256 rows. */
 static void vote_shape(const hl_handle *h, int R, int *rows, int *nwin,
                        int *threads)
 {
     const int slices = h->Tp / HL_SLICE;
+    const int maxr = hl_vote_max_rows();
     int nw;
     if (h->win_rows_override > 0) {
-        nw = (R + h->win_rows_override - 1) / h->win_rows_override;
+        nw = (R + std::min(h->win_rows_override, maxr) - 1) /
+             std::min(h->win_rows_override, maxr);
     } else {
-        int nmin = (R + 1407) / 1408;
-        int want = (3 * std::max(h->sms, 1) + slices - 1) / slices;
+        int nmin = (R + maxr - 1) / maxr;
+        int want = (2 * std::max(h->sms, 1) + slices - 1) / slices;
         int nmax = std::max(1, R / 256);
         nw = std::max(nmin, std::min(want, nmax));
     }
@@ -352,22 +354,30 @@ static void vote_shape(const hl_handle *h, int R, int *rows, int *nwin,
     *threads = h->threads_override > 0 ? h->threads_override : 1024;
 }
 
-/* Heaviest-first order of the (slice, window) items: the share of the ROI
- * whose rho at the slice's middle angle falls in the window, estimated on a
- * 64 x 64 grid of cell centres.  Cached per geometry. */
-static int item_order(hl_handle *h, int w, int hh, int rho_min, int R,
-                      int rows, int nwin, const int **dev_order)
+/* Work items of the vote kernel, heaviest first.  The weight of a (slice,
+ * window) block is the share of the ROI whose rho at the slice's middle
+ * angle falls in the window, estimated on a 64 x 64 grid of cell centres.
+ * A block heavier than a third of one CTA's fair share (total / ctas) is
+ * split into parts that each vote a contiguous share of the point stream
+ * (at most 16 parts).  Cached per geometry; *split tells whether any block
+ * was split (the accumulator must then start at zero). */
+static int vote_items(hl_handle *h, int w, int hh, int rho_min, int R,
+                      int rows, int nwin, int ctas, const int2 **dev_items,
+                      int *nitems_out, int *split)
 {
     const int slices = h->Tp / HL_SLICE;
-    const int nitems = slices * nwin;
+    const int nblocks = slices * nwin;
     if (h->order_dev && h->order_w == w && h->order_h == hh &&
         h->order_rows == rows && h->order_R == R && h->order_T == h->T &&
-        h->order_derho == h->p.derho) {
-        *dev_order = h->order_dev;
+        h->order_derho == h->p.derho && h->order_ctas == ctas) {
+        *dev_items = h->order_dev;
+        *nitems_out = h->order_n;
+        *split = h->order_split;
         return HL_NO_ERROR;
     }
-    std::vector<double> wt((size_t)nitems, 0.0);
+    std::vector<double> wt((size_t)nblocks, 0.0);
     const int G = 64;
+    double total = 0.0;
     for (int sl = 0; sl < slices; sl++) {
         const int k0 = sl * HL_SLICE;
         const int k1 = std::min(k0 + HL_SLICE, h->T) - 1;
@@ -382,18 +392,34 @@ static int item_order(hl_handle *h, int w, int hh, int rho_min, int R,
                 const int row = (int)floor((x * c + y * s) / h->p.derho) - rho_min;
                 const int wn = std::min(std::max(row / rows, 0), nwin - 1);
                 wt[(size_t)sl + (size_t)slices * wn] += (k1 - k0 + 1);
+                total += (k1 - k0 + 1);
             }
         }
     }
-    std::vector<int> ord((size_t)nitems);
-    for (int i = 0; i < nitems; i++)
-        ord[i] = i;
-    std::stable_sort(ord.begin(), ord.end(),
-                     [&](int a, int b) { return wt[a] > wt[b]; });
-    int rc = grow((void **)&h->order_dev, &h->cap_order, sizeof(int) * (size_t)nitems);
+    const double cap = total / (3.0 * std::max(ctas, 1));
+    struct part_t { double wt; int blk, part, nparts; };
+    std::vector<part_t> parts;
+    parts.reserve((size_t)nblocks * 2);
+    int any_split = 0;
+    for (int b = 0; b < nblocks; b++) {
+        int np = 1;
+        if (cap > 0.0 && wt[b] > cap)
+            np = std::min(16, (int)ceil(wt[b] / cap));
+        if (np > 1)
+            any_split = 1;
+        for (int q = 0; q < np; q++)
+            parts.push_back({wt[b] / np, b, q, np});
+    }
+    std::stable_sort(parts.begin(), parts.end(),
+                     [](const part_t &a, const part_t &b) { return a.wt > b.wt; });
+    const int n = (int)parts.size();
+    std::vector<int2> items((size_t)n);
+    for (int i = 0; i < n; i++)
+        items[i] = make_int2(parts[i].blk, parts[i].part | (parts[i].nparts << 16));
+    int rc = grow((void **)&h->order_dev, &h->cap_order, sizeof(int2) * (size_t)n);
     if (rc != HL_NO_ERROR)
         return rc;
-    CK(cudaMemcpy(h->order_dev, ord.data(), sizeof(int) * (size_t)nitems,
+    CK(cudaMemcpy(h->order_dev, items.data(), sizeof(int2) * (size_t)n,
                   cudaMemcpyHostToDevice));
     h->order_w = w;
     h->order_h = hh;
@@ -401,7 +427,12 @@ static int item_order(hl_handle *h, int w, int hh, int rho_min, int R,
     h->order_R = R;
     h->order_T = h->T;
     h->order_derho = h->p.derho;
-    *dev_order = h->order_dev;
+    h->order_ctas = ctas;
+    h->order_n = n;
+    h->order_split = any_split;
+    *dev_items = h->order_dev;
+    *nitems_out = n;
+    *split = any_split;
     return HL_NO_ERROR;
 }
 
@@ -410,7 +441,7 @@ static int ensure_image(hl_handle *h, const hl_geom &g, int w, int hh)
     int rc;
     size_t ntiles = (size_t)g.tiles_x * g.tiles_y;
     if ((rc = grow((void **)&h->d_pts, &h->cap_pts,
-                   sizeof(uint32_t) * ((size_t)w * hh + 16))) != HL_NO_ERROR)
+                   sizeof(float2) * ((size_t)w * hh + 16))) != HL_NO_ERROR)
         return rc;
     if (h->cap_tiles < ntiles + 1 || !h->d_tile_state) {
         size_t cap = 0;
@@ -499,7 +530,8 @@ static int run_ab(hl_handle *h, const hl_roi &roi, const hl_geom &g,
         h->epoch = 1;
     }
     ca.epoch = h->epoch;
-    ca.pts = h->d_pts;
+    ca.pts = nullptr;
+    ca.pts_f2 = reinterpret_cast<float2 *>(h->d_pts);
     ca.tile_off = h->d_tile_off;
     ca.count = h->d_counters + 2;
     ca.status = h->d_counters + 1;
@@ -510,7 +542,7 @@ static int run_ab(hl_handle *h, const hl_roi &roi, const hl_geom &g,
     prof_mark(h, 1, s);
 
     hl_vote_args va;
-    va.pts = h->d_pts;
+    va.pts = reinterpret_cast<const float2 *>(h->d_pts);
     va.tile_off = h->d_tile_off;
     va.ntiles = ntiles;
     va.tiles_x = g.tiles_x;
@@ -527,16 +559,19 @@ static int run_ab(hl_handle *h, const hl_roi &roi, const hl_geom &g,
     va.irho = (float)(1.0 / h->p.derho);   /* okano_3_0/HoughLine.cu:107 */
     va.acc = h->d_acc;
     va.status = h->d_counters + 1;
-    va.nitems = (h->Tp / HL_SLICE) * va.nwin;
-    int rc = item_order(h, roi.w, roi.h, g.rho_min, g.numrho, va.win_rows,
-                        va.nwin, &va.item_order);
-    if (rc != HL_NO_ERROR)
-        return rc;
     /* persistent CTAs: as many as fit (one per SM at 1024 threads) */
     const size_t smem = hl_vote_smem_bytes(va.win_rows);
     const int per_sm = std::max(1, std::min(2048 / threads,
                                             (int)((228u * 1024u) / (smem + 1024))));
-    const int grid = std::min(va.nitems, std::max(h->sms, 1) * per_sm);
+    const int ctas = std::max(h->sms, 1) * per_sm;
+    int split = 0;
+    int rc = vote_items(h, roi.w, roi.h, g.rho_min, g.numrho, va.win_rows,
+                        va.nwin, ctas, &va.items, &va.nitems, &split);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    if (split)   /* parts of a split block add into the accumulator */
+        CK(cudaMemsetAsync(h->d_acc, 0, sizeof(int32_t) * (size_t)g.numrho * h->Tp, s));
+    const int grid = std::min(va.nitems, ctas);
     va.work = reinterpret_cast<unsigned *>(h->d_counters + 9);
     va.work_base = h->work_base;
     CK(hl_launch_vote(&va, threads, grid, s));
@@ -721,6 +756,7 @@ extern "C" int hl_compact(hl_handle *h, const hl_image_desc *img,
     }
     ca.epoch = h->epoch;
     ca.pts = pts_dev;
+    ca.pts_f2 = nullptr;
     ca.tile_off = tile_off_dev;
     ca.count = count_dev;
     ca.status = h->d_counters + 1;

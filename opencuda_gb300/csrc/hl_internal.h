@@ -49,14 +49,15 @@ typedef struct hl_compact_args {
     unsigned int *ticket;            /* monotonically increasing counter */
     unsigned int ticket_base;        /* value of *ticket at launch */
     unsigned int epoch;              /* 1..2^30-1, distinct per launch */
-    uint32_t *pts;                   /* out: packed x | y << 16 */
+    uint32_t *pts;                   /* out: packed x | y << 16, or NULL */
+    float2 *pts_f2;                  /* out: (x, y) as floats, or NULL */
     int *tile_off;                   /* out: [ntiles + 1] */
     int *count;                      /* out: total points */
     int *status;
 } hl_compact_args;
 
 typedef struct hl_vote_args {
-    const uint32_t *pts;
+    const float2 *pts;        /* (x, y) of every edge point, tile-major */
     const int *tile_off;
     int ntiles, tiles_x;
     int w, h;                 /* ROI size (tile clipping) */
@@ -67,9 +68,12 @@ typedef struct hl_vote_args {
     float irho;
     int32_t *acc;             /* [R][Tp] */
     int *status;
-    /* persistent scheduling: items (slice, window) are taken in the order
-     * item_order[] (heaviest first) from a monotonically increasing counter */
-    const int *item_order;    /* [nitems] = slice + nslices * window */
+    /* persistent scheduling: work items are taken in the order items[]
+     * (heaviest first) from a monotonically increasing counter.  An item is
+     * one part of a (slice, window) block: .x = slice + nslices * window,
+     * .y = part | nparts << 16; a block split into several parts adds its
+     * partial counts into a zeroed accumulator with red.global */
+    const int2 *items;
     int nitems;
     unsigned *work;           /* counter */
     unsigned work_base;       /* its value at launch */
@@ -78,10 +82,13 @@ typedef struct hl_vote_args {
 /* Tiles the allocation-free compaction entry point can serve. */
 #define HL_NOALLOC_MAX_TILES 65536
 
-/* Vote-kernel staging: points per TMA batch and pieces per batch. */
+/* Vote-kernel staging: points per TMA batch, ring slots, tiles per
+ * coarse-filter group. */
 #define HL_VOTE_CHUNK 1024
-#define HL_VOTE_PIECES 16
-#define HL_VOTE_TG 1024       /* tiles per coarse-filter group */
+#define HL_VOTE_SLOTS 4
+#define HL_VOTE_TG 4096
+/* largest rho window (rows) one CTA can hold next to its staging */
+int hl_vote_max_rows(void);
 
 typedef struct hl_peak_args {
     const int32_t *acc;       /* [R][Tp] */

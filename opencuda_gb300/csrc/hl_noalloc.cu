@@ -88,6 +88,7 @@ extern "C" int hl_compact_noalloc(const hl_image_desc *img, uint32_t *pts_dev,
     ca.tile_state = scratch + 2;
     ca.epoch = 1;
     ca.pts = pts_dev;
+    ca.pts_f2 = nullptr;
     ca.tile_off = tile_off_dev;
     ca.count = count_dev;
     return hl_launch_compact(&ca, s) == cudaSuccess ? HL_NO_ERROR : HL_CUDA_ERROR;

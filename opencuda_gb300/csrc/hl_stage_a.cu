@@ -154,6 +154,7 @@ hl_compact_kernel(hl_compact_args a)
     __shared__ int s_grp;
     __shared__ unsigned long long s_wsum[HL_COMPACT_THREADS / 32];
     __shared__ int s_tbase[CT_GROUP];
+    __shared__ int s_tcnt[CT_GROUP];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int ngroups = (a.ntiles + CT_GROUP - 1) / CT_GROUP;
 
@@ -223,20 +224,28 @@ hl_compact_kernel(hl_compact_args a)
         const unsigned long long tot4 = __shfl_sync(FULL, wi, nw - 1);
         if (lane < nw)
             s_wsum[lane] = wi - ws;
+        /* float2 output: every tile holds an even number of entries (one
+         * sentinel pads an odd count), so runs of tiles start and end on
+         * 16-byte boundaries */
+        const int pad = a.pts_f2 ? 1 : 0;
         int total = 0;
 #pragma unroll
-        for (int q = 0; q < CT_GROUP; q++)
-            total += (int)((tot4 >> (16 * q)) & 0xffffu);
+        for (int q = 0; q < CT_GROUP; q++) {
+            const int cq = (int)((tot4 >> (16 * q)) & 0xffffu);
+            total += cq + (cq & pad);
+        }
         const int excl = lookback(a.tile_state, grp, total, a.epoch, a.status);
         if (lane == 0) {
             int run = excl;
 #pragma unroll
             for (int q = 0; q < CT_GROUP; q++) {
                 const int tile = grp * CT_GROUP + q;
+                const int cq = (int)((tot4 >> (16 * q)) & 0xffffu);
                 s_tbase[q] = run;
+                s_tcnt[q] = cq;
                 if (tile < a.ntiles)
                     a.tile_off[tile] = run;
-                run += (int)((tot4 >> (16 * q)) & 0xffffu);
+                run += cq + (cq & pad);
             }
             if (grp == ngroups - 1) {
                 a.tile_off[a.ntiles] = run;
@@ -254,9 +263,17 @@ hl_compact_kernel(hl_compact_args a)
         while (mm) {
             const int bb = __ffs(mm) - 1;
             mm &= mm - 1;
-            a.pts[pos++] = (uint32_t)(xq[q] + bb) | yy;
+            if (a.pts_f2)
+                a.pts_f2[pos] = make_float2((float)(xq[q] + bb), (float)yq[q]);
+            else
+                a.pts[pos] = (uint32_t)(xq[q] + bb) | yy;
+            pos++;
         }
     }
+    /* the sentinel (1e30, 0) never votes inside an accumulator: its rho is
+     * 1e30 * cos(theta_k), and cosf of a float angle is never 0 */
+    if (a.pts_f2 && tid < CT_GROUP && (s_tcnt[tid] & 1))
+        a.pts_f2[s_tbase[tid] + s_tcnt[tid]] = make_float2(1.0e30f, 0.0f);
 }
 
 cudaError_t hl_launch_compact(const hl_compact_args *a, cudaStream_t s)

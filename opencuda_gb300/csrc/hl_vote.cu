@@ -9,40 +9,46 @@
  *
  * Work decomposition.  A work item is one (theta slice, rho window) block of
  * the accumulator, held in shared memory as acc[row][lane]: 32 thetas (one
- * per lane) x win_rows rho bins.  A warp takes two points per step; its 32
+ * per lane) x win_rows rho bins.  A warp votes one point at a time; its 32
  * lanes add to 32 different thetas of the same point -- 32 different banks --
- * so every shared atomic instruction is conflict-free and no two lanes ever
- * hit one address (the aggregation a warp-aggregated atomic would buy is built
+ * so every shared-memory reduction is conflict-free and no two lanes ever hit
+ * one address (the aggregation a warp-aggregated atomic would buy is built
  * into the layout).
  *
- * Persistent CTAs take items heaviest-first from a global counter.  For an
- * item, a coarse filter marks the 128x32 compaction tiles whose rho interval
- * over the slice meets the window; runs of marked tiles are contiguous in the
- * tile-major point list, and thread 0 streams them into shared memory with
- * cp.async.bulk (TMA bulk copies of 16-byte aligned supersets of each run)
- * completing on an mbarrier, two batches in flight.  All threads then unpack
- * each batch, drop points whose own rho interval over the slice misses the
- * window, and vote.  At the end of the item the block is stored with
- * coalesced 128-byte rows into acc[R][Tp]; every bin is written exactly once,
- * so the global accumulator needs no clearing.
+ * Pipeline.  Persistent CTAs take items heaviest-first from a global counter.
+ * For an item, all threads mark the 128x32 compaction tiles whose rho
+ * interval over the slice meets the window and turn the marks into runs of
+ * tiles -- contiguous ranges of the tile-major point list, 16-byte aligned
+ * because the compaction pads every tile to an even number of float2
+ * entries.  The runs, laid end to end, form the item's point stream.  Then
+ * the CTA splits into one producer warp and consumer warps that meet only on
+ * mbarriers: batch b is stream range [b*CHUNK, (b+1)*CHUNK); the producer's
+ * lanes each copy one run's part of it into a ring of HL_VOTE_SLOTS
+ * shared-memory slots with cp.async.bulk (TMA bulk copies completing on the
+ * slot's full barrier), so a slot holds its batch gap-free; each consumer
+ * warp votes its share of the slot straight from shared memory and arrives
+ * on the slot's empty barrier, which the producer waits on before refilling
+ * it.  No block-wide barrier separates batches.
+ * At the end of the item the block is stored with coalesced 128-byte rows
+ * into acc[R][Tp]; every bin is written exactly once, so the global
+ * accumulator needs no clearing.
  *
- * Bounds: a point votes without per-vote checks only when its rho interval
- * over the slice lies, with three bins of slack, inside the window; a point
- * that straddles the window checks every vote (predicated red.shared), lanes
- * beyond T add into a private sink word, and mbarrier waits are bounded (a
- * time-out sets a status bit that the host reads with the result; the CTA
- * keeps the same barrier sequence and stops taking items).
+ * Per point and consumer warp: one broadcast shared load, two multiplies,
+ * one add, one float->int truncation, the window test and one predicated
+ * red.shared -- the truncation (16 per SM-clock) is the binding pipe.
  *
- * Instruction budget per point and warp on the interior path: one shared
- * load per two points, two multiplies, one add, one float->int truncation,
- * one address multiply-add and one red.shared -- the truncation (16 per
- * SM-clock) is the binding pipe, about half the measured red.shared rate.
+ * Bounds: every vote tests its window row (lanes past the last theta get an
+ * empty window), mbarrier waits are bounded (a time-out sets a status bit
+ * that the host reads with the result; every warp still reaches the same
+ * block barriers).
  */
 #include "hl_internal.h"
 
 #define FULL 0xffffffffu
-#define RAWCAP (HL_VOTE_CHUNK + 6 * HL_VOTE_PIECES + 32)
-#define MBAR_SPIN_LIMIT (1 << 22)
+#define MBAR_SPIN_LIMIT (1 << 20)
+/* float2 entries of one ring slot (runs are gap-free: the compaction pads
+ * every tile to an even number of points, 16 bytes) */
+#define SLOT_CAP HL_VOTE_CHUNK
 
 template <bool UNIT>
 __device__ __forceinline__ int rho_of(float x, float y, float c, float s,
@@ -57,16 +63,6 @@ __device__ __forceinline__ int rho_of(float x, float y, float c, float s,
     return __float2int_rz(__fadd_rn(a, b));
 }
 
-/* rho values of the two points (x0, y0), (x1, y1) of a pair record
- * {x0, x1, y0, y1} for this lane's (c, s) */
-template <bool UNIT>
-__device__ __forceinline__ void rho_pair(const float4 &q, float c, float s,
-                                         float irho, int &r0, int &r1)
-{
-    r0 = rho_of<UNIT>(q.x, q.z, c, s, irho);
-    r1 = rho_of<UNIT>(q.y, q.w, c, s, irho);
-}
-
 /* ---- mbarrier + bulk copy ---------------------------------------------- */
 __device__ __forceinline__ unsigned smem_u32(const void *p)
 {
@@ -76,6 +72,11 @@ __device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned n)
 {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
                  "r"(n)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar))
                  : "memory");
 }
 __device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar,
@@ -115,6 +116,36 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar,
     return false;
 }
 
+/* the same wait, but each try_wait may suspend the warp for up to about a
+ * microsecond instead of spinning, leaving issue slots to working warps */
+__device__ __forceinline__ bool mbar_wait_sleep(unsigned long long *bar,
+                                                unsigned parity)
+{
+    const unsigned a = smem_u32(bar);
+    for (int i = 0; i < MBAR_SPIN_LIMIT / 64; i++) {
+        unsigned ok;
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], "
+            "%2, %3; selp.u32 %0, 1, 0, p; }"
+            : "=r"(ok)
+            : "r"(a), "r"(parity), "r"(1000u)
+            : "memory");
+        if (ok)
+            return true;
+    }
+    return false;
+}
+
+/* one vote if the window-relative row rl is below lim (predicated
+ * red.shared, no returned value, no branch) */
+__device__ __forceinline__ void red_smem_if(unsigned addr, unsigned rl,
+                                            unsigned lim)
+{
+    asm volatile("{ .reg .pred p; setp.lt.u32 p, %1, %2; "
+                 "@p red.shared.add.u32 [%0], 1; }" ::"r"(addr),
+                 "r"(rl), "r"(lim));
+}
+
 /* Conservative test: can any point of tile t vote into rho bins
  * [lo_bin, hi_bin] for a theta in [th0, th1]?  rho(x, y, th) is linear in
  * (x, y) for fixed th, so its extremes over the tile lie at the corners; over
@@ -151,26 +182,22 @@ __device__ __forceinline__ bool tile_hits(int t, int tiles_x, int w, int h,
 }
 
 struct VoteSmem {
-    unsigned long long mbar[2];
+    unsigned long long full[HL_VOTE_SLOTS];
+    unsigned long long empty[HL_VOTE_SLOTS];
     int item;
+    int part;
     int nruns;
-    int nin[3];                       /* interior points kept, per batch */
-    int nst[3];                       /* straddling points kept, per batch */
-    int np[2];
-    int total[2];
     int timeout;
-    int pc_src[2][HL_VOTE_PIECES];    /* first point copied (multiple of 4) */
-    int pc_roff[2][HL_VOTE_PIECES];   /* offset in raw[slot] */
-    int pc_skip[2][HL_VOTE_PIECES];   /* leading points copied but not used */
-    int pc_base[2][HL_VOTE_PIECES + 1];
+    int total;                         /* points in the group's runs */
     unsigned mask[HL_VOTE_TG / 32];
-    int run_s[HL_VOTE_TG / 2 + 1];
-    int run_e[HL_VOTE_TG / 2 + 1];
-    int sink[HL_SLICE];               /* votes of lanes past the last theta */
-    alignas(16) unsigned raw[2][RAWCAP];
-    /* unpacked points as pair records {x0, x1, y0, y1} */
-    alignas(16) float4 cin[2][HL_VOTE_CHUNK / 2 + 1];
-    alignas(16) float4 cst[2][HL_VOTE_CHUNK / 2 + 1];
+    unsigned sw[HL_VOTE_TG / 32];      /* run starts per mask word */
+    unsigned ew[HL_VOTE_TG / 32];      /* run ends per mask word */
+    int ws[HL_VOTE_TG / 32];           /* runs starting before the word */
+    int we[HL_VOTE_TG / 32];
+    int run_s[HL_VOTE_TG / 2];
+    int run_e[HL_VOTE_TG / 2];
+    int rpre[HL_VOTE_TG / 2];          /* stream position of each run */
+    alignas(16) float2 raw[HL_VOTE_SLOTS][SLOT_CAP];
 };
 
 #define VOTE_FIXED ((sizeof(VoteSmem) + 127) / 128 * 128)
@@ -180,81 +207,10 @@ size_t hl_vote_smem_bytes(int win_rows)
     return VOTE_FIXED + (size_t)win_rows * HL_SLICE * sizeof(int);
 }
 
-/* one vote: shared-memory reduction without a returned value */
-__device__ __forceinline__ void red_smem(unsigned addr)
+int hl_vote_max_rows(void)
 {
-    asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(addr));
-}
-/* one vote if the window-relative row rl is below lim */
-__device__ __forceinline__ void red_smem_if(unsigned addr, unsigned rl,
-                                            unsigned lim)
-{
-    asm volatile("{ .reg .pred p; setp.lt.u32 p, %1, %2; "
-                 "@p red.shared.add.u32 [%0], 1; }" ::"r"(addr),
-                 "r"(rl), "r"(lim));
-}
-
-/* Producer (thread 0): form the next batch of up to HL_VOTE_CHUNK points from
- * the run list and start its bulk copies into raw[slot].  State: run index r
- * and point cursor pos.  Source and destination of every copy are 16-byte
- * aligned (whole groups of 4 points) and the point list is allocated with at
- * least 4 entries of slack, so the rounded-up tail stays in bounds. */
-__device__ void produce(VoteSmem &sm, int slot, const uint32_t *pts, int &r,
-                        int &pos)
-{
-    int total = 0, np = 0, roff = 0;
-    const int nruns = sm.nruns;
-    while (np < HL_VOTE_PIECES && total < HL_VOTE_CHUNK && r < nruns) {
-        if (pos >= sm.run_e[r]) {
-            r++;
-            if (r < nruns)
-                pos = sm.run_s[r];
-            continue;
-        }
-        const int take = min(sm.run_e[r] - pos, HL_VOTE_CHUNK - total);
-        const int a0 = pos & ~3;
-        const int a1 = (pos + take + 3) & ~3;
-        sm.pc_src[slot][np] = a0;
-        sm.pc_roff[slot][np] = roff;
-        sm.pc_skip[slot][np] = pos - a0;
-        sm.pc_base[slot][np] = total;
-        roff += a1 - a0;
-        total += take;
-        pos += take;
-        np++;
-    }
-    sm.pc_base[slot][np] = total;
-    sm.np[slot] = np;
-    sm.total[slot] = total;
-    if (total > 0) {
-        mbar_expect_tx(&sm.mbar[slot], (unsigned)roff * 4u);
-        for (int p = 0; p < np; p++) {
-            const int end = (p + 1 < np) ? sm.pc_roff[slot][p + 1] : roff;
-            const int nb = end - sm.pc_roff[slot][p];
-            bulk_g2s(&sm.raw[slot][sm.pc_roff[slot][p]], pts + sm.pc_src[slot][p],
-                     (unsigned)nb * 4u, &sm.mbar[slot]);
-        }
-    }
-}
-
-/* append a point to a pair-record list with a warp-aggregated counter */
-__device__ __forceinline__ void append_point(bool take, float x, float y,
-                                             int *counter, float *list)
-{
-    const int lane = threadIdx.x & 31;
-    const unsigned bm = __ballot_sync(FULL, take);
-    if (!bm)
-        return;
-    const int leader = __ffs(bm) - 1;
-    int base = 0;
-    if (lane == leader)
-        base = atomicAdd(counter, __popc(bm));
-    base = __shfl_sync(FULL, base, leader);
-    if (take) {
-        const int q = base + __popc(bm & ((1u << lane) - 1u));
-        list[(q >> 1) * 4 + (q & 1)] = x;
-        list[(q >> 1) * 4 + 2 + (q & 1)] = y;
-    }
+    const size_t cap = 227u * 1024u;
+    return (int)((cap - VOTE_FIXED) / (HL_SLICE * sizeof(int))) & ~7;
 }
 
 template <bool UNIT>
@@ -266,47 +222,52 @@ hl_vote_kernel(hl_vote_args a)
     int *s_acc = reinterpret_cast<int *>(vote_raw + VOTE_FIXED);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nthr = blockDim.x, nwarps = nthr >> 5;
+    const int ncons = nwarps - 1;               /* consumer warps 1..nwarps-1 */
     const int nslices = a.Tp / HL_SLICE;
 
     if (tid == 0) {
-        mbar_init(&sm.mbar[0], 1);
-        mbar_init(&sm.mbar[1], 1);
+        for (int i = 0; i < HL_VOTE_SLOTS; i++) {
+            mbar_init(&sm.full[i], 1);
+            mbar_init(&sm.empty[i], (unsigned)ncons);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         sm.timeout = 0;
     }
-    unsigned use0 = 0u, use1 = 0u;   /* completed phases of mbar[0], mbar[1] */
+    /* running batch index, the same sequence on the producer and consumers:
+     * slot = seq % SLOTS, phase = (seq / SLOTS) & 1 */
+    unsigned seq = 0;
     __syncthreads();
 
     while (true) {
         if (tid == 0) {
             const unsigned t = atomicAdd(a.work, 1u) - a.work_base;
-            sm.item = (t < (unsigned)a.nitems) ? a.item_order[t] : -1;
+            if (t < (unsigned)a.nitems) {
+                const int2 it = a.items[t];
+                sm.item = it.x;
+                sm.part = it.y;
+            } else {
+                sm.item = -1;
+            }
         }
         __syncthreads();
         const int item = sm.item;
-        if (item < 0 || sm.timeout)
+        if (item < 0)
             break;
+        const int part = sm.part & 0xffff, nparts = max(sm.part >> 16, 1);
         const int slice = item % nslices, win = item / nslices;
         const int k0 = slice * HL_SLICE, k = k0 + lane;
         const float c = a.cosv[k], s = a.sinv[k];   /* table padded to Tp */
         const int w0 = win * a.win_rows;
         const int rows = min(a.win_rows, a.R - w0);
         const int row_base = a.rho_min + w0;       /* rho bin of local row 0 */
-        const bool kv = k < a.T;
-        const unsigned lrows = kv ? (unsigned)rows : 0u;
+        const unsigned lrows = (k < a.T) ? (unsigned)rows : 0u;
         const int klast = min(k0 + HL_SLICE - 1, a.T - 1);
         const float c0 = a.cosv[k0], s0 = a.sinv[k0];
         const float c1 = a.cosv[klast], s1 = a.sinv[klast];
         const float lo_bin = (float)row_base;
         const float hi_bin = (float)(row_base + rows - 1);
         const bool filter = a.nwin > 1;
-        /* shared addresses: bin row rl of this lane is acc_l + rl * 128;
-         * interior votes index by rho directly (base folded), and lanes past
-         * the last theta vote into their own sink word */
         const unsigned acc_l = smem_u32(s_acc) + 4u * lane;
-        const unsigned in_mul = kv ? 128u : 0u;
-        const unsigned in_base = kv ? acc_l - 128u * (unsigned)row_base
-                                    : smem_u32(&sm.sink[lane]);
 
         {
             int4 *z = reinterpret_cast<int4 *>(s_acc);
@@ -330,160 +291,188 @@ hl_vote_kernel(hl_vote_args a)
                     sm.mask[wd] = m;
             }
             __syncthreads();
-            /* runs of marked tiles -> point ranges (warp 0) */
+            /* run boundaries per word and their prefix counts (warp 0, four
+             * words per lane) */
             if (warp == 0) {
-                const unsigned m = sm.mask[lane];
-                const unsigned prev = __shfl_up_sync(FULL, m, 1);
-                const unsigned next = __shfl_down_sync(FULL, m, 1);
-                const unsigned carry_in = (lane > 0) ? (prev >> 31) : 0u;
-                const unsigned carry_out = (lane < 31) ? (next & 1u) : 0u;
-                unsigned starts = m & ~((m << 1) | carry_in);
-                unsigned ends = m & ~((m >> 1) | (carry_out << 31));
-                const int ns = __popc(starts), ne = __popc(ends);
-                int bs = ns, be = ne;
+                constexpr int WPL = HL_VOTE_TG / 32 / 32;
+                int cs = 0, ce = 0;
+                unsigned st[WPL], en[WPL];
+#pragma unroll
+                for (int q = 0; q < WPL; q++) {
+                    const int wd = lane * WPL + q;
+                    const unsigned m = sm.mask[wd];
+                    const unsigned prev = (wd > 0) ? sm.mask[wd - 1] : 0u;
+                    const unsigned next = (wd + 1 < HL_VOTE_TG / 32) ? sm.mask[wd + 1] : 0u;
+                    st[q] = m & ~((m << 1) | (prev >> 31));
+                    en[q] = m & ~((m >> 1) | ((next & 1u) << 31));
+                    cs += __popc(st[q]);
+                    ce += __popc(en[q]);
+                }
+                int is = cs, ie = ce;
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
-                    const int t1 = __shfl_up_sync(FULL, bs, o);
-                    const int t2 = __shfl_up_sync(FULL, be, o);
+                    const int t1 = __shfl_up_sync(FULL, is, o);
+                    const int t2 = __shfl_up_sync(FULL, ie, o);
                     if (lane >= o) {
-                        bs += t1;
-                        be += t2;
+                        is += t1;
+                        ie += t2;
                     }
                 }
-                bs -= ns;
-                be -= ne;
-                while (starts) {
-                    const int b = __ffs(starts) - 1;
-                    starts &= starts - 1;
-                    sm.run_s[bs++] = a.tile_off[tg + lane * 32 + b];
-                }
-                while (ends) {
-                    const int b = __ffs(ends) - 1;
-                    ends &= ends - 1;
-                    sm.run_e[be++] = a.tile_off[tg + lane * 32 + b + 1];
+                is -= cs;
+                ie -= ce;
+#pragma unroll
+                for (int q = 0; q < WPL; q++) {
+                    const int wd = lane * WPL + q;
+                    sm.sw[wd] = st[q];
+                    sm.ew[wd] = en[q];
+                    sm.ws[wd] = is;
+                    sm.we[wd] = ie;
+                    is += __popc(st[q]);
+                    ie += __popc(en[q]);
                 }
                 if (lane == 31)
-                    sm.nruns = bs;
+                    sm.nruns = is;
+            }
+            __syncthreads();
+            /* run endpoints -> point ranges, one tile per thread */
+            for (int tl = tid; tl < tg_n; tl += nthr) {
+                const int wd = tl >> 5, b = tl & 31;
+                const unsigned below = (1u << b) - 1u;
+                if ((sm.sw[wd] >> b) & 1u)
+                    sm.run_s[sm.ws[wd] + __popc(sm.sw[wd] & below)] = a.tile_off[tg + tl];
+                if ((sm.ew[wd] >> b) & 1u)
+                    sm.run_e[sm.we[wd] + __popc(sm.ew[wd] & below)] = a.tile_off[tg + tl + 1];
             }
             __syncthreads();
 
-            /* stream the runs through shared memory, two batches in flight */
-            int r = 0, pos = (sm.nruns > 0) ? sm.run_s[0] : 0;
-            if (tid == 0) {
-                sm.nin[0] = sm.nin[1] = sm.nin[2] = 0;
-                sm.nst[0] = sm.nst[1] = sm.nst[2] = 0;
-                produce(sm, 0, a.pts, r, pos);
-                produce(sm, 1, a.pts, r, pos);
+            /* stream positions of the runs (warp 0: a chunk of runs per
+             * lane, then a warp scan of the chunk sums) */
+            if (warp == 0) {
+                const int nr = sm.nruns;
+                const int per = (nr + 31) / 32;
+                const int r0 = min(nr, lane * per), r1 = min(nr, r0 + per);
+                int sum = 0;
+                for (int r = r0; r < r1; r++)
+                    sum += sm.run_e[r] - sm.run_s[r];
+                int incl = sum;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t = __shfl_up_sync(FULL, incl, o);
+                    if (lane >= o)
+                        incl += t;
+                }
+                int pos = incl - sum;
+                for (int r = r0; r < r1; r++) {
+                    sm.rpre[r] = pos;
+                    pos += sm.run_e[r] - sm.run_s[r];
+                }
+                if (lane == 31)
+                    sm.total = incl;
             }
             __syncthreads();
-            for (int b = 0;; b++) {
-                const int slot = b & 1;
-                const int total = sm.total[slot];
-                if (total == 0)
-                    break;
-                const unsigned par = (slot ? use1 : use0) & 1u;
-                const bool ok = mbar_wait(&sm.mbar[slot], par);
-                if (slot)
-                    use1++;
-                else
-                    use0++;
-                if (!ok && lane == 0) {
-                    /* the batch never arrived: flag it and carry on with the
-                     * same barriers (votes stay inside the window, so the
-                     * result is only wrong, and the call reports it) */
-                    sm.timeout = 1;
-                    atomicOr(a.status, HL_ST_VOTE_TIMEOUT);
-                }
-                /* unpack; each point's own rho interval over the slice sorts
-                 * it into interior (every vote inside the window), straddling
-                 * (some inside) or dropped */
-                const int np = sm.np[slot];
-                const int cnt_i = b % 3;
-                float *lin = reinterpret_cast<float *>(sm.cin[slot]);
-                float *lst = reinterpret_cast<float *>(sm.cst[slot]);
-                for (int j0 = 0; j0 < total; j0 += nthr) {
-                    const int j = j0 + tid;
-                    bool inner = false, strad = false;
-                    float x = 0.f, y = 0.f;
-                    if (j < total) {
-                        int p = 0;
-                        while (p + 1 < np && sm.pc_base[slot][p + 1] <= j)
-                            p++;
-                        const unsigned u =
-                            sm.raw[slot][sm.pc_roff[slot][p] + sm.pc_skip[slot][p] +
-                                         (j - sm.pc_base[slot][p])];
-                        x = (float)(u & 0xffffu);
-                        y = (float)(u >> 16);
-                        const float f0 = x * c0 + y * s0;
-                        const float f1 = x * c1 + y * s1;
-                        float lo = fminf(f0, f1), hi = fmaxf(f0, f1);
-                        const float tol = 1e-3f * (x + y) + 1e-3f;
-                        if (c0 * y - s0 * x >= -tol && x * s1 - y * c1 >= -tol)
-                            hi = fmaxf(hi, x + y);
-                        lo = lo * a.irho;
-                        hi = hi * a.irho;
-                        inner = (lo - 3.0f >= lo_bin) && (hi + 3.0f <= hi_bin);
-                        strad = !inner && (lo - 3.0f <= hi_bin) && (hi + 3.0f >= lo_bin);
-                    }
-                    append_point(inner, x, y, &sm.nin[cnt_i], lin);
-                    append_point(strad, x, y, &sm.nst[cnt_i], lst);
-                }
-                __syncthreads();
-                const int n_in = sm.nin[cnt_i], n_st = sm.nst[cnt_i];
-                if (tid == 0) {
-                    /* counters of batch b + 2: last read (for batch b - 1)
-                     * before this step's barrier by every thread */
-                    sm.nin[(b + 2) % 3] = 0;
-                    sm.nst[(b + 2) % 3] = 0;
-                    produce(sm, slot, a.pts, r, pos);
-                }
-                /* interior points: every vote lands in the window */
+            const int total = sm.total;
+            const int nb_all = (total + HL_VOTE_CHUNK - 1) / HL_VOTE_CHUNK;
+            /* this part's share of the batches */
+            const int b_lo = (int)((long long)nb_all * part / nparts);
+            const int b_hi = (int)((long long)nb_all * (part + 1) / nparts);
+            const int nruns = sm.nruns;
+
+            if (warp == 0) {
+                /* producer warp: batch b is stream range [b*CHUNK, ...);
+                 * lane i copies the part of run r0 + i overlapping it, and a
+                 * ballot finds the first run of the next batch */
+                int r0 = 0;
                 {
-                    const int npairs = n_in >> 1;
-                    const float4 *c4 = sm.cin[slot];
-                    int p = warp;
-                    for (; p + nwarps < npairs; p += 2 * nwarps) {
-                        const float4 qa = c4[p];
-                        const float4 qb = c4[p + nwarps];
-                        int r0, r1, r2, r3;
-                        rho_pair<UNIT>(qa, c, s, a.irho, r0, r1);
-                        rho_pair<UNIT>(qb, c, s, a.irho, r2, r3);
-                        red_smem((unsigned)r0 * in_mul + in_base);
-                        red_smem((unsigned)r1 * in_mul + in_base);
-                        red_smem((unsigned)r2 * in_mul + in_base);
-                        red_smem((unsigned)r3 * in_mul + in_base);
+                    /* first run ending after this part's first point */
+                    const int s_first = b_lo * HL_VOTE_CHUNK;
+                    int lo = 0, hi = max(nruns - 1, 0);
+                    while (lo < hi) {
+                        const int mid = (lo + hi) >> 1;
+                        if (sm.rpre[mid] + (sm.run_e[mid] - sm.run_s[mid]) <= s_first)
+                            lo = mid + 1;
+                        else
+                            hi = mid;
                     }
-                    if (p < npairs) {
-                        int r0, r1;
-                        rho_pair<UNIT>(c4[p], c, s, a.irho, r0, r1);
-                        red_smem((unsigned)r0 * in_mul + in_base);
-                        red_smem((unsigned)r1 * in_mul + in_base);
-                    }
-                    if ((n_in & 1) && warp == nwarps - 1) {
-                        const float4 q = c4[npairs];
-                        const int r0 = rho_of<UNIT>(q.x, q.z, c, s, a.irho);
-                        red_smem((unsigned)r0 * in_mul + in_base);
-                    }
+                    r0 = lo;
                 }
-                /* straddling points: only the lanes inside the window vote */
-                {
-                    const int npairs = n_st >> 1;
-                    const float4 *c4 = sm.cst[slot];
-                    int p = nwarps - 1 - warp;   /* other end of the warp range */
-                    for (; p < npairs; p += nwarps) {
-                        int r0, r1;
-                        rho_pair<UNIT>(c4[p], c, s, a.irho, r0, r1);
-                        const unsigned l0 = (unsigned)(r0 - row_base);
-                        const unsigned l1 = (unsigned)(r1 - row_base);
+                for (int b = b_lo; b < b_hi; b++) {
+                    const int slot = (int)(seq % HL_VOTE_SLOTS);
+                    if (lane == 0 && seq >= HL_VOTE_SLOTS && !*(volatile int *)&sm.timeout &&
+                        !mbar_wait(&sm.empty[slot], ((seq / HL_VOTE_SLOTS) - 1u) & 1u)) {
+                        sm.timeout = 1;
+                        atomicOr(a.status, HL_ST_VOTE_TIMEOUT);
+                    }
+                    const int s0 = b * HL_VOTE_CHUNK;
+                    const int e0 = min(total, s0 + HL_VOTE_CHUNK);
+                    if (lane == 0)
+                        mbar_expect_tx(&sm.full[slot], (unsigned)(e0 - s0) * 8u);
+                    __syncwarp();
+                    /* runs from r0 on: every run ending at or before e0 lies
+                     * wholly in this batch; the first one reaching past e0
+                     * is shared with the next batch and ends the scan (the
+                     * runs after it start at or beyond e0) */
+                    int next = nruns;
+                    for (int rb = r0; rb < nruns; rb += 32) {
+                        const int r = rb + lane;
+                        bool past = false;
+                        if (r < nruns) {
+                            const int rs = sm.rpre[r];
+                            const int re = rs + (sm.run_e[r] - sm.run_s[r]);
+                            const int ps = max(s0, rs), pe = min(e0, re);
+                            if (pe > ps)
+                                bulk_g2s(&sm.raw[slot][ps - s0],
+                                         a.pts + sm.run_s[r] + (ps - rs),
+                                         (unsigned)(pe - ps) * 8u, &sm.full[slot]);
+                            past = re > e0;
+                        }
+                        const unsigned pm = __ballot_sync(FULL, past);
+                        if (pm) {
+                            next = rb + __ffs(pm) - 1;
+                            break;
+                        }
+                    }
+                    r0 = next;
+                    seq++;
+                }
+            } else {
+                /* consumer warps: vote every point of a batch, then free
+                 * the slot */
+                const int cw = warp - 1;
+                for (int b = b_lo; b < b_hi; b++) {
+                    const int slot = (int)(seq % HL_VOTE_SLOTS);
+                    /* after a time-out nobody waits any more */
+                    const bool ok = *(volatile int *)&sm.timeout ||
+                                    mbar_wait_sleep(&sm.full[slot], (seq / HL_VOTE_SLOTS) & 1u);
+                    if (!ok && lane == 0) {
+                        sm.timeout = 1;
+                        atomicOr(a.status, HL_ST_VOTE_TIMEOUT);
+                    }
+                    seq++;
+                    const int n = min(HL_VOTE_CHUNK, total - b * HL_VOTE_CHUNK);
+                    const float2 *pts = sm.raw[slot];
+                    int j = cw;
+                    for (; j + 3 * ncons < n; j += 4 * ncons) {
+                        const float2 p0 = pts[j];
+                        const float2 p1 = pts[j + ncons];
+                        const float2 p2 = pts[j + 2 * ncons];
+                        const float2 p3 = pts[j + 3 * ncons];
+                        const unsigned l0 = (unsigned)(rho_of<UNIT>(p0.x, p0.y, c, s, a.irho) - row_base);
+                        const unsigned l1 = (unsigned)(rho_of<UNIT>(p1.x, p1.y, c, s, a.irho) - row_base);
+                        const unsigned l2 = (unsigned)(rho_of<UNIT>(p2.x, p2.y, c, s, a.irho) - row_base);
+                        const unsigned l3 = (unsigned)(rho_of<UNIT>(p3.x, p3.y, c, s, a.irho) - row_base);
                         red_smem_if(acc_l + 128u * l0, l0, lrows);
                         red_smem_if(acc_l + 128u * l1, l1, lrows);
+                        red_smem_if(acc_l + 128u * l2, l2, lrows);
+                        red_smem_if(acc_l + 128u * l3, l3, lrows);
                     }
-                    if ((n_st & 1) && warp == 0) {
-                        const float4 q = c4[npairs];
-                        const int r0 = rho_of<UNIT>(q.x, q.z, c, s, a.irho);
-                        const unsigned l0 = (unsigned)(r0 - row_base);
+                    for (; j < n; j += ncons) {
+                        const float2 p0 = pts[j];
+                        const unsigned l0 = (unsigned)(rho_of<UNIT>(p0.x, p0.y, c, s, a.irho) - row_base);
                         red_smem_if(acc_l + 128u * l0, l0, lrows);
                     }
+                    __syncwarp();
+                    if (lane == 0)
+                        mbar_arrive(&sm.empty[slot]);
                 }
             }
             __syncthreads();
@@ -493,11 +482,23 @@ hl_vote_kernel(hl_vote_args a)
         int4 *dst4 = reinterpret_cast<int4 *>(a.acc);
         const int4 *src4 = reinterpret_cast<const int4 *>(s_acc);
         const int tp4 = a.Tp >> 2;
-        for (int i = tid; i < rows * (HL_SLICE / 4); i += nthr) {
-            const int rr = i >> 3, q = i & 7;
-            dst4[(size_t)(w0 + rr) * tp4 + (k0 >> 2) + q] = src4[i];
+        if (nparts == 1) {
+            for (int i = tid; i < rows * (HL_SLICE / 4); i += nthr) {
+                const int rr = i >> 3, q = i & 7;
+                dst4[(size_t)(w0 + rr) * tp4 + (k0 >> 2) + q] = src4[i];
+            }
+        } else {
+            /* one part of a split block: add its nonzero counts into the
+             * zeroed accumulator */
+            for (int i = tid; i < rows * HL_SLICE; i += nthr) {
+                const int v = s_acc[i];
+                if (v)
+                    atomicAdd(&a.acc[(size_t)(w0 + (i >> 5)) * a.Tp + k0 + (i & 31)], v);
+            }
         }
         __syncthreads();
+        if (sm.timeout)
+            break;
     }
 }
 
