@@ -34,13 +34,14 @@
  * accumulator needs no clearing.
  *
  * Per point and consumer warp: one broadcast shared load, two multiplies,
- * one add, one float->int truncation, the window test and one predicated
- * red.shared -- the truncation (16 per SM-clock) is the binding pipe.
+ * two adds (the second one rounds to an integer, see vote_row), one
+ * subtract, one unsigned min and one address multiply-add, and one
+ * red.shared -- nine issue slots and no branch per vote.
  *
- * Bounds: every vote tests its window row (lanes past the last theta get an
- * empty window), mbarrier waits are bounded (a time-out sets a status bit
- * that the host reads with the result; every warp still reaches the same
- * block barriers).
+ * Bounds: every vote's row is clamped to the window's dump row (lanes past
+ * the last theta to row 0 of their padding column, zeroed before the store),
+ * mbarrier waits are bounded (a time-out sets a status bit that the host
+ * reads with the result; every warp still reaches the same block barriers).
  */
 #include "hl_internal.h"
 
@@ -51,8 +52,8 @@
 #define SLOT_CAP HL_VOTE_CHUNK
 
 template <bool UNIT>
-__device__ __forceinline__ int rho_of(float x, float y, float c, float s,
-                                      float irho)
+__device__ __forceinline__ float rho_f(float x, float y, float c, float s,
+                                       float irho)
 {
     float a = __fmul_rn(x, c);
     float b = __fmul_rn(y, s);
@@ -60,7 +61,42 @@ __device__ __forceinline__ int rho_of(float x, float y, float c, float s,
         a = __fmul_rn(a, irho);
         b = __fmul_rn(b, irho);
     }
-    return __float2int_rz(__fadd_rn(a, b));
+    return __fadd_rn(a, b);
+}
+template <bool UNIT>
+__device__ __forceinline__ int rho_of(float x, float y, float c, float s,
+                                      float irho)
+{
+    return __float2int_rz(rho_f<UNIT>(x, y, c, s, irho));
+}
+
+/* Float -> integer without the conversion pipe (16 results per SM-clock).
+ * M = 1.5 * 2^23: for |v| < 2^22 the sum v + M lies in [2^23, 2^24), where
+ * floats are spaced 1 apart, so the sum rounded toward zero is M + floor(v)
+ * and rounded up is M + ceil(v), and its bit pattern is bits(M) plus that
+ * integer.  Truncation equals floor for v >= 0 and ceil for v < 0, so a rho
+ * window whose rows are all >= 1 may use floor (a negative v then lands below
+ * the window either way), one whose rows are all <= -1 may use ceil, and only
+ * the window holding row 0 needs the exact conversion. */
+#define RHO_MAGIC 12582912.0f
+#define RHO_MAGIC_BITS 0x4B400000
+enum { CV_EXACT = 0, CV_FLOOR = 1, CV_CEIL = 2 };
+
+/* window-relative row of a point for this lane's theta; base is the rho of
+ * row 0 (CV_EXACT) or RHO_MAGIC_BITS plus that rho */
+template <bool UNIT, int CV>
+__device__ __forceinline__ unsigned vote_row(float x, float y, float c,
+                                             float s, float irho, int base)
+{
+    const float v = rho_f<UNIT>(x, y, c, s, irho);
+    int r;
+    if (CV == CV_FLOOR)
+        r = __float_as_int(__fadd_rz(v, RHO_MAGIC));
+    else if (CV == CV_CEIL)
+        r = __float_as_int(__fadd_ru(v, RHO_MAGIC));
+    else
+        r = __float2int_rz(v);
+    return (unsigned)(r - base);
 }
 
 /* ---- mbarrier + bulk copy ---------------------------------------------- */
@@ -136,14 +172,41 @@ __device__ __forceinline__ bool mbar_wait_sleep(unsigned long long *bar,
     return false;
 }
 
-/* one vote if the window-relative row rl is below lim (predicated
- * red.shared, no returned value, no branch) */
-__device__ __forceinline__ void red_smem_if(unsigned addr, unsigned rl,
-                                            unsigned lim)
+/* one vote, no returned value */
+__device__ __forceinline__ void red_smem(unsigned addr)
 {
-    asm volatile("{ .reg .pred p; setp.lt.u32 p, %1, %2; "
-                 "@p red.shared.add.u32 [%0], 1; }" ::"r"(addr),
-                 "r"(rl), "r"(lim));
+    asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(addr));
+}
+
+/* Votes of a consumer warp for points j, j + step, ... < n of a ring slot.
+ * A row outside the window (rl >= lim as unsigned) is sent to row lim: the
+ * dump row just past the window (lim = window rows) or, for lanes past the
+ * last theta (lim = 0), row 0 of the lane's own padding column.  No vote is
+ * predicated, so the loop has no branch per vote. */
+template <bool UNIT, int CV>
+__device__ __forceinline__ void vote_batch(const float2 *pts, int n, int j,
+                                           int step, float c, float s,
+                                           float irho, int base,
+                                           unsigned acc_l, unsigned lim)
+{
+    for (; j + 3 * step < n; j += 4 * step) {
+        const float2 p0 = pts[j];
+        const float2 p1 = pts[j + step];
+        const float2 p2 = pts[j + 2 * step];
+        const float2 p3 = pts[j + 3 * step];
+        const unsigned l0 = min(vote_row<UNIT, CV>(p0.x, p0.y, c, s, irho, base), lim);
+        const unsigned l1 = min(vote_row<UNIT, CV>(p1.x, p1.y, c, s, irho, base), lim);
+        const unsigned l2 = min(vote_row<UNIT, CV>(p2.x, p2.y, c, s, irho, base), lim);
+        const unsigned l3 = min(vote_row<UNIT, CV>(p3.x, p3.y, c, s, irho, base), lim);
+        red_smem(acc_l + 128u * l0);
+        red_smem(acc_l + 128u * l1);
+        red_smem(acc_l + 128u * l2);
+        red_smem(acc_l + 128u * l3);
+    }
+    for (; j < n; j += step) {
+        const float2 p0 = pts[j];
+        red_smem(acc_l + 128u * min(vote_row<UNIT, CV>(p0.x, p0.y, c, s, irho, base), lim));
+    }
 }
 
 /* Conservative test: can any point of tile t vote into rho bins
@@ -202,15 +265,16 @@ struct VoteSmem {
 
 #define VOTE_FIXED ((sizeof(VoteSmem) + 127) / 128 * 128)
 
+/* the window's rows plus the dump row */
 size_t hl_vote_smem_bytes(int win_rows)
 {
-    return VOTE_FIXED + (size_t)win_rows * HL_SLICE * sizeof(int);
+    return VOTE_FIXED + (size_t)(win_rows + 1) * HL_SLICE * sizeof(int);
 }
 
 int hl_vote_max_rows(void)
 {
     const size_t cap = 227u * 1024u;
-    return (int)((cap - VOTE_FIXED) / (HL_SLICE * sizeof(int))) & ~7;
+    return (int)((cap - VOTE_FIXED) / (HL_SLICE * sizeof(int)) - 1) & ~7;
 }
 
 template <bool UNIT>
@@ -261,6 +325,9 @@ hl_vote_kernel(hl_vote_args a)
         const int rows = min(a.win_rows, a.R - w0);
         const int row_base = a.rho_min + w0;       /* rho bin of local row 0 */
         const unsigned lrows = (k < a.T) ? (unsigned)rows : 0u;
+        const int cv = row_base >= 1 ? CV_FLOOR
+                       : (row_base + rows - 1 <= -1 ? CV_CEIL : CV_EXACT);
+        const int vbase = cv == CV_EXACT ? row_base : RHO_MAGIC_BITS + row_base;
         const int klast = min(k0 + HL_SLICE - 1, a.T - 1);
         const float c0 = a.cosv[k0], s0 = a.sinv[k0];
         const float c1 = a.cosv[klast], s1 = a.sinv[klast];
@@ -450,26 +517,15 @@ hl_vote_kernel(hl_vote_args a)
                     seq++;
                     const int n = min(HL_VOTE_CHUNK, total - b * HL_VOTE_CHUNK);
                     const float2 *pts = sm.raw[slot];
-                    int j = cw;
-                    for (; j + 3 * ncons < n; j += 4 * ncons) {
-                        const float2 p0 = pts[j];
-                        const float2 p1 = pts[j + ncons];
-                        const float2 p2 = pts[j + 2 * ncons];
-                        const float2 p3 = pts[j + 3 * ncons];
-                        const unsigned l0 = (unsigned)(rho_of<UNIT>(p0.x, p0.y, c, s, a.irho) - row_base);
-                        const unsigned l1 = (unsigned)(rho_of<UNIT>(p1.x, p1.y, c, s, a.irho) - row_base);
-                        const unsigned l2 = (unsigned)(rho_of<UNIT>(p2.x, p2.y, c, s, a.irho) - row_base);
-                        const unsigned l3 = (unsigned)(rho_of<UNIT>(p3.x, p3.y, c, s, a.irho) - row_base);
-                        red_smem_if(acc_l + 128u * l0, l0, lrows);
-                        red_smem_if(acc_l + 128u * l1, l1, lrows);
-                        red_smem_if(acc_l + 128u * l2, l2, lrows);
-                        red_smem_if(acc_l + 128u * l3, l3, lrows);
-                    }
-                    for (; j < n; j += ncons) {
-                        const float2 p0 = pts[j];
-                        const unsigned l0 = (unsigned)(rho_of<UNIT>(p0.x, p0.y, c, s, a.irho) - row_base);
-                        red_smem_if(acc_l + 128u * l0, l0, lrows);
-                    }
+                    if (cv == CV_FLOOR)
+                        vote_batch<UNIT, CV_FLOOR>(pts, n, cw, ncons, c, s, a.irho,
+                                                   vbase, acc_l, lrows);
+                    else if (cv == CV_CEIL)
+                        vote_batch<UNIT, CV_CEIL>(pts, n, cw, ncons, c, s, a.irho,
+                                                  vbase, acc_l, lrows);
+                    else
+                        vote_batch<UNIT, CV_EXACT>(pts, n, cw, ncons, c, s, a.irho,
+                                                   vbase, acc_l, lrows);
                     __syncwarp();
                     if (lane == 0)
                         mbar_arrive(&sm.empty[slot]);
@@ -482,17 +538,26 @@ hl_vote_kernel(hl_vote_args a)
         int4 *dst4 = reinterpret_cast<int4 *>(a.acc);
         const int4 *src4 = reinterpret_cast<const int4 *>(s_acc);
         const int tp4 = a.Tp >> 2;
+        /* row 0 of the padding columns (thetas >= T) holds dumped votes */
         if (nparts == 1) {
             for (int i = tid; i < rows * (HL_SLICE / 4); i += nthr) {
                 const int rr = i >> 3, q = i & 7;
-                dst4[(size_t)(w0 + rr) * tp4 + (k0 >> 2) + q] = src4[i];
+                int4 v = src4[i];
+                if (rr == 0) {
+                    const int kq = k0 + 4 * q;
+                    if (kq >= a.T) v.x = 0;
+                    if (kq + 1 >= a.T) v.y = 0;
+                    if (kq + 2 >= a.T) v.z = 0;
+                    if (kq + 3 >= a.T) v.w = 0;
+                }
+                dst4[(size_t)(w0 + rr) * tp4 + (k0 >> 2) + q] = v;
             }
         } else {
             /* one part of a split block: add its nonzero counts into the
              * zeroed accumulator */
             for (int i = tid; i < rows * HL_SLICE; i += nthr) {
                 const int v = s_acc[i];
-                if (v)
+                if (v && k0 + (i & 31) < a.T)
                     atomicAdd(&a.acc[(size_t)(w0 + (i >> 5)) * a.Tp + k0 + (i & 31)], v);
             }
         }
