@@ -22,21 +22,23 @@
  * because the compaction pads every tile to an even number of float2
  * entries.  The runs, laid end to end, form the item's point stream.  Then
  * the CTA splits into one producer warp and consumer warps that meet only on
- * mbarriers: batch b is stream range [b*CHUNK, (b+1)*CHUNK); the producer's
- * lanes each copy one run's part of it into a ring of HL_VOTE_SLOTS
- * shared-memory slots with cp.async.bulk (TMA bulk copies completing on the
- * slot's full barrier), so a slot holds its batch gap-free; each consumer
- * warp votes its share of the slot straight from shared memory and arrives
- * on the slot's empty barrier, which the producer waits on before refilling
- * it.  No block-wide barrier separates batches.
+ * mbarriers: a batch is 32 points per consumer warp, batch b the stream
+ * range [b*B, (b+1)*B); the producer's lanes each copy one run's part of it
+ * into a ring of HL_VOTE_SLOTS shared-memory slots with cp.async.bulk (TMA
+ * bulk copies completing on the slot's full barrier), so a slot holds its
+ * batch gap-free; consumer warp i votes points [32i, 32i + 32) of the slot
+ * straight from shared memory and arrives on the slot's empty barrier, which
+ * the producer waits on before refilling it.  No block-wide barrier
+ * separates batches.
  * At the end of the item the block is stored with coalesced 128-byte rows
  * into acc[R][Tp]; every bin is written exactly once, so the global
  * accumulator needs no clearing.
  *
- * Per point and consumer warp: one broadcast shared load, two multiplies,
- * two adds (the second one rounds to an integer, see vote_row), one
- * subtract, one unsigned min and one address multiply-add, and one
- * red.shared -- nine issue slots and no branch per vote.
+ * Per point and consumer warp: half a broadcast shared load (16-byte loads
+ * of point pairs), two multiplies, two adds (the second one rounds to an
+ * integer, see vote_row), one subtract, one unsigned min, one address
+ * multiply-add and one red.shared -- under nine issue slots and no branch
+ * per vote.
  *
  * Bounds: every vote's row is clamped to the window's dump row (lanes past
  * the last theta to row 0 of their padding column, zeroed before the store),
@@ -172,6 +174,12 @@ __device__ __forceinline__ bool mbar_wait_sleep(unsigned long long *bar,
     return false;
 }
 
+/* 32 points (16 float4 pairs) of one consumer warp's share, no bounds */
+template <bool UNIT, int CV>
+__device__ __forceinline__ void vote_share32(const float2 *pts, float c,
+                                             float s, float irho, int base,
+                                             unsigned acc_l, unsigned lim);
+
 /* one vote, no returned value */
 __device__ __forceinline__ void red_smem(unsigned addr)
 {
@@ -207,6 +215,38 @@ __device__ __forceinline__ void vote_batch(const float2 *pts, int n, int j,
         const float2 p0 = pts[j];
         red_smem(acc_l + 128u * min(vote_row<UNIT, CV>(p0.x, p0.y, c, s, irho, base), lim));
     }
+}
+
+template <bool UNIT, int CV>
+__device__ __forceinline__ void vote_share32(const float2 *pts, float c,
+                                             float s, float irho, int base,
+                                             unsigned acc_l, unsigned lim)
+{
+    const float4 *q = reinterpret_cast<const float4 *>(pts);
+#pragma unroll
+    for (int i = 0; i < 16; i += 2) {
+        const float4 u = q[i], w = q[i + 1];
+        const unsigned l0 = min(vote_row<UNIT, CV>(u.x, u.y, c, s, irho, base), lim);
+        const unsigned l1 = min(vote_row<UNIT, CV>(u.z, u.w, c, s, irho, base), lim);
+        const unsigned l2 = min(vote_row<UNIT, CV>(w.x, w.y, c, s, irho, base), lim);
+        const unsigned l3 = min(vote_row<UNIT, CV>(w.z, w.w, c, s, irho, base), lim);
+        red_smem(acc_l + 128u * l0);
+        red_smem(acc_l + 128u * l1);
+        red_smem(acc_l + 128u * l2);
+        red_smem(acc_l + 128u * l3);
+    }
+}
+
+/* a consumer warp's share of a slot: up to 32 points starting at pts */
+template <bool UNIT, int CV>
+__device__ __forceinline__ void vote_share(const float2 *pts, int m, float c,
+                                           float s, float irho, int base,
+                                           unsigned acc_l, unsigned lim)
+{
+    if (m >= 32)
+        vote_share32<UNIT, CV>(pts, c, s, irho, base, acc_l, lim);
+    else if (m > 0)
+        vote_batch<UNIT, CV>(pts, m, 0, 1, c, s, irho, base, acc_l, lim);
 }
 
 /* Conservative test: can any point of tile t vote into rho bins
@@ -287,6 +327,8 @@ hl_vote_kernel(hl_vote_args a)
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nthr = blockDim.x, nwarps = nthr >> 5;
     const int ncons = nwarps - 1;               /* consumer warps 1..nwarps-1 */
+    /* points per batch: 32 per consumer warp (at most SLOT_CAP) */
+    const int batch = 32 * ncons;
     const int nslices = a.Tp / HL_SLICE;
 
     if (tid == 0) {
@@ -438,7 +480,7 @@ hl_vote_kernel(hl_vote_args a)
             }
             __syncthreads();
             const int total = sm.total;
-            const int nb_all = (total + HL_VOTE_CHUNK - 1) / HL_VOTE_CHUNK;
+            const int nb_all = (total + batch - 1) / batch;
             /* this part's share of the batches */
             const int b_lo = (int)((long long)nb_all * part / nparts);
             const int b_hi = (int)((long long)nb_all * (part + 1) / nparts);
@@ -451,7 +493,7 @@ hl_vote_kernel(hl_vote_args a)
                 int r0 = 0;
                 {
                     /* first run ending after this part's first point */
-                    const int s_first = b_lo * HL_VOTE_CHUNK;
+                    const int s_first = b_lo * batch;
                     int lo = 0, hi = max(nruns - 1, 0);
                     while (lo < hi) {
                         const int mid = (lo + hi) >> 1;
@@ -469,8 +511,8 @@ hl_vote_kernel(hl_vote_args a)
                         sm.timeout = 1;
                         atomicOr(a.status, HL_ST_VOTE_TIMEOUT);
                     }
-                    const int s0 = b * HL_VOTE_CHUNK;
-                    const int e0 = min(total, s0 + HL_VOTE_CHUNK);
+                    const int s0 = b * batch;
+                    const int e0 = min(total, s0 + batch);
                     if (lane == 0)
                         mbar_expect_tx(&sm.full[slot], (unsigned)(e0 - s0) * 8u);
                     __syncwarp();
@@ -515,17 +557,15 @@ hl_vote_kernel(hl_vote_args a)
                         atomicOr(a.status, HL_ST_VOTE_TIMEOUT);
                     }
                     seq++;
-                    const int n = min(HL_VOTE_CHUNK, total - b * HL_VOTE_CHUNK);
-                    const float2 *pts = sm.raw[slot];
+                    /* this warp's share: points [32 cw, 32 cw + 32) */
+                    const int m = min(32, total - b * batch - 32 * cw);
+                    const float2 *pts = sm.raw[slot] + 32 * cw;
                     if (cv == CV_FLOOR)
-                        vote_batch<UNIT, CV_FLOOR>(pts, n, cw, ncons, c, s, a.irho,
-                                                   vbase, acc_l, lrows);
+                        vote_share<UNIT, CV_FLOOR>(pts, m, c, s, a.irho, vbase, acc_l, lrows);
                     else if (cv == CV_CEIL)
-                        vote_batch<UNIT, CV_CEIL>(pts, n, cw, ncons, c, s, a.irho,
-                                                  vbase, acc_l, lrows);
+                        vote_share<UNIT, CV_CEIL>(pts, m, c, s, a.irho, vbase, acc_l, lrows);
                     else
-                        vote_batch<UNIT, CV_EXACT>(pts, n, cw, ncons, c, s, a.irho,
-                                                   vbase, acc_l, lrows);
+                        vote_share<UNIT, CV_EXACT>(pts, m, c, s, a.irho, vbase, acc_l, lrows);
                     __syncwarp();
                     if (lane == 0)
                         mbar_arrive(&sm.empty[slot]);
