@@ -48,7 +48,7 @@
 #include "hl_internal.h"
 
 #define FULL 0xffffffffu
-#define MBAR_SPIN_LIMIT (1 << 20)
+#define MBAR_WAIT_LIMIT (1 << 14)
 /* float2 entries of one ring slot (runs are gap-free: the compaction pads
  * every tile to an even number of points, 16 bytes) */
 #define SLOT_CAP HL_VOTE_CHUNK
@@ -135,32 +135,14 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src,
         "l"(src), "r"(bytes), "r"(smem_u32(bar))
         : "memory");
 }
-/* bounded wait for the phase with the given parity; false on time-out */
-__device__ __forceinline__ bool mbar_wait(unsigned long long *bar,
-                                          unsigned parity)
-{
-    const unsigned a = smem_u32(bar);
-    for (int i = 0; i < MBAR_SPIN_LIMIT; i++) {
-        unsigned ok;
-        asm volatile(
-            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], "
-            "%2; selp.u32 %0, 1, 0, p; }"
-            : "=r"(ok)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (ok)
-            return true;
-    }
-    return false;
-}
-
-/* the same wait, but each try_wait may suspend the warp for up to about a
- * microsecond instead of spinning, leaving issue slots to working warps */
+/* bounded wait for the phase with the given parity (false on time-out);
+ * each try_wait may suspend the warp for up to about a microsecond instead
+ * of spinning, leaving issue slots to working warps */
 __device__ __forceinline__ bool mbar_wait_sleep(unsigned long long *bar,
                                                 unsigned parity)
 {
     const unsigned a = smem_u32(bar);
-    for (int i = 0; i < MBAR_SPIN_LIMIT / 64; i++) {
+    for (int i = 0; i < MBAR_WAIT_LIMIT; i++) {
         unsigned ok;
         asm volatile(
             "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], "
@@ -507,7 +489,7 @@ hl_vote_kernel(hl_vote_args a)
                 for (int b = b_lo; b < b_hi; b++) {
                     const int slot = (int)(seq % HL_VOTE_SLOTS);
                     if (lane == 0 && seq >= HL_VOTE_SLOTS && !*(volatile int *)&sm.timeout &&
-                        !mbar_wait(&sm.empty[slot], ((seq / HL_VOTE_SLOTS) - 1u) & 1u)) {
+                        !mbar_wait_sleep(&sm.empty[slot], ((seq / HL_VOTE_SLOTS) - 1u) & 1u)) {
                         sm.timeout = 1;
                         atomicOr(a.status, HL_ST_VOTE_TIMEOUT);
                     }
