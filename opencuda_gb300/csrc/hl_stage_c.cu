@@ -11,8 +11,8 @@
  *   hl_finalize_kernel -- one CTA: top-M selection (MSD radix select when the
  *                        peaks exceed one 1024-key chunk), rank sort of the
  *                        chunk (keys are unique), the reference's float
- *                        decode, the pairwise suppression bitmask, and the
- *                        greedy merge as one warp's walk over that bitmask;
+ *                        decode, the pairwise predecessor bitmask, and the
+ *                        greedy merge resolved in parallel rounds;
  *                        writes min(survivors, linesmax) LineParam records.
  * Ranking is canonical: votes descending, then the reference raster index
  * (rho-major, theta-minor) ascending -- the reference's Shell sort
@@ -111,8 +111,14 @@ struct FinSmem {
     float ang[FIN_CHUNK];
     int dist[FIN_CHUNK];
     int votes[FIN_CHUNK];
-    unsigned mask[FIN_CHUNK][FIN_CHUNK / 32];   /* suppression rows */
+    /* earlier similar candidates; rows padded to 33 words so that threads
+     * on consecutive candidates hit different banks */
+    unsigned pred[FIN_CHUNK][FIN_CHUNK / 32 + 1];
     unsigned removed[FIN_CHUNK / 32];
+    unsigned dec[FIN_CHUNK / 32];    /* decided candidates */
+    unsigned alive[FIN_CHUNK / 32];  /* decided survivors */
+    unsigned ndec[FIN_CHUNK / 32];
+    unsigned nalive[FIN_CHUNK / 32];
     int surv[FIN_CHUNK];
     float sang[FIN_SCACHE];
     int sdist[FIN_SCACHE];
@@ -120,23 +126,37 @@ struct FinSmem {
     int misc[8];
 };
 
-/* The merge predicate, okano_3_0/HoughLine.cu:909-920: the angle test is in
- * float, the wrap-around angle M_PI - a - b in double, rounded to float. */
+/* The merge predicate, okano_3_0/HoughLine.cu:909-920, for an earlier line
+ * (ai, di) and a later one (aj, dj): the angle test is in float, the
+ * wrap-around angle M_PI - ai - aj in double, rounded to float.  The float
+ * estimate (pi_f - ai) - aj is within 4e-7 of that value (pi_f is 8.7e-8 from
+ * pi, two roundings of at most 1.2e-7 for operands below 2*pi, the final
+ * rounding is below 4e-9 near the threshold), so the double form -- slow on
+ * this GPU -- runs only when the estimate lies within 1e-6 of thresang. */
+/* the exact wrap-around test (double), kept out of line so that it is only
+ * ever executed, never evaluated speculatively */
+static __device__ __noinline__ bool wrap_exact(float ai, float aj,
+                                               float thresang)
+{
+    double t = __dsub_rn(__dsub_rn(3.14159265358979323846, (double)ai),
+                         (double)aj);
+    return __double2float_rn(fabs(t)) < thresang;
+}
+
 __device__ __forceinline__ bool similar(float ai, int di, float aj, int dj,
                                         int thresdis, float thresang)
 {
-    int dd = abs(di - dj);
-    if (dd < thresdis && fabsf(__fsub_rn(ai, aj)) < thresang)
-        return true;
-    int ds = abs(di + dj);
-    if (ds < thresdis) {
-        double t = __dsub_rn(__dsub_rn(3.14159265358979323846, (double)ai),
-                             (double)aj);
-        float da2 = __double2float_rn(fabs(t));
-        if (da2 < thresang)
-            return true;
-    }
-    return false;
+    /* evaluated without short-circuit branches; only the rare ambiguous
+     * wrap-around case branches */
+    const bool same = (abs(di - dj) < thresdis) &
+                      (fabsf(__fsub_rn(ai, aj)) < thresang);
+    const bool near = abs(di + dj) < thresdis;
+    const float est = fabsf(__fsub_rn(__fsub_rn(3.14159265f, ai), aj));
+    const bool lo = est < thresang - 1e-6f, hi = est > thresang + 1e-6f;
+    bool wrap = near & lo;
+    if (near & !lo & !hi)
+        wrap = wrap_exact(ai, aj, thresang);
+    return same | wrap;
 }
 
 /* Reference decode, okano_3_0/HoughLine.cu:882-897. */
@@ -223,20 +243,35 @@ hl_finalize_kernel(hl_final_args a, float scale)
             __syncthreads();
         }
         /* descending order by rank: keys are unique (the bin index is part of
-         * every key), so a key's rank is the number of larger keys; every
-         * thread ranks its keys against all m with broadcast reads, no
-         * barrier inside */
+         * every key), so a key's rank is the number of larger keys.  tpk
+         * consecutive threads (a power of two, as many as the block allows)
+         * rank one key, each against every tpk-th key, then sum by shuffles */
         __syncthreads();
-        for (int i = tid; i < m; i += blockDim.x) {
-            const unsigned long long ki = sm.keys[i];
-            int rank = 0;
-            int j = 0;
-            for (; j + 4 <= m; j += 4)
-                rank += (sm.keys[j] > ki) + (sm.keys[j + 1] > ki) +
-                        (sm.keys[j + 2] > ki) + (sm.keys[j + 3] > ki);
-            for (; j < m; j++)
-                rank += sm.keys[j] > ki;
-            sm.sorted[rank] = ki;
+        {
+            int tpk = 1;
+            while (tpk < 32 && 2 * tpk * m <= (int)blockDim.x)
+                tpk <<= 1;
+            const int per = blockDim.x / tpk;
+            const int part = tid & (tpk - 1);
+            for (int i0 = 0; i0 < m; i0 += per) {
+                const int i = i0 + tid / tpk;
+                const bool have = i < m;
+                const unsigned long long ki = have ? sm.keys[i] : 0ull;
+                int rank = 0;
+                if (have) {
+                    int j = part;
+                    for (; j + 3 * tpk < m; j += 4 * tpk)
+                        rank += (sm.keys[j] > ki) + (sm.keys[j + tpk] > ki) +
+                                (sm.keys[j + 2 * tpk] > ki) +
+                                (sm.keys[j + 3 * tpk] > ki);
+                    for (; j < m; j += tpk)
+                        rank += sm.keys[j] > ki;
+                }
+                for (int o = tpk >> 1; o > 0; o >>= 1)
+                    rank += __shfl_xor_sync(FULL, rank, o);
+                if (have && part == 0)
+                    sm.sorted[rank] = ki;
+            }
         }
         __syncthreads();
         taken += m;
@@ -272,57 +307,136 @@ hl_finalize_kernel(hl_final_args a, float scale)
                 atomicOr(&sm.removed[i >> 5], 1u << (i & 31));
         }
         __syncthreads();
-        /* suppression bitmask: bit j of mask[i] <=> i < j and similar(i, j).
-         * One thread per (row i, word w), word-major so a warp's threads share
-         * w and read the word's 32 candidates with broadcast loads; the 32
-         * tests of a word are independent (no serial chain). */
-        for (int e = tid; e < m * W; e += blockDim.x) {
-            const int wd = e / m, i = e - wd * m;
-            const int j0 = wd << 5;
-            unsigned bits = 0u;
-            if (j0 + 31 > i) {
-                const float ai = sm.ang[i];
-                const int di = sm.dist[i];
-                const int jn = min(32, m - j0);
-#pragma unroll 8
-                for (int b = 0; b < 32; b++) {
-                    const int j = j0 + b;
-                    const bool hit = b < jn && j > i &&
-                                     similar(ai, di, sm.ang[j], sm.dist[j],
-                                             a.thresdis, a.thresang);
-                    bits |= (unsigned)hit << b;
+        /* predecessor bitmask: bit j of pred[i] <=> j < i and similar(j, i).
+         * Only the words holding some j < i are built: entry (i, wd) for
+         * 32 wd < i, enumerated word by word.  Four adjacent threads share
+         * an entry (8 tests each, OR-ed by shuffles); the threads of a warp
+         * mostly share wd and read the word's candidates with broadcast
+         * loads. */
+        {
+            int nent = 0;
+            for (int wd = 0; wd < W; wd++)
+                nent += max(0, m - 32 * wd - 1);
+            const int span = (4 * nent + 31) & ~31;
+            for (int e = tid; e < span; e += blockDim.x) {
+                const int q = e & 3, en = e >> 2;
+                unsigned bits = 0u;
+                int i = 0, wd = 0, jn = 0;
+                if (en < nent) {
+                    int rem = en;
+                    while (rem >= m - 32 * wd - 1) {
+                        rem -= m - 32 * wd - 1;
+                        wd++;
+                    }
+                    i = 32 * wd + 1 + rem;
+                    jn = min(32, i - (wd << 5));
                 }
+                {
+                    /* every lane runs the same 8 tests (invalid ones masked
+                     * afterwards), so the rare exact wrap-around test is a
+                     * warp-uniform branch */
+                    const int j0 = wd << 5;
+                    const float ai = sm.ang[i];
+                    const int di = sm.dist[i];
+#pragma unroll
+                    for (int b = 8 * q; b < 8 * q + 8; b++) {
+                        const int j = min(j0 + b, m - 1);
+                        const float aj = sm.ang[j];
+                        const int dj = sm.dist[j];
+                        const bool same = (abs(dj - di) < a.thresdis) &
+                                          (fabsf(__fsub_rn(aj, ai)) < a.thresang);
+                        const bool near = abs(dj + di) < a.thresdis;
+                        const float est = fabsf(__fsub_rn(__fsub_rn(3.14159265f, aj), ai));
+                        const bool lo = est < a.thresang - 1e-6f;
+                        const bool hi = est > a.thresang + 1e-6f;
+                        bool wrap = near & lo;
+                        const bool amb = near & !lo & !hi & (b < jn);
+                        if (__any_sync(FULL, amb)) {
+                            if (amb)
+                                wrap = wrap_exact(aj, ai, a.thresang);
+                        }
+                        bits |= (unsigned)((same | wrap) & (b < jn)) << b;
+                    }
+                }
+                bits |= __shfl_xor_sync(FULL, bits, 1);
+                bits |= __shfl_xor_sync(FULL, bits, 2);
+                if (en < nent && q == 0)
+                    sm.pred[i][wd] = bits;
             }
-            sm.mask[i][wd] = bits;
+        }
+        /* The greedy pass of okano_3_0/HoughLine.cu:900-927 keeps candidate i
+         * iff it was not removed by an earlier chunk and no earlier kept
+         * candidate is similar to it.  Resolved in rounds: an undecided
+         * candidate with a kept predecessor is dropped, one whose
+         * predecessors are all decided (none kept) is kept.  Each round
+         * decides at least the first undecided candidate; in practice a few
+         * rounds decide them all. */
+        if (tid < 32) {
+            unsigned d = (tid < W) ? sm.removed[tid] : 0xffffffffu;
+            if (tid == W - 1 && (m & 31))
+                d |= ~((1u << (m & 31)) - 1u);
+            sm.dec[tid] = d;
+            sm.alive[tid] = 0u;
+            sm.ndec[tid] = 0u;
+            sm.nalive[tid] = 0u;
         }
         __syncthreads();
-        /* the greedy pass of okano_3_0/HoughLine.cu:900-927 over the chunk:
-         * one warp jumps from survivor to survivor (lane w holds word w of
-         * the removed set), OR-ing each survivor's suppression row in */
-        if (tid < 32) {
-            const int lane = tid;
-            unsigned rem = (lane < W) ? sm.removed[lane] : 0xffffffffu;
-            if (lane == W - 1 && (m & 31))
-                rem |= ~((1u << (m & 31)) - 1u);
-            int ns = 0;
-            const int room = K - S;
-            while (ns < room) {
-                const unsigned avail = ~rem;
-                const unsigned lanes = __ballot_sync(FULL, avail != 0u);
-                if (!lanes)
-                    break;
-                const int wl = __ffs(lanes) - 1;
-                const unsigned wv = __shfl_sync(FULL, avail, wl);
-                const int i = (wl << 5) + __ffs(wv) - 1;
-                if (lane == 0)
-                    sm.surv[ns] = i;
-                ns++;
-                rem |= (lane < W) ? sm.mask[i][lane] : 0u;
-                if (lane == wl)
-                    rem |= 1u << (i & 31);
+        for (int round = 0; round < m; round++) {
+            for (int i = tid; i < m; i += blockDim.x) {
+                const int iw = i >> 5;
+                const unsigned ib = 1u << (i & 31);
+                if (sm.dec[iw] & ib)
+                    continue;
+                bool all = true, kill = false;
+                for (int w = 0; w < ((i + 31) >> 5); w++) {
+                    const unsigned pw = sm.pred[i][w];
+                    all = all && !(pw & ~sm.dec[w]);
+                    kill = kill || (pw & sm.alive[w]);
+                }
+                if (kill) {
+                    atomicOr(&sm.ndec[iw], ib);
+                } else if (all) {
+                    atomicOr(&sm.ndec[iw], ib);
+                    atomicOr(&sm.nalive[iw], ib);
+                }
             }
-            if (lane == 0)
-                sm.misc[3] = ns;
+            __syncthreads();
+            if (tid < 32) {
+                const unsigned d = sm.dec[tid] | sm.ndec[tid];
+                sm.dec[tid] = d;
+                sm.alive[tid] |= sm.nalive[tid];
+                sm.ndec[tid] = 0u;
+                sm.nalive[tid] = 0u;
+                const bool done = __all_sync(FULL, d == 0xffffffffu);
+                if (tid == 0)
+                    sm.misc[4] = done;
+            }
+            __syncthreads();
+            if (sm.misc[4])
+                break;
+        }
+        /* survivors in rank order, at most room of them */
+        {
+            const int room = K - S;
+            for (int i = tid; i < m; i += blockDim.x) {
+                const int iw = i >> 5;
+                const unsigned al = sm.alive[iw];
+                if ((al >> (i & 31)) & 1u) {
+                    int q = __popc(al & ((1u << (i & 31)) - 1u));
+                    for (int w = 0; w < iw; w++)
+                        q += __popc(sm.alive[w]);
+                    if (q < room)
+                        sm.surv[q] = i;
+                }
+            }
+            if (tid < 32) {
+                int c = __popc(sm.alive[tid]);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1)
+                    c += __shfl_xor_sync(FULL, c, o);
+                if (tid == 0)
+                    sm.misc[3] = min(c, room);
+            }
         }
         __syncthreads();
         const int ns = sm.misc[3];
