@@ -148,7 +148,7 @@ __device__ int lookback(unsigned long long *state, int tile, int total,
  * for every 16 KB of image. */
 #define CT_GROUP HL_COMPACT_GROUP
 
-__global__ void __launch_bounds__(HL_COMPACT_THREADS)
+__global__ void __launch_bounds__(HL_COMPACT_THREADS, 8)
 hl_compact_kernel(hl_compact_args a)
 {
     __shared__ int s_grp;
@@ -168,32 +168,37 @@ hl_compact_kernel(hl_compact_args a)
         return;
     const int r = tid >> 3, ch = tid & 7;
 
+    /* this thread's 16 pixels of tile q: row ty*32 + r, columns
+     * tx*128 + 16*ch .. +15 (recomputed where needed, to keep the live
+     * registers low enough for eight CTAs per SM) */
+    const int tx0 = (grp * CT_GROUP) % a.tiles_x, ty0 = (grp * CT_GROUP) / a.tiles_x;
+#define CT_TILE_XY(q, xx, yy)                                                  \
+    const int xx = ((tx0 + (q)) % a.tiles_x) * HL_TILE_W + ch * 16;            \
+    const int yy = (ty0 + (tx0 + (q)) / a.tiles_x) * HL_TILE_H + r
     /* all loads first */
     uint4 v[CT_GROUP];
-    int yq[CT_GROUP], xq[CT_GROUP];
-    bool vec[CT_GROUP], any[CT_GROUP];
 #pragma unroll
     for (int q = 0; q < CT_GROUP; q++) {
-        const int tile = grp * CT_GROUP + q;
-        const int tx = tile % a.tiles_x, ty = tile / a.tiles_x;
-        yq[q] = ty * HL_TILE_H + r;
-        xq[q] = tx * HL_TILE_W + ch * 16;
-        any[q] = tile < a.ntiles && yq[q] < a.roi.h && xq[q] < a.roi.w;
-        const uint8_t *p = a.roi.base + (size_t)yq[q] * (size_t)a.roi.pitch + xq[q];
-        vec[q] = any[q] && xq[q] + 16 <= a.roi.w && (((uintptr_t)p) & 15u) == 0;
-        v[q] = vec[q] ? __ldcs((const uint4 *)p) : make_uint4(0, 0, 0, 0);
+        CT_TILE_XY(q, xq, yq);
+        const bool any = grp * CT_GROUP + q < a.ntiles && yq < a.roi.h && xq < a.roi.w;
+        const uint8_t *p = a.roi.base + (size_t)yq * (size_t)a.roi.pitch + xq;
+        const bool vec = any && xq + 16 <= a.roi.w && (((uintptr_t)p) & 15u) == 0;
+        v[q] = vec ? __ldcs((const uint4 *)p) : make_uint4(0, 0, 0, 0);
     }
     uint32_t m[CT_GROUP];
     unsigned long long cnt4 = 0;   /* four 16-bit counts, tile q in bits 16q */
 #pragma unroll
     for (int q = 0; q < CT_GROUP; q++) {
+        CT_TILE_XY(q, xq, yq);
+        const bool any = grp * CT_GROUP + q < a.ntiles && yq < a.roi.h && xq < a.roi.w;
+        const uint8_t *p = a.roi.base + (size_t)yq * (size_t)a.roi.pitch + xq;
+        const bool vec = any && xq + 16 <= a.roi.w && (((uintptr_t)p) & 15u) == 0;
         uint32_t mm = 0;
-        if (vec[q]) {
+        if (vec) {
             mm = eq255x4(v[q].x) | (eq255x4(v[q].y) << 4) |
                  (eq255x4(v[q].z) << 8) | (eq255x4(v[q].w) << 12);
-        } else if (any[q]) {
-            const uint8_t *p = a.roi.base + (size_t)yq[q] * (size_t)a.roi.pitch + xq[q];
-            const int lim = min(16, a.roi.w - xq[q]);
+        } else if (any) {
+            const int lim = min(16, a.roi.w - xq);
             for (int i = 0; i < lim; i++)
                 mm |= (uint32_t)(p[i] == 255) << i;
         }
@@ -257,19 +262,21 @@ hl_compact_kernel(hl_compact_args a)
     const unsigned long long ex4 = s_wsum[warp] + incl - cnt4;
 #pragma unroll
     for (int q = 0; q < CT_GROUP; q++) {
+        CT_TILE_XY(q, xq, yq);
         uint32_t mm = m[q];
         int pos = s_tbase[q] + (int)((ex4 >> (16 * q)) & 0xffffu);
-        const uint32_t yy = (uint32_t)yq[q] << 16;
+        const uint32_t yy = (uint32_t)yq << 16;
         while (mm) {
             const int bb = __ffs(mm) - 1;
             mm &= mm - 1;
             if (a.pts_f2)
-                a.pts_f2[pos] = make_float2((float)(xq[q] + bb), (float)yq[q]);
+                a.pts_f2[pos] = make_float2((float)(xq + bb), (float)yq);
             else
-                a.pts[pos] = (uint32_t)(xq[q] + bb) | yy;
+                a.pts[pos] = (uint32_t)(xq + bb) | yy;
             pos++;
         }
     }
+#undef CT_TILE_XY
     /* the sentinel (1e30, 0) never votes inside an accumulator: its rho is
      * 1e30 * cos(theta_k), and cosf of a float angle is never 0 */
     if (a.pts_f2 && tid < CT_GROUP && (s_tcnt[tid] & 1))
