@@ -521,6 +521,10 @@ static int run_ab(hl_handle *h, const hl_roi &roi, const hl_geom &g,
     ca.roi = roi;
     ca.tiles_x = g.tiles_x;
     ca.ntiles = ntiles;
+    ca.imgs = nullptr;
+    ca.group_img = nullptr;
+    ca.nimg = 0;
+    ca.ngroups = 0;
     ca.tile_state = h->d_tile_state;
     ca.ticket = reinterpret_cast<unsigned *>(h->d_counters + 3);
     ca.ticket_base = h->ticket_base;
@@ -542,22 +546,24 @@ static int run_ab(hl_handle *h, const hl_roi &roi, const hl_geom &g,
     prof_mark(h, 1, s);
 
     hl_vote_args va;
-    va.pts = reinterpret_cast<const float2 *>(h->d_pts);
-    va.tile_off = h->d_tile_off;
-    va.ntiles = ntiles;
-    va.tiles_x = g.tiles_x;
-    va.w = roi.w;
-    va.h = roi.h;
+    va.imgs = nullptr;
+    va.img0.pts = reinterpret_cast<const float2 *>(h->d_pts);
+    va.img0.tile_off = h->d_tile_off;
+    va.img0.ntiles = ntiles;
+    va.img0.tiles_x = g.tiles_x;
+    va.img0.w = roi.w;
+    va.img0.h = roi.h;
+    va.img0.rho_min = g.rho_min;
+    va.img0.R = g.numrho;
+    va.img0.pad = 0;
+    va.img0.acc = h->d_acc;
     va.cosv = h->d_cos;
     va.sinv = h->d_sin;
     va.T = h->T;
     va.Tp = h->Tp;
-    va.rho_min = g.rho_min;
-    va.R = g.numrho;
     int threads;
-    vote_shape(h, g.numrho, &va.win_rows, &va.nwin, &threads);
+    vote_shape(h, g.numrho, &va.win_rows, &va.img0.nwin, &threads);
     va.irho = (float)(1.0 / h->p.derho);   /* okano_3_0/HoughLine.cu:107 */
-    va.acc = h->d_acc;
     va.status = h->d_counters + 1;
     /* persistent CTAs: as many as fit (one per SM at 1024 threads) */
     const size_t smem = hl_vote_smem_bytes(va.win_rows);
@@ -566,7 +572,7 @@ static int run_ab(hl_handle *h, const hl_roi &roi, const hl_geom &g,
     const int ctas = std::max(h->sms, 1) * per_sm;
     int split = 0;
     int rc = vote_items(h, roi.w, roi.h, g.rho_min, g.numrho, va.win_rows,
-                        va.nwin, ctas, &va.items, &va.nitems, &split);
+                        va.img0.nwin, ctas, &va.items, &va.nitems, &split);
     if (rc != HL_NO_ERROR)
         return rc;
     if (split)   /* parts of a split block add into the accumulator */
@@ -588,37 +594,42 @@ static int run_c(hl_handle *h, const hl_geom &g, int linesmax,
                  int *launches)
 {
     hl_peak_args pa;
-    pa.acc = h->d_acc;
-    pa.R = g.numrho;
+    pa.imgs = nullptr;
+    pa.img0.acc = h->d_acc;
+    pa.img0.keys = h->d_keys;
+    pa.img0.ncand = h->d_counters + 0;
+    pa.img0.R = g.numrho;
+    pa.img0.cap = key_cap(h);
+    pa.chunks = nullptr;
+    pa.nchunks = (g.numrho + HL_PEAK_ROWS - 1) / HL_PEAK_ROWS;
     pa.T = h->T;
     pa.Tp = h->Tp;
     pa.threshold = h->p.threshold;
-    pa.keys = h->d_keys;
-    pa.ncand = h->d_counters + 0;
-    pa.cap = key_cap(h);
     pa.status = h->d_counters + 1;
     CK(hl_launch_peaks(&pa, s));
     (*launches)++;
     prof_mark(h, 3, s);
 
     hl_final_args fa;
-    fa.keys = h->d_keys;
-    fa.ncand = h->d_counters + 0;
-    fa.cap = pa.cap;
+    fa.imgs = nullptr;
+    fa.img0.keys = h->d_keys;
+    fa.img0.ncand = h->d_counters + 0;
+    fa.img0.cap = pa.img0.cap;
+    fa.img0.rho_min = g.rho_min;
+    fa.img0.ref_numrho = g.ref_numrho;
+    fa.img0.pad = 0;
     fa.T = h->T;
-    fa.rho_min = g.rho_min;
-    fa.ref_numrho = g.ref_numrho;
     fa.detheta = h->p.detheta;
     fa.thresdis = h->p.thresdis;
     fa.thresang = h->p.thresang;
     fa.linesmax = linesmax;
     fa.hdr = reinterpret_cast<hl_result_hdr *>(h->d_result);
-    fa.lines = lines_dev ? lines_dev
-                         : reinterpret_cast<hl_line *>(h->d_result +
-                                                       sizeof(hl_result_hdr));
+    fa.img0.lines = lines_dev ? lines_dev
+                              : reinterpret_cast<hl_line *>(h->d_result +
+                                                            sizeof(hl_result_hdr));
     fa.status = h->d_counters + 1;
-    fa.count_out = count_dev;
-    CK(hl_launch_finalize(&fa, s));
+    fa.img0.count_out = count_dev;
+    CK(hl_launch_finalize(&fa, 1, s));
     (*launches)++;
     prof_mark(h, 4, s);
     return HL_NO_ERROR;
@@ -746,6 +757,10 @@ extern "C" int hl_compact(hl_handle *h, const hl_image_desc *img,
     ca.roi = roi;
     ca.tiles_x = g.tiles_x;
     ca.ntiles = ntiles;
+    ca.imgs = nullptr;
+    ca.group_img = nullptr;
+    ca.nimg = 0;
+    ca.ngroups = 0;
     ca.tile_state = h->d_tile_state;
     ca.ticket = reinterpret_cast<unsigned *>(h->d_counters + 3);
     ca.ticket_base = h->ticket_base;

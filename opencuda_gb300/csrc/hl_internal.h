@@ -42,9 +42,25 @@ typedef struct hl_roi {
     int w, h;
 } hl_roi;
 
-typedef struct hl_compact_args {
+/* One image of a batched compaction: its tiles occupy [tile_base, +ntiles)
+ * of the batch's tile_off array and its 4-tile groups [group_base, +ngroups)
+ * of the batch's group space; the point list and the look-back run over the
+ * whole batch, so the images' points are laid end to end. */
+typedef struct hl_compact_img {
     hl_roi roi;
     int tiles_x, ntiles;
+    int tile_base, group_base, ngroups;
+    int pad;
+} hl_compact_img;
+
+typedef struct hl_compact_args {
+    /* one image (imgs == NULL) ... */
+    hl_roi roi;
+    int tiles_x, ntiles;
+    /* ... or a batch: group g belongs to image group_img[g] */
+    const hl_compact_img *imgs;
+    const int *group_img;
+    int nimg, ngroups;
     unsigned long long *tile_state;  /* [ntiles], epoch-tagged */
     unsigned int *ticket;            /* monotonically increasing counter */
     unsigned int ticket_base;        /* value of *ticket at launch */
@@ -56,23 +72,32 @@ typedef struct hl_compact_args {
     int *status;
 } hl_compact_args;
 
-typedef struct hl_vote_args {
+/* One image of a vote launch. */
+typedef struct hl_vote_img {
     const float2 *pts;        /* (x, y) of every edge point, tile-major */
-    const int *tile_off;
+    const int *tile_off;      /* the image's [ntiles + 1] tile offsets */
     int ntiles, tiles_x;
     int w, h;                 /* ROI size (tile clipping) */
+    int rho_min, R;
+    int nwin;                 /* rho windows of win_rows rows */
+    int pad;
+    int32_t *acc;             /* [R][Tp] */
+} hl_vote_img;
+
+typedef struct hl_vote_args {
+    const hl_vote_img *imgs;  /* per image, or NULL: the one image img0 */
+    hl_vote_img img0;
     const float *cosv, *sinv; /* [theta_pad] */
     int T, Tp;
-    int rho_min, R;
-    int win_rows, nwin;       /* rho window per work item */
+    int win_rows;             /* rho window per work item */
     float irho;
-    int32_t *acc;             /* [R][Tp] */
     int *status;
     /* persistent scheduling: work items are taken in the order items[]
      * (heaviest first) from a monotonically increasing counter.  An item is
-     * one part of a (slice, window) block: .x = slice + nslices * window,
-     * .y = part | nparts << 16; a block split into several parts adds its
-     * partial counts into a zeroed accumulator with red.global */
+     * one part of a (slice, window) block of one image: .x = block | image
+     * << 16 with block = slice + nslices * window, .y = part | nparts << 16;
+     * a block split into several parts adds its partial counts into a zeroed
+     * accumulator with red.global */
     const int2 *items;
     int nitems;
     unsigned *work;           /* counter */
@@ -91,29 +116,50 @@ typedef struct hl_vote_args {
 /* largest rho window (rows) one CTA can hold next to its staging */
 int hl_vote_max_rows(void);
 
-typedef struct hl_peak_args {
+/* One image of a peak pass. */
+typedef struct hl_peak_img {
     const int32_t *acc;       /* [R][Tp] */
-    int R, T, Tp;
-    int threshold;
     unsigned long long *keys; /* votes << 32 | ~tight_index */
     int *ncand;
-    int cap;
+    int R, cap;
+} hl_peak_img;
+
+/* rows of an accumulator one peak-pass chunk covers */
+#define HL_PEAK_ROWS 8
+
+typedef struct hl_peak_args {
+    const hl_peak_img *imgs;  /* per image, or NULL: the one image img0 */
+    hl_peak_img img0;
+    const int2 *chunks;       /* {image, first row}, HL_PEAK_ROWS rows each;
+                                 NULL: chunk c is rows c * HL_PEAK_ROWS.. of
+                                 img0 */
+    int nchunks;
+    int T, Tp;
+    int threshold;
     int *status;
 } hl_peak_args;
 
-typedef struct hl_final_args {
+/* One image of a finalize launch (one CTA per image). */
+typedef struct hl_final_img {
     const unsigned long long *keys;
     int *ncand;               /* read, then reset to 0 for the next call */
     int cap;
-    int T, rho_min, ref_numrho;
+    int rho_min, ref_numrho;
+    int pad;
+    hl_line *lines;           /* out: [linesmax] */
+    int *count_out;           /* out: lines written, or NULL */
+} hl_final_img;
+
+typedef struct hl_final_args {
+    const hl_final_img *imgs; /* per image (CTA), or NULL: the one image img0 */
+    hl_final_img img0;
+    int T;
     double detheta;
     int thresdis;
     float thresang;
     int linesmax;
-    hl_line *lines;           /* out: [linesmax] */
-    hl_result_hdr *hdr;       /* out */
-    int *status;              /* read, then reset to 0 */
-    int *count_out;           /* optional extra copy of hdr->count */
+    hl_result_hdr *hdr;       /* out (one image), or NULL */
+    int *status;              /* read; reset to 0 when hdr is set */
 } hl_final_args;
 
 /* launchers (return cudaGetLastError() after the launch) */
@@ -130,7 +176,7 @@ cudaError_t hl_launch_vote_points(const int *xy, int n, const float *cosv,
                                   float irho, int32_t *acc, int threads,
                                   cudaStream_t s);
 cudaError_t hl_launch_peaks(const hl_peak_args *a, cudaStream_t s);
-cudaError_t hl_launch_finalize(const hl_final_args *a, cudaStream_t s);
+cudaError_t hl_launch_finalize(const hl_final_args *a, int nimg, cudaStream_t s);
 cudaError_t hl_launch_to_tight(const int32_t *acc, int R, int T, int Tp,
                                int32_t *out, cudaStream_t s);
 cudaError_t hl_launch_to_ref(const int32_t *acc, int R, int T, int Tp,

@@ -82,6 +82,10 @@ extern "C" int hl_compact_noalloc(const hl_image_desc *img, uint32_t *pts_dev,
     ca.roi.h = h;
     ca.tiles_x = tiles_x;
     ca.ntiles = (int)ntiles;
+    ca.imgs = nullptr;
+    ca.group_img = nullptr;
+    ca.nimg = 0;
+    ca.ngroups = 0;
     ca.ticket = reinterpret_cast<unsigned *>(scratch);
     ca.ticket_base = 0;
     ca.status = reinterpret_cast<int *>(scratch + 1);

@@ -152,37 +152,51 @@ __global__ void __launch_bounds__(HL_COMPACT_THREADS, 8)
 hl_compact_kernel(hl_compact_args a)
 {
     __shared__ int s_grp;
+    __shared__ hl_compact_img s_im;
     __shared__ unsigned long long s_wsum[HL_COMPACT_THREADS / 32];
     __shared__ int s_tbase[CT_GROUP];
     __shared__ int s_tcnt[CT_GROUP];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int ngroups = (a.ntiles + CT_GROUP - 1) / CT_GROUP;
+    const int ngroups = a.imgs ? a.ngroups : (a.ntiles + CT_GROUP - 1) / CT_GROUP;
 
     /* Groups are taken in ticket order, so every predecessor of a group is
      * already resident when the group looks back: the waits always end. */
-    if (tid == 0)
-        s_grp = (int)(atomicAdd(a.ticket, 1u) - a.ticket_base);
+    if (tid == 0) {
+        const int g = (int)(atomicAdd(a.ticket, 1u) - a.ticket_base);
+        s_grp = g;
+        if (!a.imgs) {
+            s_im.roi = a.roi;
+            s_im.tiles_x = a.tiles_x;
+            s_im.ntiles = a.ntiles;
+            s_im.tile_base = 0;
+            s_im.group_base = 0;
+            s_im.ngroups = ngroups;
+        } else if (g >= 0 && g < ngroups) {
+            s_im = a.imgs[a.group_img[g]];
+        }
+    }
     __syncthreads();
-    const int grp = s_grp;
-    if (grp < 0 || grp >= ngroups)
+    const int ggrp = s_grp;              /* group in the batch (look-back) */
+    if (ggrp < 0 || ggrp >= ngroups)
         return;
+    const int grp = ggrp - s_im.group_base;   /* group in its image */
     const int r = tid >> 3, ch = tid & 7;
 
     /* this thread's 16 pixels of tile q: row ty*32 + r, columns
      * tx*128 + 16*ch .. +15 (recomputed where needed, to keep the live
      * registers low enough for eight CTAs per SM) */
-    const int tx0 = (grp * CT_GROUP) % a.tiles_x, ty0 = (grp * CT_GROUP) / a.tiles_x;
+    const int tx0 = (grp * CT_GROUP) % s_im.tiles_x, ty0 = (grp * CT_GROUP) / s_im.tiles_x;
 #define CT_TILE_XY(q, xx, yy)                                                  \
-    const int xx = ((tx0 + (q)) % a.tiles_x) * HL_TILE_W + ch * 16;            \
-    const int yy = (ty0 + (tx0 + (q)) / a.tiles_x) * HL_TILE_H + r
+    const int xx = ((tx0 + (q)) % s_im.tiles_x) * HL_TILE_W + ch * 16;         \
+    const int yy = (ty0 + (tx0 + (q)) / s_im.tiles_x) * HL_TILE_H + r
     /* all loads first */
     uint4 v[CT_GROUP];
 #pragma unroll
     for (int q = 0; q < CT_GROUP; q++) {
         CT_TILE_XY(q, xq, yq);
-        const bool any = grp * CT_GROUP + q < a.ntiles && yq < a.roi.h && xq < a.roi.w;
-        const uint8_t *p = a.roi.base + (size_t)yq * (size_t)a.roi.pitch + xq;
-        const bool vec = any && xq + 16 <= a.roi.w && (((uintptr_t)p) & 15u) == 0;
+        const bool any = grp * CT_GROUP + q < s_im.ntiles && yq < s_im.roi.h && xq < s_im.roi.w;
+        const uint8_t *p = s_im.roi.base + (size_t)yq * (size_t)s_im.roi.pitch + xq;
+        const bool vec = any && xq + 16 <= s_im.roi.w && (((uintptr_t)p) & 15u) == 0;
         v[q] = vec ? __ldcs((const uint4 *)p) : make_uint4(0, 0, 0, 0);
     }
     uint32_t m[CT_GROUP];
@@ -190,15 +204,15 @@ hl_compact_kernel(hl_compact_args a)
 #pragma unroll
     for (int q = 0; q < CT_GROUP; q++) {
         CT_TILE_XY(q, xq, yq);
-        const bool any = grp * CT_GROUP + q < a.ntiles && yq < a.roi.h && xq < a.roi.w;
-        const uint8_t *p = a.roi.base + (size_t)yq * (size_t)a.roi.pitch + xq;
-        const bool vec = any && xq + 16 <= a.roi.w && (((uintptr_t)p) & 15u) == 0;
+        const bool any = grp * CT_GROUP + q < s_im.ntiles && yq < s_im.roi.h && xq < s_im.roi.w;
+        const uint8_t *p = s_im.roi.base + (size_t)yq * (size_t)s_im.roi.pitch + xq;
+        const bool vec = any && xq + 16 <= s_im.roi.w && (((uintptr_t)p) & 15u) == 0;
         uint32_t mm = 0;
         if (vec) {
             mm = eq255x4(v[q].x) | (eq255x4(v[q].y) << 4) |
                  (eq255x4(v[q].z) << 8) | (eq255x4(v[q].w) << 12);
         } else if (any) {
-            const int lim = min(16, a.roi.w - xq);
+            const int lim = min(16, s_im.roi.w - xq);
             for (int i = 0; i < lim; i++)
                 mm |= (uint32_t)(p[i] == 255) << i;
         }
@@ -239,7 +253,7 @@ hl_compact_kernel(hl_compact_args a)
             const int cq = (int)((tot4 >> (16 * q)) & 0xffffu);
             total += cq + (cq & pad);
         }
-        const int excl = lookback(a.tile_state, grp, total, a.epoch, a.status);
+        const int excl = lookback(a.tile_state, ggrp, total, a.epoch, a.status);
         if (lane == 0) {
             int run = excl;
 #pragma unroll
@@ -248,14 +262,15 @@ hl_compact_kernel(hl_compact_args a)
                 const int cq = (int)((tot4 >> (16 * q)) & 0xffffu);
                 s_tbase[q] = run;
                 s_tcnt[q] = cq;
-                if (tile < a.ntiles)
-                    a.tile_off[tile] = run;
+                if (tile < s_im.ntiles)
+                    a.tile_off[s_im.tile_base + tile] = run;
                 run += cq + (cq & pad);
             }
-            if (grp == ngroups - 1) {
-                a.tile_off[a.ntiles] = run;
+            /* the image's end (equal to the next image's start) */
+            if (grp == s_im.ngroups - 1)
+                a.tile_off[s_im.tile_base + s_im.ntiles] = run;
+            if (ggrp == ngroups - 1)
                 *a.count = run;
-            }
         }
     }
     __syncthreads();
@@ -285,7 +300,7 @@ hl_compact_kernel(hl_compact_args a)
 
 cudaError_t hl_launch_compact(const hl_compact_args *a, cudaStream_t s)
 {
-    const int ngroups = (a->ntiles + CT_GROUP - 1) / CT_GROUP;
+    const int ngroups = a->imgs ? a->ngroups : (a->ntiles + CT_GROUP - 1) / CT_GROUP;
     hl_compact_kernel<<<ngroups, HL_COMPACT_THREADS, 0, s>>>(*a);
     return cudaGetLastError();
 }

@@ -31,7 +31,7 @@
 
 /* append one peak key (warp-aggregated: one global atomic per warp) */
 __device__ __forceinline__ void push_key(bool is, unsigned long long key,
-                                         const hl_peak_args &a)
+                                         const hl_peak_img &im, int *status)
 {
     const int lane = threadIdx.x & 31;
     const unsigned b = __ballot_sync(FULL, is);
@@ -40,52 +40,61 @@ __device__ __forceinline__ void push_key(bool is, unsigned long long key,
     const int leader = __ffs(b) - 1;
     int base = 0;
     if (lane == leader)
-        base = atomicAdd(a.ncand, __popc(b));
+        base = atomicAdd(im.ncand, __popc(b));
     base = __shfl_sync(FULL, base, leader);
     if (is) {
         const int pos = base + __popc(b & ((1u << lane) - 1u));
-        if (pos < a.cap)
-            a.keys[pos] = key;
+        if (pos < im.cap)
+            im.keys[pos] = key;
         else
-            atomicOr(a.status, HL_ST_CAND_OVERFLOW);
+            atomicOr(status, HL_ST_CAND_OVERFLOW);
     }
 }
 
-/* One thread per 4 consecutive bins of a row (one 16-byte streaming load);
- * the neighbours are read only for bins above the threshold, which are rare,
- * so the kernel is one pass over the accumulator at HBM speed. */
+/* Chunks of HL_PEAK_ROWS accumulator rows of one image each, taken
+ * grid-stride; one thread per 4 consecutive bins of a row (one 16-byte
+ * streaming load).  The neighbours are read only for bins above the
+ * threshold, which are rare, so the pass is one read of every accumulator
+ * at HBM speed. */
 __global__ void __launch_bounds__(256) hl_peaks_kernel(hl_peak_args a)
 {
     const int q4 = a.Tp >> 2;
-    const size_t total = (size_t)a.R * q4;
-    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-         e - threadIdx.x < total; e += (size_t)gridDim.x * blockDim.x) {
-        int4 v = make_int4(0, 0, 0, 0);
-        const int row = (e < total) ? (int)(e / q4) : 0;
-        const int k4 = (e < total) ? (int)(e % q4) * 4 : 0;
-        if (e < total)
-            v = __ldcs(reinterpret_cast<const int4 *>(a.acc) + e);
-        const int vv[4] = {v.x, v.y, v.z, v.w};
+    for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
+        const int2 ch = a.chunks ? a.chunks[c] : make_int2(0, c * HL_PEAK_ROWS);
+        const hl_peak_img im = a.imgs ? a.imgs[ch.x] : a.img0;
+        const int row0 = ch.y;
+        const int nrow = min(HL_PEAK_ROWS, im.R - row0);
+        const int total = nrow * q4;
+        const int4 *src = reinterpret_cast<const int4 *>(im.acc) + (size_t)row0 * q4;
+        for (int e0 = 0; e0 < total; e0 += blockDim.x) {
+            const int e = e0 + threadIdx.x;
+            int4 v = make_int4(0, 0, 0, 0);
+            const int row = row0 + ((e < total) ? e / q4 : 0);
+            const int k4 = (e < total) ? (e % q4) * 4 : 0;
+            if (e < total)
+                v = __ldcs(src + e);
+            const int vv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const int k = k4 + q;
-            bool is = false;
-            unsigned long long key = 0;
-            if (e < total && k < a.T && vv[q] > a.threshold) {
-                const int32_t *p = a.acc + (size_t)row * a.Tp + k;
-                const int W = (k > 0) ? p[-1] : 0;
-                const int E = (k + 1 < a.T) ? p[1] : 0;
-                const int N = (row > 0) ? p[-a.Tp] : 0;
-                const int S = (row + 1 < a.R) ? p[a.Tp] : 0;
-                const int x = vv[q];
-                /* okano_3_0/HoughLine.cu:195-199 */
-                if (x > W && x >= E && x > N && x >= S) {
-                    is = true;
-                    const unsigned idx = (unsigned)row * (unsigned)a.T + (unsigned)k;
-                    key = ((unsigned long long)(unsigned)x << 32) | (unsigned)(~idx);
+            for (int q = 0; q < 4; q++) {
+                const int k = k4 + q;
+                bool is = false;
+                unsigned long long key = 0;
+                if (e < total && k < a.T && vv[q] > a.threshold) {
+                    const int32_t *p = im.acc + (size_t)row * a.Tp + k;
+                    const int W = (k > 0) ? p[-1] : 0;
+                    const int E = (k + 1 < a.T) ? p[1] : 0;
+                    const int N = (row > 0) ? p[-a.Tp] : 0;
+                    const int S = (row + 1 < im.R) ? p[a.Tp] : 0;
+                    const int x = vv[q];
+                    /* okano_3_0/HoughLine.cu:195-199 */
+                    if (x > W && x >= E && x > N && x >= S) {
+                        is = true;
+                        const unsigned idx = (unsigned)row * (unsigned)a.T + (unsigned)k;
+                        key = ((unsigned long long)(unsigned)x << 32) | (unsigned)(~idx);
+                    }
                 }
+                push_key(is, key, im, a.status);
             }
-            push_key(is, key, a);
         }
     }
 }
@@ -95,10 +104,8 @@ cudaError_t hl_launch_peaks(const hl_peak_args *a, cudaStream_t s)
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const size_t total = (size_t)a->R * (a->Tp >> 2);
-    size_t blocks = (total + 255) / 256;
-    blocks = std::min(blocks, (size_t)sms * 8);
-    hl_peaks_kernel<<<(unsigned)std::max(blocks, (size_t)1), 256, 0, s>>>(*a);
+    const int blocks = std::max(1, std::min(a->nchunks, sms * 8));
+    hl_peaks_kernel<<<blocks, 256, 0, s>>>(*a);
     return cudaGetLastError();
 }
 
@@ -184,10 +191,11 @@ hl_finalize_kernel(hl_final_args a, float scale)
     extern __shared__ __align__(16) unsigned char fin_raw[];
     FinSmem &sm = *reinterpret_cast<FinSmem *>(fin_raw);
     const int tid = threadIdx.x;
-    const int ncand_raw = *a.ncand;
-    const int n = min(ncand_raw, a.cap);
+    const hl_final_img im = a.imgs ? a.imgs[blockIdx.x] : a.img0;  /* CTA = image */
+    const int ncand_raw = *im.ncand;
+    const int n = min(ncand_raw, im.cap);
     const int K = a.linesmax;
-    const int off = (a.ref_numrho - 1) / 2;
+    const int off = (im.ref_numrho - 1) / 2;
     int S = 0;          /* survivors written so far */
     int taken = 0;
     unsigned long long upper = ~0ull;
@@ -196,7 +204,7 @@ hl_finalize_kernel(hl_final_args a, float scale)
         const int m = min(FIN_CHUNK, n - taken);
         if (n <= FIN_CHUNK) {
             for (int i = tid; i < m; i += blockDim.x)
-                sm.keys[i] = a.keys[i];
+                sm.keys[i] = im.keys[i];
         } else {
             /* MSD radix select of the m-th largest key below `upper` */
             unsigned long long prefix = 0, pmask = 0;
@@ -206,7 +214,7 @@ hl_finalize_kernel(hl_final_args a, float scale)
                     sm.hist[i] = 0;
                 __syncthreads();
                 for (int i = tid; i < n; i += blockDim.x) {
-                    unsigned long long kk = a.keys[i];
+                    unsigned long long kk = im.keys[i];
                     if (kk < upper && (kk & pmask) == prefix)
                         atomicAdd(&sm.hist[(kk >> (8 * d)) & 255], 1);
                 }
@@ -233,7 +241,7 @@ hl_finalize_kernel(hl_final_args a, float scale)
                 sm.misc[2] = 0;
             __syncthreads();
             for (int i = tid; i < n; i += blockDim.x) {
-                unsigned long long kk = a.keys[i];
+                unsigned long long kk = im.keys[i];
                 if (kk < upper && kk >= prefix) {
                     int pos = atomicAdd(&sm.misc[2], 1);
                     if (pos < FIN_CHUNK)
@@ -285,7 +293,7 @@ hl_finalize_kernel(hl_final_args a, float scale)
         for (int i = tid; i < m; i += blockDim.x) {
             float ang;
             int dist, vts;
-            decode(sm.sorted[i], a.T, a.rho_min, off, scale, a.detheta, &ang,
+            decode(sm.sorted[i], a.T, im.rho_min, off, scale, a.detheta, &ang,
                    &dist, &vts);
             sm.ang[i] = ang;
             sm.dist[i] = dist;
@@ -298,8 +306,8 @@ hl_finalize_kernel(hl_final_args a, float scale)
                     qa = sm.sang[q];
                     qd = sm.sdist[q];
                 } else {
-                    qa = a.lines[q].angle;
-                    qd = a.lines[q].distance;
+                    qa = im.lines[q].angle;
+                    qd = im.lines[q].distance;
                 }
                 dead = similar(qa, qd, ang, dist, a.thresdis, a.thresang);
             }
@@ -447,7 +455,7 @@ hl_finalize_kernel(hl_final_args a, float scale)
             L.angle = sm.ang[i];
             L.distance = sm.dist[i];
             L.votes = sm.votes[i];
-            a.lines[o] = L;
+            im.lines[o] = L;
             if (o < FIN_SCACHE) {
                 sm.sang[o] = L.angle;
                 sm.sdist[o] = L.distance;
@@ -457,20 +465,25 @@ hl_finalize_kernel(hl_final_args a, float scale)
         __syncthreads();
     }
     if (tid == 0) {
-        int st = *a.status;
-        if (ncand_raw > a.cap)
-            st |= HL_ST_CAND_OVERFLOW;
-        a.hdr->count = (K > 0) ? S : K;
-        a.hdr->status = st;
-        a.hdr->ncand = ncand_raw;
-        if (a.count_out)
-            *a.count_out = (K > 0) ? S : K;
-        *a.ncand = 0;
-        *a.status = 0;
+        const int cnt = (K > 0) ? S : K;
+        if (im.count_out)
+            *im.count_out = cnt;
+        *im.ncand = 0;
+        if (ncand_raw > im.cap)
+            atomicOr(a.status, HL_ST_CAND_OVERFLOW);
+        if (a.hdr) {   /* one image: report and clear the status word */
+            int st = *a.status;
+            if (ncand_raw > im.cap)
+                st |= HL_ST_CAND_OVERFLOW;
+            a.hdr->count = cnt;
+            a.hdr->status = st;
+            a.hdr->ncand = ncand_raw;
+            *a.status = 0;
+        }
     }
 }
 
-cudaError_t hl_launch_finalize(const hl_final_args *a, cudaStream_t s)
+cudaError_t hl_launch_finalize(const hl_final_args *a, int nimg, cudaStream_t s)
 {
     const size_t smem = sizeof(FinSmem);
     cudaError_t e = cudaFuncSetAttribute(
@@ -479,7 +492,7 @@ cudaError_t hl_launch_finalize(const hl_final_args *a, cudaStream_t s)
     if (e != cudaSuccess)
         return e;
     const float scale = (float)(1.0 / (a->T + 2));   /* :882-883 */
-    hl_finalize_kernel<<<1, FIN_THREADS, smem, s>>>(*a, scale);
+    hl_finalize_kernel<<<nimg, FIN_THREADS, smem, s>>>(*a, scale);
     return cudaGetLastError();
 }
 

@@ -267,6 +267,7 @@ __device__ __forceinline__ bool tile_hits(int t, int tiles_x, int w, int h,
 }
 
 struct VoteSmem {
+    hl_vote_img im;                    /* the current item's image */
     unsigned long long full[HL_VOTE_SLOTS];
     unsigned long long empty[HL_VOTE_SLOTS];
     int item;
@@ -331,8 +332,9 @@ hl_vote_kernel(hl_vote_args a)
             const unsigned t = atomicAdd(a.work, 1u) - a.work_base;
             if (t < (unsigned)a.nitems) {
                 const int2 it = a.items[t];
-                sm.item = it.x;
+                sm.item = it.x & 0xffff;
                 sm.part = it.y;
+                sm.im = a.imgs ? a.imgs[(unsigned)it.x >> 16] : a.img0;
             } else {
                 sm.item = -1;
             }
@@ -346,8 +348,8 @@ hl_vote_kernel(hl_vote_args a)
         const int k0 = slice * HL_SLICE, k = k0 + lane;
         const float c = a.cosv[k], s = a.sinv[k];   /* table padded to Tp */
         const int w0 = win * a.win_rows;
-        const int rows = min(a.win_rows, a.R - w0);
-        const int row_base = a.rho_min + w0;       /* rho bin of local row 0 */
+        const int rows = min(a.win_rows, sm.im.R - w0);
+        const int row_base = sm.im.rho_min + w0;   /* rho bin of local row 0 */
         const unsigned lrows = (k < a.T) ? (unsigned)rows : 0u;
         const int cv = row_base >= 1 ? CV_FLOOR
                        : (row_base + rows - 1 <= -1 ? CV_CEIL : CV_EXACT);
@@ -357,7 +359,12 @@ hl_vote_kernel(hl_vote_args a)
         const float c1 = a.cosv[klast], s1 = a.sinv[klast];
         const float lo_bin = (float)row_base;
         const float hi_bin = (float)(row_base + rows - 1);
-        const bool filter = a.nwin > 1;
+        const bool filter = sm.im.nwin > 1;
+        const int ntiles = sm.im.ntiles, tiles_x = sm.im.tiles_x;
+        const int img_w = sm.im.w, img_h = sm.im.h;
+        const int *tile_off = sm.im.tile_off;
+        const float2 *pts_g = sm.im.pts;
+        int32_t *acc_g = sm.im.acc;
         const unsigned acc_l = smem_u32(s_acc) + 4u * lane;
 
         {
@@ -367,14 +374,14 @@ hl_vote_kernel(hl_vote_args a)
                 z[i] = zero;
         }
 
-        for (int tg = 0; tg < a.ntiles; tg += HL_VOTE_TG) {
-            const int tg_n = min(HL_VOTE_TG, a.ntiles - tg);
+        for (int tg = 0; tg < ntiles; tg += HL_VOTE_TG) {
+            const int tg_n = min(HL_VOTE_TG, ntiles - tg);
             /* coarse filter: one bit per tile of the group */
             for (int wd = warp; wd < HL_VOTE_TG / 32; wd += nwarps) {
                 const int tl = wd * 32 + lane;
                 bool hit = false;
                 if (tl < tg_n)
-                    hit = !filter || tile_hits(tg + tl, a.tiles_x, a.w, a.h, c0,
+                    hit = !filter || tile_hits(tg + tl, tiles_x, img_w, img_h, c0,
                                                s0, c1, s1, lo_bin, hi_bin,
                                                a.irho);
                 const unsigned m = __ballot_sync(FULL, hit);
@@ -430,9 +437,9 @@ hl_vote_kernel(hl_vote_args a)
                 const int wd = tl >> 5, b = tl & 31;
                 const unsigned below = (1u << b) - 1u;
                 if ((sm.sw[wd] >> b) & 1u)
-                    sm.run_s[sm.ws[wd] + __popc(sm.sw[wd] & below)] = a.tile_off[tg + tl];
+                    sm.run_s[sm.ws[wd] + __popc(sm.sw[wd] & below)] = tile_off[tg + tl];
                 if ((sm.ew[wd] >> b) & 1u)
-                    sm.run_e[sm.we[wd] + __popc(sm.ew[wd] & below)] = a.tile_off[tg + tl + 1];
+                    sm.run_e[sm.we[wd] + __popc(sm.ew[wd] & below)] = tile_off[tg + tl + 1];
             }
             __syncthreads();
 
@@ -512,7 +519,7 @@ hl_vote_kernel(hl_vote_args a)
                             const int ps = max(s0, rs), pe = min(e0, re);
                             if (pe > ps)
                                 bulk_g2s(&sm.raw[slot][ps - s0],
-                                         a.pts + sm.run_s[r] + (ps - rs),
+                                         pts_g + sm.run_s[r] + (ps - rs),
                                          (unsigned)(pe - ps) * 8u, &sm.full[slot]);
                             past = re > e0;
                         }
@@ -557,7 +564,7 @@ hl_vote_kernel(hl_vote_args a)
         }
 
         /* store the block: row i of the window -> acc[(w0 + i) * Tp + k0 ..] */
-        int4 *dst4 = reinterpret_cast<int4 *>(a.acc);
+        int4 *dst4 = reinterpret_cast<int4 *>(acc_g);
         const int4 *src4 = reinterpret_cast<const int4 *>(s_acc);
         const int tp4 = a.Tp >> 2;
         /* row 0 of the padding columns (thetas >= T) holds dumped votes */
@@ -580,7 +587,7 @@ hl_vote_kernel(hl_vote_args a)
             for (int i = tid; i < rows * HL_SLICE; i += nthr) {
                 const int v = s_acc[i];
                 if (v && k0 + (i & 31) < a.T)
-                    atomicAdd(&a.acc[(size_t)(w0 + (i >> 5)) * a.Tp + k0 + (i & 31)], v);
+                    atomicAdd(&acc_g[(size_t)(w0 + (i >> 5)) * a.Tp + k0 + (i & 31)], v);
             }
         }
         __syncthreads();
