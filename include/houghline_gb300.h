@@ -108,6 +108,49 @@ int hl_plain_async(hl_handle *h, const hl_image_desc *img, int linesmax,
 /* Device status word of the last asynchronous call (0 = fine); syncs. */
 int hl_last_status(hl_handle *h, int *status, void *stream);
 
+/* Batched plain HoughLine: nimg independent DEVICE images (each with its own
+ * size and ROI) through one compaction, one persistent vote launch over the
+ * (image, theta slice, rho window) work queue, one peak pass and one
+ * finalize CTA per image.  Every image gets the result hl_plain would give
+ * it (same vote rule, its own rho range, the handle's theta step, thresdis
+ * and thresang); thresholds[i] replaces the handle's vote threshold for
+ * image i when thresholds is not NULL.  The reference has no batched entry
+ * point: a caller loops over HoughLine::houghLine (okano_3_0/HoughLine.cu:
+ * 635-955), as the tiled HoughRec callers do (okano_3_0/HoughRec.cu:716-760).
+ *
+ * hl_batch: lines is a HOST array of nimg * linesmax records (image i at
+ * i * linesmax), counts a HOST array of nimg line counts.  Synchronises.
+ * hl_batch_async: the same into DEVICE arrays, no host sync (the per-image
+ * tables are staged in pinned memory owned by the handle, reused once the
+ * previous batch call on the handle has read them); in-kernel errors are
+ * reported by hl_last_status.
+ * With hl_set_batch_graph(h, 1) a call whose image sizes, linesmax, output
+ * pointers and launch shape equal the previous call's replays a captured
+ * CUDA graph of the whole pipeline instead of launching its kernels one by
+ * one (the first such call captures it). */
+int hl_batch(hl_handle *h, const hl_image_desc *imgs, int nimg,
+             const int *thresholds, int linesmax, hl_line *lines, int *counts,
+             void *stream);
+int hl_batch_async(hl_handle *h, const hl_image_desc *imgs, int nimg,
+                   const int *thresholds, int linesmax, hl_line *lines_dev,
+                   int *counts_dev, void *stream);
+int hl_set_batch_graph(hl_handle *h, int enable);
+
+/* Autotuner (no reference counterpart): times hl_batch_async on the given
+ * images for every candidate vote-kernel shape (rho-window rows x threads
+ * per CTA), keeps the fastest with hl_set_vote_shape and reports it.
+ * tried[] (optional, up to max_tried entries) receives every candidate and
+ * its mean milliseconds per batch; *ntried their number. */
+typedef struct hl_tune_entry {
+    int window_rows;
+    int threads;
+    float ms;
+} hl_tune_entry;
+int hl_autotune(hl_handle *h, const hl_image_desc *imgs, int nimg,
+                const int *thresholds, int linesmax, hl_tune_entry *best,
+                hl_tune_entry *tried, int max_tried, int *ntried,
+                void *stream);
+
 /* HoughLine::houghLineCor / houghLine(NULL, guidingset, ...),
  * okano_3_0/HoughLine.cu:352-632: votes over an interleaved (x, y) int list
  * in DEVICE memory.  The accumulator covers the set's bounding box from the

@@ -60,6 +60,10 @@ class hl_scene_params(C.Structure):
                 ("seed", C.c_uint64)]
 
 
+class hl_tune_entry(C.Structure):
+    _fields_ = [("window_rows", C.c_int), ("threads", C.c_int), ("ms", C.c_float)]
+
+
 H = C.c_void_p
 P = C.c_void_p
 I = C.c_int
@@ -76,6 +80,11 @@ SIGNATURES = {
     "hl_plain": (I, [H, C.POINTER(hl_image_desc), PI, P, P]),
     "hl_plain_async": (I, [H, C.POINTER(hl_image_desc), I, P, P, P]),
     "hl_last_status": (I, [H, PI, P]),
+    "hl_batch": (I, [H, C.POINTER(hl_image_desc), I, PI, I, P, PI, P]),
+    "hl_batch_async": (I, [H, C.POINTER(hl_image_desc), I, PI, I, P, P, P]),
+    "hl_set_batch_graph": (I, [H, I]),
+    "hl_autotune": (I, [H, C.POINTER(hl_image_desc), I, PI, I, C.POINTER(hl_tune_entry),
+                        C.POINTER(hl_tune_entry), I, PI, P]),
     "hl_plain_points": (I, [H, P, I, PI, P, P]),
     "hl_compact": (I, [H, C.POINTER(hl_image_desc), P, P, P, P]),
     "hl_compact_noalloc": (I, [C.POINTER(hl_image_desc), P, P, P, P]),

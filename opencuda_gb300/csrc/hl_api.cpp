@@ -25,6 +25,8 @@
 #error "M_PI required: numtheta = (int)(M_PI / detheta)"
 #endif
 
+struct hl_batch_ws;   /* batched-path workspace (hl_batch*) */
+
 struct hl_handle {
     hl_params p;
     int T, Tp;
@@ -62,6 +64,12 @@ struct hl_handle {
     int order_n, order_split;
     double order_derho;
     unsigned work_base;
+
+    /* batched path: workspace, CUDA-graph switch; whether the last
+     * asynchronous call was a batch (hl_last_status reads its status) */
+    hl_batch_ws *bw;
+    int batch_graph;
+    int last_batch;
 
     /* per-stage CUDA-event timing (hl_profile) */
     int prof;
@@ -195,10 +203,13 @@ extern "C" int hl_create(hl_handle **out, const hl_params *params)
     return HL_NO_ERROR;
 }
 
+static void batch_free(hl_handle *h);
+
 extern "C" int hl_destroy(hl_handle *h)
 {
     if (!h)
         return HL_NULL_POINTER;
+    batch_free(h);
     void *ptrs[] = {h->d_cos, h->d_sin, h->d_pts, h->d_tile_state,
                     h->d_tile_off, h->d_acc, h->d_keys, h->d_aux,
                     h->d_result, h->d_counters, h->order_dev};
@@ -600,11 +611,12 @@ static int run_c(hl_handle *h, const hl_geom &g, int linesmax,
     pa.img0.ncand = h->d_counters + 0;
     pa.img0.R = g.numrho;
     pa.img0.cap = key_cap(h);
+    pa.img0.threshold = h->p.threshold;
+    pa.img0.pad = 0;
     pa.chunks = nullptr;
     pa.nchunks = (g.numrho + HL_PEAK_ROWS - 1) / HL_PEAK_ROWS;
     pa.T = h->T;
     pa.Tp = h->Tp;
-    pa.threshold = h->p.threshold;
     pa.status = h->d_counters + 1;
     CK(hl_launch_peaks(&pa, s));
     (*launches)++;
@@ -684,6 +696,7 @@ static int plain_launch(hl_handle *h, const hl_image_desc *img, int linesmax,
     if ((rc = ensure_acc(h, g.numrho, linesmax)) != HL_NO_ERROR)
         return rc;
     int launches = 0;
+    h->last_batch = 0;
     if ((rc = run_ab(h, roi, g, s, &launches)) != HL_NO_ERROR)
         return rc;
     rc = run_c(h, g, linesmax, lines_dev, count_dev, s, &launches);
@@ -717,12 +730,16 @@ extern "C" int hl_plain_async(hl_handle *h, const hl_image_desc *img,
                         reinterpret_cast<cudaStream_t>(stream));
 }
 
+static int batch_last_status(hl_handle *h, int *status, cudaStream_t s);
+
 extern "C" int hl_last_status(hl_handle *h, int *status, void *stream)
 {
     if (!h || !status)
         return HL_NULL_POINTER;
     hl_result_hdr hdr;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (h->last_batch)
+        return batch_last_status(h, status, s);
     if (!h->d_result) {
         *status = 0;
         return HL_NO_ERROR;
@@ -1045,5 +1062,663 @@ extern "C" int hl_real_line(hl_handle *h, const hl_image_desc *img, int x1,
     if (pointnum)
         *pointnum = n;
     h->last_launches = 1;
+    return HL_NO_ERROR;
+}
+
+/* ==================================================================== */
+/* Batched path                                                          */
+/* ==================================================================== */
+
+/* Counters of a batch call, cleared at its start: [0] compaction ticket,
+ * [1] vote work counter, [2] status word, [3] total points. */
+#define BW_NCNT 16
+
+struct hl_batch_ws {
+    float2 *d_pts;
+    size_t cap_pts;
+    unsigned long long *d_state;   /* look-back state per 4-tile group */
+    size_t cap_state;
+    int *d_tile_off;
+    size_t cap_tile_off;
+    int32_t *d_acc;
+    size_t cap_acc;
+    unsigned long long *d_keys;
+    size_t cap_keys;
+    int *d_ncand;                  /* per image, zero between calls */
+    size_t cap_ncand;
+    int *d_cnt;
+    unsigned char *d_tab;          /* per-image tables of one call */
+    size_t cap_tab;
+    unsigned char *h_tab;          /* their pinned staging copy */
+    size_t cap_htab;
+    hl_line *d_lines;              /* hl_batch's device results */
+    size_t cap_lines;
+    int *d_counts;
+    size_t cap_counts;
+    unsigned char *h_res;          /* pinned copy of results + status */
+    size_t cap_hres;
+    cudaEvent_t tab_read;          /* the previous call's table upload */
+    int tab_event;
+
+    /* the plan of the last call (reused while the geometry is the same) */
+    std::vector<int> key;
+    size_t tab_bytes;
+    size_t off_cimg, off_gimg, off_vimg, off_items, off_pimg, off_chunks,
+        off_fimg;
+    int ngroups, ntiles, nitems, nchunks, grid, threads, win_rows;
+    size_t npts_cap, acc_ints, nkeys;
+    std::vector<size_t> acc_off, key_off;
+    std::vector<int> key_cap_i, tile_base, group_base, nwin, rho_min, R,
+        ref_numrho;
+    std::vector<int> split_img;    /* images whose accumulator is added to */
+    std::vector<int2> items;
+    std::vector<int2> chunks;
+    std::vector<int> group_img;
+
+    /* captured pipeline (captured on a private stream: the caller's may be
+     * the legacy default stream, which cannot be captured) */
+    cudaStream_t cap_stream;
+    cudaGraphExec_t gexec;
+    std::vector<long long> gkey;
+};
+
+static void batch_free(hl_handle *h)
+{
+    hl_batch_ws *b = h->bw;
+    if (!b)
+        return;
+    void *dp[] = {b->d_pts, b->d_state, b->d_tile_off, b->d_acc, b->d_keys,
+                  b->d_ncand, b->d_cnt, b->d_tab, b->d_lines, b->d_counts};
+    for (void *q : dp)
+        if (q)
+            cudaFree(q);
+    if (b->h_tab)
+        cudaFreeHost(b->h_tab);
+    if (b->h_res)
+        cudaFreeHost(b->h_res);
+    if (b->tab_event)
+        cudaEventDestroy(b->tab_read);
+    if (b->gexec)
+        cudaGraphExecDestroy(b->gexec);
+    if (b->cap_stream)
+        cudaStreamDestroy(b->cap_stream);
+    delete b;
+    h->bw = nullptr;
+}
+
+static int grow_host(unsigned char **ptr, size_t *cap, size_t need)
+{
+    if (*cap >= need && *ptr)
+        return HL_NO_ERROR;
+    size_t nb = std::max(need, (size_t)4096);
+    nb += nb / 4;
+    if (*ptr)
+        cudaFreeHost(*ptr);
+    *ptr = nullptr;
+    *cap = 0;
+    CK(cudaMallocHost(ptr, nb));
+    *cap = nb;
+    return HL_NO_ERROR;
+}
+
+static size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+/* Per-image rho-window weights of the vote items on an 8 x 8 grid of cell
+ * centres (the image's share of points in each (slice, window) block when
+ * edges are spread evenly), in units of pixels. */
+static void batch_block_weights(const hl_handle *h, int w, int hh, int rho_min,
+                                int rows, int nwin, std::vector<double> &wt)
+{
+    const int slices = h->Tp / HL_SLICE;
+    wt.assign((size_t)slices * nwin, 0.0);
+    const int G = 8;
+    const double cell = (double)w * hh / (G * G);
+    for (int sl = 0; sl < slices; sl++) {
+        const int k0 = sl * HL_SLICE;
+        const int k1 = std::min(k0 + HL_SLICE, h->T) - 1;
+        if (k0 >= h->T)
+            continue;
+        const double th = 0.5 * (k0 + k1) * h->p.detheta;
+        const double c = cos(th), sn = sin(th);
+        for (int gy = 0; gy < G; gy++) {
+            const double y = (gy + 0.5) * hh / G;
+            for (int gx = 0; gx < G; gx++) {
+                const double x = (gx + 0.5) * w / G;
+                const int row = (int)floor((x * c + y * sn) / h->p.derho) - rho_min;
+                const int wn = std::min(std::max(row / rows, 0), nwin - 1);
+                wt[(size_t)sl + (size_t)slices * wn] += cell * (k1 - k0 + 1);
+            }
+        }
+    }
+}
+
+/* Plan a batch: sizes, offsets, work items, chunks; fills the pinned tables
+ * (image pointers and thresholds included).  The geometry part is reused
+ * when the sizes and the launch shape equal the previous call's. */
+static int batch_plan(hl_handle *h, const hl_image_desc *imgs, int nimg,
+                      const int *thr, int K, hl_line *lines_dev,
+                      int *counts_dev, const hl_roi *rois)
+{
+    hl_batch_ws *b = h->bw;
+    const int slices = h->Tp / HL_SLICE;
+    int maxR = 1;
+    std::vector<hl_geom> gs((size_t)nimg);
+    for (int i = 0; i < nimg; i++) {
+        int rc = hl_geometry(h, rois[i].w, rois[i].h, &gs[i]);
+        if (rc != HL_NO_ERROR)
+            return rc;
+        maxR = std::max(maxR, gs[i].numrho);
+    }
+    /* launch shape: the override (autotuner) or the largest window that
+     * fits, 1024 threads */
+    const int maxr = hl_vote_max_rows();
+    int rows = h->win_rows_override > 0 ? std::min(h->win_rows_override, maxr)
+                                        : std::min(maxR, maxr);
+    rows = std::max(8, (rows + 7) / 8 * 8);
+    rows = std::min(rows, maxr);
+    const int threads = h->threads_override > 0 ? h->threads_override : 1024;
+    const size_t smem = hl_vote_smem_bytes(rows);
+    const int per_sm = std::max(1, std::min(2048 / threads,
+                                            (int)((228u * 1024u) / (smem + 1024))));
+    const int ctas = std::max(h->sms, 1) * per_sm;
+
+    std::vector<int> key;
+    key.reserve(2 * (size_t)nimg + 8);
+    key.push_back(nimg);
+    key.push_back(rows);
+    key.push_back(threads);
+    key.push_back(h->T);
+    for (int i = 0; i < nimg; i++) {
+        key.push_back(rois[i].w);
+        key.push_back(rois[i].h);
+    }
+    if (key != b->key) {
+        b->key = key;
+        b->win_rows = rows;
+        b->threads = threads;
+        b->acc_off.assign(nimg, 0);
+        b->key_off.assign(nimg, 0);
+        b->key_cap_i.assign(nimg, 0);
+        b->tile_base.assign(nimg, 0);
+        b->group_base.assign(nimg, 0);
+        b->nwin.assign(nimg, 0);
+        b->rho_min.assign(nimg, 0);
+        b->R.assign(nimg, 0);
+        b->ref_numrho.assign(nimg, 0);
+        b->group_img.clear();
+        b->chunks.clear();
+        size_t acc = 0, keys = 0, pts = 16;
+        int tiles = 0, groups = 0;
+        std::vector<double> allw;
+        std::vector<int2> blocks;
+        std::vector<double> wt;
+        double total = 0.0;
+        for (int i = 0; i < nimg; i++) {
+            const hl_geom &g = gs[i];
+            const int nt = g.tiles_x * g.tiles_y;
+            const int ng = (nt + HL_COMPACT_GROUP - 1) / HL_COMPACT_GROUP;
+            b->tile_base[i] = tiles;
+            b->group_base[i] = groups;
+            for (int q = 0; q < ng; q++)
+                b->group_img.push_back(i);
+            tiles += nt;
+            groups += ng;
+            pts += (size_t)rois[i].w * rois[i].h + (size_t)nt;
+            b->acc_off[i] = acc;
+            acc += (size_t)g.numrho * h->Tp;
+            /* peak-key capacity: the bound of ensure_acc, at most 2^17 */
+            const size_t kc = std::min((size_t)g.numrho * ((h->T + 1) / 2) + 32,
+                                       (size_t)1 << 17);
+            b->key_off[i] = keys;
+            b->key_cap_i[i] = (int)kc;
+            keys += kc;
+            b->rho_min[i] = g.rho_min;
+            b->R[i] = g.numrho;
+            b->ref_numrho[i] = g.ref_numrho;
+            b->nwin[i] = (g.numrho + rows - 1) / rows;
+            for (int r0 = 0; r0 < g.numrho; r0 += HL_PEAK_ROWS)
+                b->chunks.push_back(make_int2(i, r0));
+            if ((size_t)slices * b->nwin[i] > 0xffff)
+                return HL_OP_OVERFLOW;   /* ... and the block in 16 bits */
+            batch_block_weights(h, rois[i].w, rois[i].h, g.rho_min, rows,
+                                b->nwin[i], wt);
+            for (size_t q = 0; q < wt.size(); q++) {
+                blocks.push_back(make_int2(i, (int)q));
+                allw.push_back(wt[q]);
+                total += wt[q];
+            }
+        }
+        if (nimg > 0xffff)
+            return HL_OP_OVERFLOW;   /* the item packs the image in 16 bits */
+        /* items: heaviest first; a block heavier than a third of one CTA's
+         * share is split (its image's accumulator is then cleared first) */
+        const double cap = total / (3.0 * std::max(ctas, 1));
+        struct part_t { double wt; int img, blk, part, nparts; };
+        std::vector<part_t> parts;
+        std::vector<char> split((size_t)nimg, 0);
+        for (size_t q = 0; q < blocks.size(); q++) {
+            int np = 1;
+            if (cap > 0.0 && allw[q] > cap)
+                np = std::min(16, (int)ceil(allw[q] / cap));
+            if (np > 1)
+                split[blocks[q].x] = 1;
+            for (int pp = 0; pp < np; pp++)
+                parts.push_back({allw[q] / np, blocks[q].x, blocks[q].y, pp, np});
+        }
+        std::stable_sort(parts.begin(), parts.end(),
+                         [](const part_t &a, const part_t &c) { return a.wt > c.wt; });
+        b->items.resize(parts.size());
+        for (size_t q = 0; q < parts.size(); q++)
+            b->items[q] = make_int2(parts[q].blk | (parts[q].img << 16),
+                                    parts[q].part | (parts[q].nparts << 16));
+        b->split_img.clear();
+        for (int i = 0; i < nimg; i++)
+            if (split[i])
+                b->split_img.push_back(i);
+        b->ngroups = groups;
+        b->ntiles = tiles;
+        b->nitems = (int)b->items.size();
+        b->nchunks = (int)b->chunks.size();
+        b->grid = std::max(1, std::min(b->nitems, ctas));
+        b->npts_cap = pts;
+        b->acc_ints = acc;
+        b->nkeys = keys;
+        /* table layout */
+        size_t o = 0;
+        b->off_cimg = o;   o = align16(o + sizeof(hl_compact_img) * nimg);
+        b->off_gimg = o;   o = align16(o + sizeof(int) * (size_t)groups);
+        b->off_vimg = o;   o = align16(o + sizeof(hl_vote_img) * nimg);
+        b->off_items = o;  o = align16(o + sizeof(int2) * b->items.size());
+        b->off_pimg = o;   o = align16(o + sizeof(hl_peak_img) * nimg);
+        b->off_chunks = o; o = align16(o + sizeof(int2) * b->chunks.size());
+        b->off_fimg = o;   o = align16(o + sizeof(hl_final_img) * nimg);
+        b->tab_bytes = o;
+    }
+
+    /* device buffers */
+    int rc;
+    if ((rc = grow((void **)&b->d_pts, &b->cap_pts, sizeof(float2) * b->npts_cap)) != HL_NO_ERROR ||
+        (rc = grow((void **)&b->d_state, &b->cap_state,
+                   sizeof(unsigned long long) * ((size_t)b->ngroups + 1))) != HL_NO_ERROR ||
+        (rc = grow((void **)&b->d_tile_off, &b->cap_tile_off,
+                   sizeof(int) * ((size_t)b->ntiles + 1))) != HL_NO_ERROR ||
+        (rc = grow((void **)&b->d_acc, &b->cap_acc, sizeof(int32_t) * b->acc_ints)) != HL_NO_ERROR ||
+        (rc = grow((void **)&b->d_keys, &b->cap_keys,
+                   sizeof(unsigned long long) * b->nkeys)) != HL_NO_ERROR ||
+        (rc = grow((void **)&b->d_tab, &b->cap_tab, b->tab_bytes)) != HL_NO_ERROR)
+        return rc;
+    if (b->cap_ncand < sizeof(int) * (size_t)nimg || !b->d_ncand) {
+        if ((rc = grow((void **)&b->d_ncand, &b->cap_ncand, sizeof(int) * (size_t)nimg)) !=
+            HL_NO_ERROR)
+            return rc;
+        CK(cudaMemset(b->d_ncand, 0, b->cap_ncand));
+    }
+    if (!b->d_cnt)
+        CK(cudaMalloc(&b->d_cnt, BW_NCNT * sizeof(int)));
+    /* the previous call's upload must be done before the staging is reused */
+    if (b->tab_event)
+        CK(cudaEventSynchronize(b->tab_read));
+    if ((rc = grow_host(&b->h_tab, &b->cap_htab, b->tab_bytes)) != HL_NO_ERROR)
+        return rc;
+
+    /* tables */
+    unsigned char *t = b->h_tab;
+    hl_compact_img *ci = reinterpret_cast<hl_compact_img *>(t + b->off_cimg);
+    hl_vote_img *vi = reinterpret_cast<hl_vote_img *>(t + b->off_vimg);
+    hl_peak_img *pi = reinterpret_cast<hl_peak_img *>(t + b->off_pimg);
+    hl_final_img *fi = reinterpret_cast<hl_final_img *>(t + b->off_fimg);
+    for (int i = 0; i < nimg; i++) {
+        const hl_geom &g = gs[i];
+        const int nt = g.tiles_x * g.tiles_y;
+        ci[i].roi = rois[i];
+        ci[i].tiles_x = g.tiles_x;
+        ci[i].ntiles = nt;
+        ci[i].tile_base = b->tile_base[i];
+        ci[i].group_base = b->group_base[i];
+        ci[i].ngroups = (nt + HL_COMPACT_GROUP - 1) / HL_COMPACT_GROUP;
+        ci[i].pad = 0;
+        vi[i].pts = b->d_pts;
+        vi[i].tile_off = b->d_tile_off + b->tile_base[i];
+        vi[i].ntiles = nt;
+        vi[i].tiles_x = g.tiles_x;
+        vi[i].w = rois[i].w;
+        vi[i].h = rois[i].h;
+        vi[i].rho_min = g.rho_min;
+        vi[i].R = g.numrho;
+        vi[i].nwin = b->nwin[i];
+        vi[i].pad = 0;
+        vi[i].acc = b->d_acc + b->acc_off[i];
+        pi[i].acc = b->d_acc + b->acc_off[i];
+        pi[i].keys = b->d_keys + b->key_off[i];
+        pi[i].ncand = b->d_ncand + i;
+        pi[i].R = g.numrho;
+        pi[i].cap = b->key_cap_i[i];
+        pi[i].threshold = thr ? thr[i] : h->p.threshold;
+        pi[i].pad = 0;
+        fi[i].keys = b->d_keys + b->key_off[i];
+        fi[i].ncand = b->d_ncand + i;
+        fi[i].cap = b->key_cap_i[i];
+        fi[i].rho_min = g.rho_min;
+        fi[i].ref_numrho = g.ref_numrho;
+        fi[i].pad = 0;
+        fi[i].lines = lines_dev + (size_t)i * (size_t)std::max(K, 0);
+        fi[i].count_out = counts_dev + i;
+    }
+    memcpy(t + b->off_gimg, b->group_img.data(), sizeof(int) * b->group_img.size());
+    memcpy(t + b->off_items, b->items.data(), sizeof(int2) * b->items.size());
+    memcpy(t + b->off_chunks, b->chunks.data(), sizeof(int2) * b->chunks.size());
+    return HL_NO_ERROR;
+}
+
+/* The stream work of one planned batch call. */
+static int batch_enqueue(hl_handle *h, int nimg, int K, cudaStream_t s)
+{
+    hl_batch_ws *b = h->bw;
+    unsigned char *dt = b->d_tab;
+    CK(cudaMemsetAsync(b->d_cnt, 0, BW_NCNT * sizeof(int), s));
+    CK(cudaMemsetAsync(b->d_state, 0,
+                       sizeof(unsigned long long) * ((size_t)b->ngroups + 1), s));
+    CK(cudaMemcpyAsync(dt, b->h_tab, b->tab_bytes, cudaMemcpyHostToDevice, s));
+    for (int i : b->split_img)
+        CK(cudaMemsetAsync(b->d_acc + b->acc_off[i], 0,
+                           sizeof(int32_t) * (size_t)b->R[i] * h->Tp, s));
+
+    hl_compact_args ca;
+    memset(&ca, 0, sizeof(ca));
+    ca.imgs = reinterpret_cast<const hl_compact_img *>(dt + b->off_cimg);
+    ca.group_img = reinterpret_cast<const int *>(dt + b->off_gimg);
+    ca.nimg = nimg;
+    ca.ngroups = b->ngroups;
+    ca.tile_state = b->d_state;
+    ca.ticket = reinterpret_cast<unsigned *>(b->d_cnt + 0);
+    ca.ticket_base = 0;
+    ca.epoch = 1;
+    ca.pts = nullptr;
+    ca.pts_f2 = b->d_pts;
+    ca.tile_off = b->d_tile_off;
+    ca.count = b->d_cnt + 3;
+    ca.status = b->d_cnt + 2;
+    CK(hl_launch_compact(&ca, s));
+    prof_mark(h, 1, s);
+
+    hl_vote_args va;
+    memset(&va, 0, sizeof(va));
+    va.imgs = reinterpret_cast<const hl_vote_img *>(dt + b->off_vimg);
+    va.cosv = h->d_cos;
+    va.sinv = h->d_sin;
+    va.T = h->T;
+    va.Tp = h->Tp;
+    va.win_rows = b->win_rows;
+    va.irho = (float)(1.0 / h->p.derho);   /* okano_3_0/HoughLine.cu:107 */
+    va.status = b->d_cnt + 2;
+    va.items = reinterpret_cast<const int2 *>(dt + b->off_items);
+    va.nitems = b->nitems;
+    va.work = reinterpret_cast<unsigned *>(b->d_cnt + 1);
+    va.work_base = 0;
+    CK(hl_launch_vote(&va, b->threads, b->grid, s));
+    prof_mark(h, 2, s);
+
+    hl_peak_args pa;
+    memset(&pa, 0, sizeof(pa));
+    pa.imgs = reinterpret_cast<const hl_peak_img *>(dt + b->off_pimg);
+    pa.chunks = reinterpret_cast<const int2 *>(dt + b->off_chunks);
+    pa.nchunks = b->nchunks;
+    pa.T = h->T;
+    pa.Tp = h->Tp;
+    pa.status = b->d_cnt + 2;
+    CK(hl_launch_peaks(&pa, s));
+    prof_mark(h, 3, s);
+
+    hl_final_args fa;
+    memset(&fa, 0, sizeof(fa));
+    fa.imgs = reinterpret_cast<const hl_final_img *>(dt + b->off_fimg);
+    fa.T = h->T;
+    fa.detheta = h->p.detheta;
+    fa.thresdis = h->p.thresdis;
+    fa.thresang = h->p.thresang;
+    fa.linesmax = K;
+    fa.hdr = nullptr;
+    fa.status = b->d_cnt + 2;
+    CK(hl_launch_finalize(&fa, nimg, s));
+    prof_mark(h, 4, s);
+    return HL_NO_ERROR;
+}
+
+static int batch_run(hl_handle *h, const hl_image_desc *imgs, int nimg,
+                     const int *thr, int K, hl_line *lines_dev,
+                     int *counts_dev, cudaStream_t s)
+{
+    if (nimg <= 0)
+        return HL_INVALID_DATA;
+    if (!h->bw) {
+        h->bw = new (std::nothrow) hl_batch_ws();
+        if (!h->bw)
+            return HL_OUT_OF_MEM;
+    }
+    hl_batch_ws *b = h->bw;
+    std::vector<hl_roi> rois((size_t)nimg);
+    for (int i = 0; i < nimg; i++) {
+        int rc = roi_of(&imgs[i], &rois[i]);
+        if (rc != HL_NO_ERROR)
+            return rc;
+    }
+    int rc = batch_plan(h, imgs, nimg, thr, K, lines_dev, counts_dev, rois.data());
+    if (rc != HL_NO_ERROR)
+        return rc;
+    h->last_batch = 1;
+    h->last_launches = 4;
+    if (!b->tab_event) {
+        CK(cudaEventCreateWithFlags(&b->tab_read, cudaEventDisableTiming));
+        b->tab_event = 1;
+    }
+    prof_mark(h, 0, s);
+    if (!h->batch_graph || h->prof) {
+        rc = batch_enqueue(h, nimg, K, s);
+    } else {
+        /* graph key: the plan key plus what the captured nodes hold */
+        std::vector<long long> gk(b->key.begin(), b->key.end());
+        gk.push_back((long long)(uintptr_t)lines_dev);
+        gk.push_back((long long)(uintptr_t)counts_dev);
+        gk.push_back(K);
+        gk.push_back((long long)(uintptr_t)b->d_acc);
+        gk.push_back((long long)(uintptr_t)b->d_pts);
+        gk.push_back((long long)(uintptr_t)b->d_tab);
+        gk.push_back((long long)(uintptr_t)b->h_tab);
+        gk.push_back((long long)(uintptr_t)b->d_keys);
+        if (!b->gexec || gk != b->gkey) {
+            if (b->gexec) {
+                cudaGraphExecDestroy(b->gexec);
+                b->gexec = nullptr;
+            }
+            if (!b->cap_stream)
+                CK(cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking));
+            cudaGraph_t graph = nullptr;
+            CK(cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal));
+            rc = batch_enqueue(h, nimg, K, b->cap_stream);
+            cudaError_t e = cudaStreamEndCapture(b->cap_stream, &graph);
+            if (rc != HL_NO_ERROR) {
+                if (graph)
+                    cudaGraphDestroy(graph);
+                return rc;
+            }
+            if (e != cudaSuccess)
+                return map_err(e);
+            e = cudaGraphInstantiate(&b->gexec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) {
+                b->gexec = nullptr;
+                return map_err(e);
+            }
+            b->gkey = gk;
+        }
+        CK(cudaGraphLaunch(b->gexec, s));
+        h->last_launches = 4;
+    }
+    if (rc == HL_NO_ERROR)
+        CK(cudaEventRecord(b->tab_read, s));
+    return rc;
+}
+
+static int batch_last_status(hl_handle *h, int *status, cudaStream_t s)
+{
+    hl_batch_ws *b = h->bw;
+    if (!b || !b->d_cnt) {
+        *status = 0;
+        return HL_NO_ERROR;
+    }
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, b->d_cnt + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    *status = st;
+    return HL_NO_ERROR;
+}
+
+extern "C" int hl_set_batch_graph(hl_handle *h, int enable)
+{
+    if (!h)
+        return HL_NULL_POINTER;
+    h->batch_graph = enable ? 1 : 0;
+    return HL_NO_ERROR;
+}
+
+extern "C" int hl_batch_async(hl_handle *h, const hl_image_desc *imgs, int nimg,
+                              const int *thresholds, int linesmax,
+                              hl_line *lines_dev, int *counts_dev, void *stream)
+{
+    if (!h || !imgs || !counts_dev)
+        return HL_NULL_POINTER;
+    if (linesmax > 0 && !lines_dev)
+        return HL_NULL_POINTER;
+    return batch_run(h, imgs, nimg, thresholds, linesmax, lines_dev, counts_dev,
+                     reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int hl_batch(hl_handle *h, const hl_image_desc *imgs, int nimg,
+                        const int *thresholds, int linesmax, hl_line *lines,
+                        int *counts, void *stream)
+{
+    if (!h || !imgs || !counts)
+        return HL_NULL_POINTER;
+    if (linesmax > 0 && !lines)
+        return HL_NULL_POINTER;
+    if (nimg <= 0)
+        return HL_INVALID_DATA;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (!h->bw) {
+        h->bw = new (std::nothrow) hl_batch_ws();
+        if (!h->bw)
+            return HL_OUT_OF_MEM;
+    }
+    hl_batch_ws *b = h->bw;
+    const size_t K = (size_t)std::max(linesmax, 0);
+    int rc;
+    if ((rc = grow((void **)&b->d_lines, &b->cap_lines,
+                   sizeof(hl_line) * std::max(K * nimg, (size_t)1))) != HL_NO_ERROR ||
+        (rc = grow((void **)&b->d_counts, &b->cap_counts, sizeof(int) * nimg)) != HL_NO_ERROR)
+        return rc;
+    rc = batch_run(h, imgs, nimg, thresholds, linesmax, b->d_lines, b->d_counts, s);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    const size_t lbytes = sizeof(hl_line) * K * nimg;
+    if ((rc = grow_host(&b->h_res, &b->cap_hres, lbytes + sizeof(int) * (nimg + 1))) !=
+        HL_NO_ERROR)
+        return rc;
+    int *h_counts = reinterpret_cast<int *>(b->h_res + lbytes);
+    CK(cudaMemcpyAsync(h_counts, b->d_counts, sizeof(int) * nimg,
+                       cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h_counts + nimg, b->d_cnt + 2, sizeof(int),
+                       cudaMemcpyDeviceToHost, s));
+    if (lbytes)
+        CK(cudaMemcpyAsync(b->h_res, b->d_lines, lbytes, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (h_counts[nimg] != 0)
+        return HL_CUDA_ERROR;
+    for (int i = 0; i < nimg; i++) {
+        const int c = std::max(0, std::min(h_counts[i], linesmax));
+        counts[i] = c;
+        if (c > 0)
+            memcpy(lines + (size_t)i * K, b->h_res + sizeof(hl_line) * K * i,
+                   sizeof(hl_line) * c);
+    }
+    return HL_NO_ERROR;
+}
+
+extern "C" int hl_autotune(hl_handle *h, const hl_image_desc *imgs, int nimg,
+                           const int *thresholds, int linesmax,
+                           hl_tune_entry *best, hl_tune_entry *tried,
+                           int max_tried, int *ntried, void *stream)
+{
+    if (!h || !imgs || !best)
+        return HL_NULL_POINTER;
+    if (nimg <= 0)
+        return HL_INVALID_DATA;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const int maxr = hl_vote_max_rows();
+    const int row_cand[] = {256, 512, 768, 1024, maxr};
+    const int thr_cand[] = {512, 1024};
+    const int K = std::max(linesmax, 1);
+    hl_line *d_lines = nullptr;
+    int *d_counts = nullptr;
+    CK(cudaMalloc(&d_lines, sizeof(hl_line) * (size_t)K * nimg));
+    if (cudaMalloc(&d_counts, sizeof(int) * nimg) != cudaSuccess) {
+        cudaFree(d_lines);
+        return HL_OUT_OF_MEM;
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int saved_rows = h->win_rows_override, saved_thr = h->threads_override;
+    const int saved_graph = h->batch_graph;
+    h->batch_graph = 0;
+    hl_tune_entry bst = {0, 0, 3.0e38f};
+    int n = 0, rc = HL_NO_ERROR;
+    for (int ti = 0; ti < 2 && rc == HL_NO_ERROR; ti++) {
+        for (int ri = 0; ri < 5 && rc == HL_NO_ERROR; ri++) {
+            const int rows = std::min(row_cand[ri], maxr);
+            if (ri < 4 && row_cand[ri] >= maxr)
+                continue;   /* the last candidate covers it */
+            h->win_rows_override = rows;
+            h->threads_override = thr_cand[ti];
+            /* warm-up (plans, allocates), then three timed calls */
+            rc = batch_run(h, imgs, nimg, thresholds, K, d_lines, d_counts, s);
+            if (rc != HL_NO_ERROR)
+                break;
+            cudaEventRecord(e0, s);
+            for (int r = 0; r < 3 && rc == HL_NO_ERROR; r++)
+                rc = batch_run(h, imgs, nimg, thresholds, K, d_lines, d_counts, s);
+            cudaEventRecord(e1, s);
+            if (cudaEventSynchronize(e1) != cudaSuccess) {
+                rc = HL_CUDA_ERROR;
+                break;
+            }
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            ms /= 3.0f;
+            hl_tune_entry te = {rows, thr_cand[ti], ms};
+            if (tried && n < max_tried)
+                tried[n] = te;
+            n++;
+            if (ms < bst.ms)
+                bst = te;
+        }
+    }
+    int st = 0;
+    if (rc == HL_NO_ERROR && batch_last_status(h, &st, s) == HL_NO_ERROR && st != 0)
+        rc = HL_CUDA_ERROR;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(d_lines);
+    cudaFree(d_counts);
+    h->batch_graph = saved_graph;
+    if (rc != HL_NO_ERROR || bst.threads == 0) {
+        h->win_rows_override = saved_rows;
+        h->threads_override = saved_thr;
+        return rc != HL_NO_ERROR ? rc : HL_CUDA_ERROR;
+    }
+    h->win_rows_override = bst.window_rows;
+    h->threads_override = bst.threads;
+    *best = bst;
+    if (ntried)
+        *ntried = n;
     return HL_NO_ERROR;
 }

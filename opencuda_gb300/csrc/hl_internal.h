@@ -122,6 +122,8 @@ typedef struct hl_peak_img {
     unsigned long long *keys; /* votes << 32 | ~tight_index */
     int *ncand;
     int R, cap;
+    int threshold;            /* votes must exceed it */
+    int pad;
 } hl_peak_img;
 
 /* rows of an accumulator one peak-pass chunk covers */
@@ -135,7 +137,6 @@ typedef struct hl_peak_args {
                                  img0 */
     int nchunks;
     int T, Tp;
-    int threshold;
     int *status;
 } hl_peak_args;
 

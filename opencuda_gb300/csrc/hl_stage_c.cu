@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(256) hl_peaks_kernel(hl_peak_args a)
                 const int k = k4 + q;
                 bool is = false;
                 unsigned long long key = 0;
-                if (e < total && k < a.T && vv[q] > a.threshold) {
+                if (e < total && k < a.T && vv[q] > im.threshold) {
                     const int32_t *p = im.acc + (size_t)row * a.Tp + k;
                     const int W = (k > 0) ? p[-1] : 0;
                     const int E = (k + 1 < a.T) ? p[1] : 0;

@@ -207,6 +207,49 @@ class HoughLine:
                                       self._stream(stream)), "hl_compact")
         return pts, offs, cnt
 
+    def houghLineBatch(self, images, linesmax: int = 16, thresholds=None,
+                       stream=None):
+        """Batched plain HoughLine over a list of device Images (hl_batch):
+        returns (rc, [[LineParam, ...] per image])."""
+        n = len(images)
+        descs = (_lib.hl_image_desc * max(n, 1))(*[im.desc() for im in images])
+        K = max(linesmax, 0)
+        out = (_lib.hl_line * max(K * n, 1))()
+        counts = (C.c_int * max(n, 1))()
+        thr = None
+        if thresholds is not None:
+            thr = (C.c_int * n)(*[int(t) for t in thresholds])
+        rc = self._L.hl_batch(self._h, descs, n, thr, linesmax, out, counts,
+                              self._stream(stream))
+        if rc != _lib.NO_ERROR:
+            return rc, []
+        res = []
+        for i in range(n):
+            res.append([LineParam(*out[i * K + j].as_tuple())
+                        for j in range(max(counts[i], 0))])
+        return rc, res
+
+    def set_batch_graph(self, enable: bool) -> int:
+        return self._L.hl_set_batch_graph(self._h, 1 if enable else 0)
+
+    def autotune(self, images, linesmax: int = 16, thresholds=None, stream=None):
+        """hl_autotune over a list of device Images: (best, [tried...]) as
+        (window_rows, threads, ms) tuples; the best shape stays selected."""
+        n = len(images)
+        descs = (_lib.hl_image_desc * max(n, 1))(*[im.desc() for im in images])
+        thr = None
+        if thresholds is not None:
+            thr = (C.c_int * n)(*[int(t) for t in thresholds])
+        best = _lib.hl_tune_entry()
+        tried = (_lib.hl_tune_entry * 16)()
+        nt = C.c_int()
+        _lib.check(self._L.hl_autotune(self._h, descs, n, thr, linesmax, C.byref(best),
+                                       tried, 16, C.byref(nt), self._stream(stream)),
+                   "hl_autotune")
+        return ((best.window_rows, best.threads, best.ms),
+                [(tried[i].window_rows, tried[i].threads, tried[i].ms)
+                 for i in range(min(nt.value, 16))])
+
     def set_vote_shape(self, window_rows: int = 0, threads: int = 0) -> int:
         return self._L.hl_set_vote_shape(self._h, window_rows, threads)
 

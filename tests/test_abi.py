@@ -54,3 +54,12 @@ def test_null_arguments_rejected_without_gpu():
     assert lib.hl_destroy(None) == _lib.NULL_POINTER
     assert lib.hl_plain(None, None, None, None, None) == _lib.NULL_POINTER
     assert lib.hl_set_vote_shape(None, 0, 0) == _lib.NULL_POINTER
+
+
+def test_batch_entry_points_reject_null_without_gpu():
+    lib = _lib.load()
+    assert lib.hl_batch(None, None, 0, None, 0, None, None, None) == _lib.NULL_POINTER
+    assert lib.hl_batch_async(None, None, 0, None, 0, None, None, None) == _lib.NULL_POINTER
+    assert lib.hl_set_batch_graph(None, 1) == _lib.NULL_POINTER
+    assert lib.hl_autotune(None, None, 0, None, 0, None, None, 0, None, None) == \
+        _lib.NULL_POINTER
