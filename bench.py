@@ -148,6 +148,63 @@ def cpu_reference_images(imgs, budget_s: float, min_images: int = 1):
     return n, el, votes, O.max_threads()
 
 
+def batched_workload(L, HoughLine, Image, dev, sp, reps: int):
+    """The batched configuration: 256 seeded uneven images (sides 256-2048),
+    theta step 0.5 deg, threshold 0.15 * max(w, h) per image, top-32, through
+    one hl_batch_async pipeline (CUDA-graph replay, autotuned vote shape);
+    images resident in HBM, L2 flushed between batches."""
+    import torch
+    import cases
+    n, K, det = 256, 32, math.pi / 360
+    imgs = [cases.synth(3, 1234, i) for i in range(n)]
+    dimgs = [Image.from_host(im, device=dev) for im in imgs]
+    thr = [int(0.15 * max(im.shape)) for im in imgs]
+    votes = sum(int((im == 255).sum()) for im in imgs) * int(math.pi / det)
+    hl = HoughLine(detheta=det)
+    best, _ = hl.autotune(dimgs, K, thr, stream=sp)
+    hl.set_batch_graph(True)
+    descs = (_lib_mod().hl_image_desc * n)(*[d.desc() for d in dimgs])
+    th = (C.c_int * n)(*thr)
+    lines = torch.empty(n * K * 3, dtype=torch.int32, device=dev)
+    counts = torch.zeros(n, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def run():
+        rc = L.hl_batch_async(hl.handle, descs, n, th, K, C.c_void_p(lines.data_ptr()),
+                              C.c_void_p(counts.data_ptr()), sp)
+        if rc != 0:
+            raise RuntimeError(f"hl_batch_async returned {rc}")
+    for _ in range(3):
+        run()
+    torch.cuda.synchronize(dev)
+    ms = []
+    for _ in range(reps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        run()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms.append(e0.elapsed_time(e1))
+    st = C.c_int()
+    L.hl_last_status(hl.handle, C.byref(st), sp)
+    if st.value != 0:
+        raise RuntimeError(f"batched device status {st.value}")
+    t = statistics.median(ms)
+    return {"workload": "batched plain HoughLine: 256 uneven images (w, h in [256, 2048]), "
+                        "T=360, rho +-diag per image, thr 0.15*max(w,h), top-32",
+            "value": n / (t / 1e3), "unit": "images/s", "ms_per_batch": t,
+            "gvotes_per_s": votes / (t / 1e3) / 1e9, "pixels": int(sum(im.size for im in imgs)),
+            "reps": reps, "graph": True, "l2": "flushed between batches",
+            "vote_shape": {"window_rows": best[0], "threads": best[1]}}
+
+
+def _lib_mod():
+    from opencuda_gb300 import _lib
+    return _lib
+
+
 def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
@@ -326,6 +383,8 @@ def run_gb300(args):
         "clocks": ck,
         "wall_s_timed_loop": t_wall,
     }
+    if not args.no_batch:
+        line["batched"] = batched_workload(L, HoughLine, Image, dev, sp, min(max(args.steps, 5), 50))
     if ws == 1 and not args.no_cpu_baseline:
         n, el, v, cores = cpu_reference_images(imgs_host, args.cpu_budget)
         line["cpu_baseline"] = {"value": n / el, "unit": "images/s", "cores": cores,
@@ -344,11 +403,13 @@ def run_gb300(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the batched (256 uneven images) measurement")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

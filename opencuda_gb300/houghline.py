@@ -260,4 +260,6 @@ class HoughLine:
     def _stream(stream):
         if stream is None:
             return None
+        if isinstance(stream, C.c_void_p):
+            return stream
         return C.c_void_p(getattr(stream, "cuda_stream", stream))
