@@ -101,6 +101,7 @@ SIGNATURES = {
     "hl_real_line": (I, [H, C.POINTER(hl_image_desc), I, I, I, I, C.c_float, C.c_float,
                          PI, PI, P]),
     "hl_synth_scene": (I, [C.POINTER(hl_scene_params), P, C.c_long]),
+    "hl_cnn_conv3x3": (I, [P, P, P, P, P, I, I, I, I, I, I, I, I, P, P]),
     "hl_synth_spec": (I, [I, C.c_uint64, I, C.POINTER(hl_scene_params)]),
 }
 

@@ -26,6 +26,7 @@
 #define HL_ST_RHO_OUT_OF_RANGE 0x4
 #define HL_ST_MERGE_OVERFLOW 0x8
 #define HL_ST_VOTE_TIMEOUT 0x10
+#define HL_ST_CNN_TIMEOUT 0x20
 
 /* Result block written by the finalize kernel (device) and copied to the
  * host in one transfer. */

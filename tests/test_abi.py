@@ -10,8 +10,11 @@ from opencuda_gb300 import _lib
 ROOT = Path(__file__).resolve().parent.parent
 
 
+C_HEADERS = ["houghline_gb300.h", "hl_proposal.h"]
+
+
 def declared_symbols():
-    text = (ROOT / "include" / "houghline_gb300.h").read_text()
+    text = "".join((ROOT / "include" / h).read_text() for h in C_HEADERS)
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(hl_[a-z0-9_]+)\s*\(", text)))
 
