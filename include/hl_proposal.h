@@ -33,6 +33,56 @@ int hl_cnn_conv3x3(const void *x, const void *w, const float *bias, void *y,
                    int stride, int relu, int mode, int *status_dev,
                    void *stream);
 
+/* ---- the network --------------------------------------------------------
+ * Input: a 256 x 256 occupancy map per image (bf16, the fraction of edge
+ * pixels in each f x f cell, hl_occupancy).  Six 3x3 convolutions with
+ * padding 1: 1 -> 32 (stride 2), 32 -> 32 (stride 2), three 32 -> 32, then
+ * 32 -> 1, ReLU after all but the last: a 64 x 64 evidence map.  The fixed
+ * coarse Hough head sums the evidence of every cell into 90 angle x 128 rho
+ * bins of the image's own rho range; logits = alpha * sums + beta.  FP32
+ * master weights (flat: per layer W [cout][9 * cin] then b [cout], then
+ * alpha, beta), BF16 copies for the tensor cores. */
+typedef struct hl_net hl_net;
+
+/* Coarse geometry of one image: evidence cell size in pixels, rho range
+ * start, coarse bins per rho unit, evidence cells covering the ROI. */
+typedef struct hl_coarse_geom {
+    float cell;
+    float rho_min;
+    float inv_rw;
+    int qh, qw;
+    int pad;
+} hl_coarse_geom;
+
+int hl_net_create(hl_net **out, unsigned long long seed);
+int hl_net_destroy(hl_net *net);
+int hl_net_num_params(void);
+int hl_net_get_params(hl_net *net, float *host);
+int hl_net_set_params(hl_net *net, const float *host);
+/* gradients of the last hl_net_train_step (host copy, num_params floats) */
+int hl_net_get_grads(hl_net *net, float *host);
+
+/* occ_dev [B][256][256] bf16 -> logits_dev [B][90][128] f32 */
+int hl_net_forward(hl_net *net, const void *occ_dev,
+                   const hl_coarse_geom *geo_host, int B, float *logits_dev,
+                   void *stream);
+
+/* One step on a batch: forward, weighted binary cross-entropy against
+ * target_dev [B][90][128] (1 where a line of the plain method lies, else 0;
+ * positives weighted by pos_weight, mean over cells), backward with the
+ * project's kernels (tensor-core input gradients, FP32 weight gradients),
+ * Adam (lr; gradients clipped to +-1; lr = 0 leaves the weights).  Writes
+ * the loss to *loss_host when not NULL (then synchronises). */
+int hl_net_train_step(hl_net *net, const void *occ_dev,
+                      const hl_coarse_geom *geo_host, const float *target_dev,
+                      int B, float lr, float pos_weight, float *loss_host,
+                      void *stream);
+
+/* Occupancy maps [nimg][256][256] bf16 and coarse geometries of DEVICE
+ * images (the handle gives the rho layout).  Synchronises. */
+int hl_occupancy(hl_handle *h, const hl_image_desc *imgs, int nimg,
+                 void *occ_dev, hl_coarse_geom *geo_host, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

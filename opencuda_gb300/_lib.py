@@ -60,6 +60,11 @@ class hl_scene_params(C.Structure):
                 ("seed", C.c_uint64)]
 
 
+class hl_coarse_geom(C.Structure):
+    _fields_ = [("cell", C.c_float), ("rho_min", C.c_float), ("inv_rw", C.c_float),
+                ("qh", C.c_int), ("qw", C.c_int), ("pad", C.c_int)]
+
+
 class hl_tune_entry(C.Structure):
     _fields_ = [("window_rows", C.c_int), ("threads", C.c_int), ("ms", C.c_float)]
 
@@ -102,6 +107,16 @@ SIGNATURES = {
                          PI, PI, P]),
     "hl_synth_scene": (I, [C.POINTER(hl_scene_params), P, C.c_long]),
     "hl_cnn_conv3x3": (I, [P, P, P, P, P, I, I, I, I, I, I, I, I, P, P]),
+    "hl_net_create": (I, [C.POINTER(P), C.c_ulonglong]),
+    "hl_net_destroy": (I, [P]),
+    "hl_net_num_params": (I, []),
+    "hl_net_get_params": (I, [P, P]),
+    "hl_net_set_params": (I, [P, P]),
+    "hl_net_get_grads": (I, [P, P]),
+    "hl_net_forward": (I, [P, P, C.POINTER(hl_coarse_geom), I, P, P]),
+    "hl_net_train_step": (I, [P, P, C.POINTER(hl_coarse_geom), P, I, C.c_float, C.c_float,
+                              C.POINTER(C.c_float), P]),
+    "hl_occupancy": (I, [H, C.POINTER(hl_image_desc), I, P, C.POINTER(hl_coarse_geom), P]),
     "hl_synth_spec": (I, [I, C.c_uint64, I, C.POINTER(hl_scene_params)]),
 }
 

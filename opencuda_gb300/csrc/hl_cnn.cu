@@ -363,3 +363,401 @@ cudaError_t hl_launch_conv3x3(const hl_conv_args *a, int mode, cudaStream_t s)
         return launch_conv<32, 32, GATHER_CONVT2>(a, sms, s);
     return cudaErrorInvalidValue;
 }
+
+/* ---- occupancy pooling ---------------------------------------------------- */
+
+/* out[b][i][j] (side x side, bf16) = fraction of 255-pixels in the f x f
+ * block (i * f.., j * f..) of image b's ROI; blocks past the ROI count as
+ * empty.  One thread per output cell. */
+__global__ void hl_pool_kernel(const hl_pool_img *imgs, int nimg, int side,
+                               __nv_bfloat16 *out)
+{
+    const int per = side * side;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+         e < (size_t)nimg * per; e += (size_t)gridDim.x * blockDim.x) {
+        const int b = (int)(e / per), r = (int)(e % per);
+        const int i = r / side, j = r % side;
+        const hl_pool_img im = imgs[b];
+        const int f = im.factor;
+        int cnt = 0;
+        const int y0 = i * f, x0 = j * f;
+        for (int y = y0; y < min(y0 + f, im.h); y++) {
+            const uint8_t *row = im.base + (size_t)y * im.pitch;
+            for (int x = x0; x < min(x0 + f, im.w); x++)
+                cnt += row[x] == 255;
+        }
+        out[e] = __float2bfloat16((float)cnt / (float)(f * f));
+    }
+}
+
+cudaError_t hl_launch_pool(const hl_pool_img *imgs, int nimg, int side,
+                           __nv_bfloat16 *out, cudaStream_t s)
+{
+    const size_t n = (size_t)nimg * side * side;
+    const int blocks = (int)std::min((n + 255) / 256, (size_t)4096);
+    hl_pool_kernel<<<std::max(blocks, 1), 256, 0, s>>>(imgs, nimg, side, out);
+    return cudaGetLastError();
+}
+
+/* ---- weight and bias gradients (CUDA cores, FP32) ------------------------ */
+
+/* dw[co][tap * cin + ci] += sum over pixels of dy[p][co] * x[in(p, tap)][ci].
+ * Thread (tap, ci) keeps 32 accumulators (one per co); a CTA walks chunks of
+ * DW_CHUNK output pixels grid-stride, with the chunk's dy rows in shared
+ * memory, and adds its sums into dw once at the end.  dy: [P][32] f32 (the
+ * output gradient after the ReLU mask), x: bf16 NHWC with cin channels
+ * (32-channel rows for cin = 32, one value for cin = 1). */
+#define DW_CHUNK 64
+__global__ void __launch_bounds__(288)
+hl_conv_dw_kernel(hl_dw_args a)
+{
+    __shared__ float s_dy[DW_CHUNK][32];
+    const int t = threadIdx.x;
+    const int tap = t / 32 < 9 ? t / 32 : 8, ci = t % 32;
+    const bool act = t < 9 * a.cin;   /* cin = 1: threads 0..8 (ci = t) */
+    const int my_tap = a.cin == 32 ? tap : t, my_ci = a.cin == 32 ? ci : 0;
+    const int ky = my_tap / 3, kx = my_tap % 3;
+    float acc[32];
+#pragma unroll
+    for (int c = 0; c < 32; c++)
+        acc[c] = 0.0f;
+    const int HWo = a.Ho * a.Wo;
+    const long long P = (long long)a.B * HWo;
+    for (long long p0 = (long long)blockIdx.x * DW_CHUNK; p0 < P;
+         p0 += (long long)gridDim.x * DW_CHUNK) {
+        for (int e = t; e < DW_CHUNK * 32; e += blockDim.x) {
+            const long long p = p0 + e / 32;
+            s_dy[e / 32][e % 32] =
+                (p < P && (e % 32) < a.dy_c) ? a.dy[p * a.dy_c + (e % 32)] : 0.0f;
+        }
+        __syncthreads();
+        if (act) {
+            for (int q = 0; q < DW_CHUNK; q++) {
+                const long long p = p0 + q;
+                if (p >= P)
+                    break;
+                const int b = (int)(p / HWo), r = (int)(p % HWo);
+                const int oy = r / a.Wo, ox = r % a.Wo;
+                const int iy = oy * a.stride - 1 + ky, ix = ox * a.stride - 1 + kx;
+                float xv = 0.0f;
+                if (iy >= 0 && ix >= 0 && iy < a.H && ix < a.W)
+                    xv = __bfloat162float(
+                        a.x[(((size_t)b * a.H + iy) * a.W + ix) * a.cin + my_ci]);
+#pragma unroll
+                for (int c = 0; c < 32; c++)
+                    acc[c] = fmaf(s_dy[q][c], xv, acc[c]);
+            }
+        }
+        __syncthreads();
+    }
+    if (act) {
+        const int kreal = 9 * a.cin;
+        const int k = my_tap * a.cin + my_ci;
+        for (int c = 0; c < a.cout; c++)
+            atomicAdd(&a.dw[(size_t)c * kreal + k], acc[c]);
+    }
+}
+
+/* db[c] += sum over pixels of dy[p][c] (dy rows of dy_c values) */
+__global__ void hl_bias_grad_kernel(const float *dy, int dy_c, long long P, int cout,
+                                    float *db)
+{
+    __shared__ float s[32][33];
+    const int c = threadIdx.x & 31, row = threadIdx.x >> 5;   /* 256 threads */
+    float acc = 0.0f;
+    if (c < dy_c)
+        for (long long p = (long long)blockIdx.x * 8 + row; p < P;
+             p += (long long)gridDim.x * 8)
+            acc += dy[p * dy_c + c];
+    s[row][c] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        float t = 0.0f;
+        for (int r = 0; r < 8; r++)
+            t += s[r][threadIdx.x];
+        if (threadIdx.x < cout)
+            atomicAdd(&db[threadIdx.x], t);
+    }
+}
+
+cudaError_t hl_launch_conv_dw(const hl_dw_args *a, cudaStream_t s)
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long P = (long long)a->B * a->Ho * a->Wo;
+    const int chunks = (int)((P + DW_CHUNK - 1) / DW_CHUNK);
+    hl_conv_dw_kernel<<<std::max(1, std::min(chunks, sms * 4)), 288, 0, s>>>(*a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || !a->db)
+        return e;
+    const int blocks = (int)std::max(1LL, std::min((P + 7) / 8, (long long)sms * 4));
+    hl_bias_grad_kernel<<<blocks, 256, 0, s>>>(a->dy, a->dy_c, P, a->cout, a->db);
+    return cudaGetLastError();
+}
+
+/* dy (bf16 NHWC 32) * [y > 0] -> f32 [P][32] and a bf16 copy (the next
+ * backward convolution's operand); y is the layer's ReLU output.  For a
+ * one-channel gradient (dy32 == NULL): g [P] f32 -> bf16 [P]. */
+__global__ void hl_relu_mask_kernel(const __nv_bfloat16 *dx, const __nv_bfloat16 *y,
+                                    long long n, float *out_f32,
+                                    __nv_bfloat16 *out_bf16)
+{
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        float g = __bfloat162float(dx[e]);
+        if (y && !(__bfloat162float(y[e]) > 0.0f))
+            g = 0.0f;
+        if (out_f32)
+            out_f32[e] = g;
+        if (out_bf16)
+            out_bf16[e] = __float2bfloat16(g);
+    }
+}
+
+cudaError_t hl_launch_relu_mask(const __nv_bfloat16 *dx, const __nv_bfloat16 *y,
+                                long long n, float *out_f32,
+                                __nv_bfloat16 *out_bf16, cudaStream_t s)
+{
+    const int blocks = (int)std::max(1LL, std::min((n + 255) / 256, 8192LL));
+    hl_relu_mask_kernel<<<blocks, 256, 0, s>>>(dx, y, n, out_f32, out_bf16);
+    return cudaGetLastError();
+}
+
+/* ---- coarse Hough head ------------------------------------------------------ */
+
+/* cos and sin of the coarse angles (t + 0.5) * pi / HL_HEAD_T, evaluated in
+ * double on the host and rounded to float; passed by value */
+struct HeadTrig {
+    float c[HL_HEAD_T], s[HL_HEAD_T];
+};
+
+static const HeadTrig &head_trig()
+{
+    static HeadTrig t;
+    static bool init = false;
+    if (!init) {
+        for (int i = 0; i < HL_HEAD_T; i++) {
+            const double th = ((double)i + 0.5) * 3.14159265358979323846 / HL_HEAD_T;
+            t.c[i] = (float)cos(th);
+            t.s[i] = (float)sin(th);
+        }
+        init = true;
+    }
+    return t;
+}
+
+/* bin of evidence cell (qy, qx) of image geometry g at coarse angle t; every
+ * operation rounded as written so the CPU oracle reproduces it */
+__device__ __forceinline__ int head_bin(const hl_head_geom &g, int qy, int qx,
+                                        float c, float s)
+{
+    const float x = __fmul_rn(__fadd_rn((float)qx, 0.5f), g.cell);
+    const float y = __fmul_rn(__fadd_rn((float)qy, 0.5f), g.cell);
+    const float rho = __fadd_rn(__fmul_rn(x, c), __fmul_rn(y, s));
+    int r = (int)floorf(__fmul_rn(__fsub_rn(rho, g.rho_min), g.inv_rw));
+    return min(max(r, 0), HL_HEAD_R - 1);
+}
+
+/* logits[b][t][r] = alpha * sum_{cells with bin r at angle t} e[b][cell] + beta
+ * One CTA per image, the [T][R] sums in shared memory. */
+__global__ void __launch_bounds__(512)
+hl_head_fwd_kernel(const float *e, int ev, const hl_head_geom *geo,
+                   const float *ab, float *hsum, float *logits, HeadTrig tr)
+{
+    __shared__ float sh[HL_HEAD_T * HL_HEAD_R];
+    __shared__ float cs[HL_HEAD_T], sn[HL_HEAD_T];
+    const int b = blockIdx.x;
+    for (int i = threadIdx.x; i < HL_HEAD_T * HL_HEAD_R; i += blockDim.x)
+        sh[i] = 0.0f;
+    if (threadIdx.x < HL_HEAD_T) {
+        cs[threadIdx.x] = tr.c[threadIdx.x];
+        sn[threadIdx.x] = tr.s[threadIdx.x];
+    }
+    __syncthreads();
+    const hl_head_geom g = geo[b];
+    const float *eb = e + (size_t)b * ev * ev;
+    for (int p = threadIdx.x; p < g.qh * ev; p += blockDim.x) {
+        const int qy = p / ev, qx = p % ev;
+        if (qx >= g.qw)
+            continue;
+        const float v = eb[qy * ev + qx];
+        if (v == 0.0f)
+            continue;
+        for (int t = 0; t < HL_HEAD_T; t++)
+            atomicAdd(&sh[t * HL_HEAD_R + head_bin(g, qy, qx, cs[t], sn[t])], v);
+    }
+    __syncthreads();
+    const float alpha = ab[0], beta = ab[1];
+    for (int i = threadIdx.x; i < HL_HEAD_T * HL_HEAD_R; i += blockDim.x) {
+        hsum[(size_t)b * HL_HEAD_T * HL_HEAD_R + i] = sh[i];
+        logits[(size_t)b * HL_HEAD_T * HL_HEAD_R + i] = alpha * sh[i] + beta;
+    }
+}
+
+/* de[b][cell] = alpha * sum_t dz[b][t][bin(cell, t)] (the gather transpose of
+ * the head); one CTA per image */
+__global__ void __launch_bounds__(512)
+hl_head_bwd_kernel(const float *dz, int ev, const hl_head_geom *geo,
+                   const float *ab, float *de, HeadTrig tr)
+{
+    __shared__ float sd[HL_HEAD_T * HL_HEAD_R];
+    __shared__ float cs[HL_HEAD_T], sn[HL_HEAD_T];
+    const int b = blockIdx.x;
+    for (int i = threadIdx.x; i < HL_HEAD_T * HL_HEAD_R; i += blockDim.x)
+        sd[i] = dz[(size_t)b * HL_HEAD_T * HL_HEAD_R + i];
+    if (threadIdx.x < HL_HEAD_T) {
+        cs[threadIdx.x] = tr.c[threadIdx.x];
+        sn[threadIdx.x] = tr.s[threadIdx.x];
+    }
+    __syncthreads();
+    const hl_head_geom g = geo[b];
+    const float alpha = ab[0];
+    for (int p = threadIdx.x; p < ev * ev; p += blockDim.x) {
+        const int qy = p / ev, qx = p % ev;
+        float acc = 0.0f;
+        if (qy < g.qh && qx < g.qw)
+            for (int t = 0; t < HL_HEAD_T; t++)
+                acc += sd[t * HL_HEAD_R + head_bin(g, qy, qx, cs[t], sn[t])];
+        de[(size_t)b * ev * ev + p] = alpha * acc;
+    }
+}
+
+cudaError_t hl_launch_head_fwd(const float *e, int ev, const hl_head_geom *geo,
+                               int nimg, const float *ab, float *hsum,
+                               float *logits, cudaStream_t s)
+{
+    hl_head_fwd_kernel<<<nimg, 512, 0, s>>>(e, ev, geo, ab, hsum, logits, head_trig());
+    return cudaGetLastError();
+}
+
+cudaError_t hl_launch_head_bwd(const float *dz, int ev, const hl_head_geom *geo,
+                               int nimg, const float *ab, float *de, cudaStream_t s)
+{
+    hl_head_bwd_kernel<<<nimg, 512, 0, s>>>(dz, ev, geo, ab, de, head_trig());
+    return cudaGetLastError();
+}
+
+/* ---- loss ------------------------------------------------------------------- */
+
+/* Weighted binary cross-entropy on logits: per cell
+ * l = -(wpos * y * log s + (1 - y) * log(1 - s)), s = sigmoid(z); dz = dl/dz /
+ * n; also d alpha = sum dz * hsum, d beta = sum dz and the summed loss. */
+__global__ void hl_bce_kernel(const float *z, const float *y, const float *hsum,
+                              long long n, float wpos, float *dz, float *dab,
+                              float *loss)
+{
+    __shared__ float r[3][256];
+    float la = 0.0f, ga = 0.0f, gb = 0.0f;
+    const float inv = 1.0f / (float)n;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const float zz = z[e], yy = y[e];
+        /* log(1 + exp(-|z|)) form, stable for large |z| */
+        const float sp = log1pf(expf(-fabsf(zz)));
+        const float log_s = fminf(zz, 0.0f) - sp;       /* log sigmoid(z) */
+        const float log_1s = fminf(-zz, 0.0f) - sp;     /* log(1 - sigmoid(z)) */
+        la += -(wpos * yy * log_s + (1.0f - yy) * log_1s);
+        const float sg = 1.0f / (1.0f + expf(-zz));
+        const float g = (wpos * yy * (sg - 1.0f) + (1.0f - yy) * sg) * inv;
+        dz[e] = g;
+        ga += g * hsum[e];
+        gb += g;
+    }
+    r[0][threadIdx.x] = la;
+    r[1][threadIdx.x] = ga;
+    r[2][threadIdx.x] = gb;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+            for (int k = 0; k < 3; k++)
+                r[k][threadIdx.x] += r[k][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        atomicAdd(loss, r[0][0] * inv);
+        atomicAdd(&dab[0], r[1][0]);
+        atomicAdd(&dab[1], r[2][0]);
+    }
+}
+
+cudaError_t hl_launch_bce(const float *z, const float *y, const float *hsum,
+                          long long n, float wpos, float *dz, float *dab,
+                          float *loss, cudaStream_t s)
+{
+    hl_bce_kernel<<<256, 256, 0, s>>>(z, y, hsum, n, wpos, dz, dab, loss);
+    return cudaGetLastError();
+}
+
+/* ---- Adam and weight layouts ---------------------------------------------- */
+
+__global__ void hl_adam_kernel(float *w, const float *g, float *m, float *v, int n,
+                               float lr, float b1, float b2, float eps, float c1,
+                               float c2, float clip)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += gridDim.x * blockDim.x) {
+        const float gi = fminf(fmaxf(g[i], -clip), clip);
+        const float mi = b1 * m[i] + (1.0f - b1) * gi;
+        const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        w[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+    }
+}
+
+cudaError_t hl_launch_adam(float *w, const float *g, float *m, float *v, int n,
+                           float lr, int step, float clip, cudaStream_t s)
+{
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.0f / (1.0f - powf(b1, (float)step));
+    const float c2 = 1.0f / (1.0f - powf(b2, (float)step));
+    hl_adam_kernel<<<(n + 255) / 256, 256, 0, s>>>(w, g, m, v, n, lr, b1, b2, 1e-8f,
+                                                   c1, c2, clip);
+    return cudaGetLastError();
+}
+
+/* FP32 master weights [cout][9 * cin] -> the bf16 operand of one layer:
+ * mode 0 forward (same layout), mode 1 flipped and transposed ([cin][tap][cout]
+ * with tap -> 8 - tap: the stride-1 input gradient as a convolution), mode 2
+ * transposed ([cin][tap][cout]: the stride-2 input-gradient gather). */
+__global__ void hl_weight_layout_kernel(const float *w, int cout, int cin, int mode,
+                                        __nv_bfloat16 *out)
+{
+    const int n = cout * 9 * cin;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += gridDim.x * blockDim.x) {
+        const int co = i / (9 * cin), r = i % (9 * cin);
+        const int tap = r / cin, ci = r % cin;
+        const float v = w[i];
+        if (mode == 0)
+            out[i] = __float2bfloat16(v);
+        else if (mode == 1)
+            out[((size_t)ci * 9 + (8 - tap)) * cout + co] = __float2bfloat16(v);
+        else
+            out[((size_t)ci * 9 + tap) * cout + co] = __float2bfloat16(v);
+    }
+}
+
+cudaError_t hl_launch_weight_layout(const float *w, int cout, int cin, int mode,
+                                    __nv_bfloat16 *out, cudaStream_t s)
+{
+    const int n = cout * 9 * cin;
+    hl_weight_layout_kernel<<<(n + 255) / 256, 256, 0, s>>>(w, cout, cin, mode, out);
+    return cudaGetLastError();
+}
+
+__global__ void hl_f32_to_bf16_kernel(const float *in, long long n, __nv_bfloat16 *out)
+{
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x)
+        out[e] = __float2bfloat16(in[e]);
+}
+
+cudaError_t hl_launch_f32_to_bf16(const float *in, long long n, __nv_bfloat16 *out,
+                                  cudaStream_t s)
+{
+    const int blocks = (int)std::max(1LL, std::min((n + 255) / 256, 8192LL));
+    hl_f32_to_bf16_kernel<<<blocks, 256, 0, s>>>(in, n, out);
+    return cudaGetLastError();
+}

@@ -114,3 +114,58 @@ def test_conv_stride1_input_gradient_is_a_convolution():
     ref = CO.conv3x3_dx(dy, w, 9, 7, 1)
     got = CO.conv3x3(dy, CO.transpose_weights(wf))
     assert np.allclose(got, ref)
+
+
+def _occ_problem(seed, B=2):
+    rng = np.random.default_rng(seed)
+    occ = np.zeros((B, 256, 256), np.float32)
+    for b in range(B):
+        for _ in range(6):       # a few lines of occupancy ~1/8
+            y0, x0 = rng.integers(0, 256, 2)
+            ang = rng.random() * np.pi
+            for tt in range(-150, 150):
+                y = int(y0 + tt * np.sin(ang))
+                x = int(x0 + tt * np.cos(ang))
+                if 0 <= y < 256 and 0 <= x < 256:
+                    occ[b, y, x] = 0.125
+        occ[b] += (rng.random((256, 256)) < 0.02) * 0.015625
+    occ = CO.bf16_round(occ)
+    geos = [(32.0, -2896.0, 128 / 5793.0, 64, 64), (16.0, -1448.0, 128 / 2897.0, 64, 50)][:B]
+    return occ, geos
+
+
+def test_network_forward_matches_oracle(lib):
+    import torch
+    from opencuda_gb300.proposal import HoughNet
+    occ, geos = _occ_problem(3)
+    net = HoughNet(seed=7)
+    p = net.get_params()
+    dev = _dev_bf16(torch, occ)
+    z = net.forward(dev, HoughNet.geos(geos)).cpu().numpy()
+    zr, H, e, acts, bins = CO.net_forward(occ, geos, p.astype(np.float64))
+    err = np.abs(z - zr)
+    assert err.max() <= 1e-2 * max(1.0, np.abs(zr).max()), err.max()
+
+
+def test_network_gradients_match_oracle(lib):
+    import torch
+    from opencuda_gb300.proposal import HoughNet
+    occ, geos = _occ_problem(4)
+    net = HoughNet(seed=11)
+    p = net.get_params()
+    rng = np.random.default_rng(5)
+    target = (rng.random((2, 90, 128)) < 0.005).astype(np.float32)
+    dev = _dev_bf16(torch, occ)
+    loss = net.train_step(dev, HoughNet.geos(geos), torch.from_numpy(target).cuda(), 0.0, 30.0)
+    g = net.get_grads()
+    assert np.array_equal(net.get_params(), p)       # lr = 0 leaves the weights
+    lref, gref = CO.net_loss_grads(occ, geos, p.astype(np.float64), target, 30.0)
+    assert abs(loss - lref) <= 1e-3 * abs(lref) + 1e-5
+    o = 0
+    for ci, co, _, _ in CO.LAYERS:
+        for n in (co * 9 * ci, co):
+            a, b = g[o:o + n], gref[o:o + n]
+            rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
+            assert rel < 0.05, (o, n, rel)
+            o += n
+    assert np.allclose(g[o:], gref[o:], rtol=1e-3, atol=1e-6)
