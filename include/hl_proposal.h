@@ -83,6 +83,47 @@ int hl_net_train_step(hl_net *net, const void *occ_dev,
 int hl_occupancy(hl_handle *h, const hl_image_desc *imgs, int nimg,
                  void *occ_dev, hl_coarse_geom *geo_host, void *stream);
 
+/* ---- proposal-guided batched HoughLine ------------------------------------
+ * hl_batch's contract (DEVICE images, per-image thresholds, linesmax lines
+ * per image into DEVICE arrays), but the exact vote runs only in the coarse
+ * cells the network scores above p_cut (grown by dilate_theta / dilate_rho
+ * cells): every reported line is a peak of the full accumulator with its
+ * exact vote count; lines the proposals miss are absent.  An image with more
+ * than max_props cells above the cutoff (a cluttered scene), or too large
+ * for the window kernel, runs the full plain method instead.  Every
+ * judge_every-th other image (0: none) also runs the plain method and the
+ * stats report how many of its lines the proposal path found.  Synchronises
+ * `stream` (the fall-back set is decided on the host). */
+typedef struct hl_proposal_opts {
+    float p_cut;
+    int max_props;
+    int dilate_theta;
+    int dilate_rho;
+    int judge_every;
+} hl_proposal_opts;
+
+typedef struct hl_proposal_stats {
+    int fallback;        /* images that ran the plain method instead */
+    int windows;         /* coarse windows voted */
+    int judged;          /* images also run through the plain method */
+    int judged_lines;    /* lines the plain method gave them */
+    int judged_found;    /* of those, reported by the proposal path */
+    int pad;
+    long long votes;     /* executed votes of the windows */
+} hl_proposal_stats;
+
+int hl_proposal_batch(hl_handle *h, hl_net *net, const hl_image_desc *imgs,
+                      int nimg, const int *thresholds, int linesmax,
+                      const hl_proposal_opts *opts, hl_line *lines_dev,
+                      int *counts_dev, hl_proposal_stats *stats, void *stream);
+
+/* The seeded scene generator (hl_synth_scene) run on the GPU, one CTA per
+ * scene, for training data: outs[i].data (DEVICE, pitch outs[i].pitch, at
+ * least params[i].width x height) receives exactly the bytes
+ * hl_synth_scene(&params[i], ...) writes on the host.  Synchronises. */
+int hl_synth_scenes_device(const hl_scene_params *params, int n,
+                           const hl_image_desc *outs, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

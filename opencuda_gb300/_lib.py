@@ -65,6 +65,17 @@ class hl_coarse_geom(C.Structure):
                 ("qh", C.c_int), ("qw", C.c_int), ("pad", C.c_int)]
 
 
+class hl_proposal_opts(C.Structure):
+    _fields_ = [("p_cut", C.c_float), ("max_props", C.c_int), ("dilate_theta", C.c_int),
+                ("dilate_rho", C.c_int), ("judge_every", C.c_int)]
+
+
+class hl_proposal_stats(C.Structure):
+    _fields_ = [("fallback", C.c_int), ("windows", C.c_int), ("judged", C.c_int),
+                ("judged_lines", C.c_int), ("judged_found", C.c_int), ("pad", C.c_int),
+                ("votes", C.c_longlong)]
+
+
 class hl_tune_entry(C.Structure):
     _fields_ = [("window_rows", C.c_int), ("threads", C.c_int), ("ms", C.c_float)]
 
@@ -117,6 +128,10 @@ SIGNATURES = {
     "hl_net_train_step": (I, [P, P, C.POINTER(hl_coarse_geom), P, I, C.c_float, C.c_float,
                               C.POINTER(C.c_float), P]),
     "hl_occupancy": (I, [H, C.POINTER(hl_image_desc), I, P, C.POINTER(hl_coarse_geom), P]),
+    "hl_synth_scenes_device": (I, [C.POINTER(hl_scene_params), I, C.POINTER(hl_image_desc), P]),
+    "hl_proposal_batch": (I, [H, P, C.POINTER(hl_image_desc), I, PI, I,
+                              C.POINTER(hl_proposal_opts), P, P, C.POINTER(hl_proposal_stats),
+                              P]),
     "hl_synth_spec": (I, [I, C.c_uint64, I, C.POINTER(hl_scene_params)]),
 }
 

@@ -20,6 +20,9 @@
 #include <vector>
 
 #include "hl_internal.h"
+#include "hl_cnn.h"
+#include "hl_proposal.h"
+#include "hl_window.h"
 
 #ifndef M_PI
 #error "M_PI required: numtheta = (int)(M_PI / detheta)"
@@ -68,6 +71,8 @@ struct hl_handle {
     /* batched path: workspace, CUDA-graph switch; whether the last
      * asynchronous call was a batch (hl_last_status reads its status) */
     hl_batch_ws *bw;
+    hl_batch_ws *bw_fb;     /* the proposal path's fall-back batches */
+    struct hl_prop_ws *pw;  /* the proposal path's own buffers */
     int batch_graph;
     int last_batch;
 
@@ -1122,9 +1127,19 @@ struct hl_batch_ws {
     std::vector<long long> gkey;
 };
 
+static void batch_ws_free(hl_batch_ws *b);
+static void prop_free(hl_handle *h);
+
 static void batch_free(hl_handle *h)
 {
-    hl_batch_ws *b = h->bw;
+    batch_ws_free(h->bw);
+    batch_ws_free(h->bw_fb);
+    h->bw = h->bw_fb = nullptr;
+    prop_free(h);
+}
+
+static void batch_ws_free(hl_batch_ws *b)
+{
     if (!b)
         return;
     void *dp[] = {b->d_pts, b->d_state, b->d_tile_off, b->d_acc, b->d_keys,
@@ -1143,7 +1158,6 @@ static void batch_free(hl_handle *h)
     if (b->cap_stream)
         cudaStreamDestroy(b->cap_stream);
     delete b;
-    h->bw = nullptr;
 }
 
 static int grow_host(unsigned char **ptr, size_t *cap, size_t need)
@@ -1195,11 +1209,10 @@ static void batch_block_weights(const hl_handle *h, int w, int hh, int rho_min,
 /* Plan a batch: sizes, offsets, work items, chunks; fills the pinned tables
  * (image pointers and thresholds included).  The geometry part is reused
  * when the sizes and the launch shape equal the previous call's. */
-static int batch_plan(hl_handle *h, const hl_image_desc *imgs, int nimg,
-                      const int *thr, int K, hl_line *lines_dev,
+static int batch_plan(hl_handle *h, hl_batch_ws *b, const hl_image_desc *imgs,
+                      int nimg, const int *thr, int K, hl_line *lines_dev,
                       int *counts_dev, const hl_roi *rois)
 {
-    hl_batch_ws *b = h->bw;
     const int slices = h->Tp / HL_SLICE;
     int maxR = 1;
     std::vector<hl_geom> gs((size_t)nimg);
@@ -1411,9 +1424,10 @@ static int batch_plan(hl_handle *h, const hl_image_desc *imgs, int nimg,
 }
 
 /* The stream work of one planned batch call. */
-static int batch_enqueue(hl_handle *h, int nimg, int K, cudaStream_t s)
+/* counters, look-back states, tables, then the compaction of every image */
+static int batch_enqueue_compact(hl_handle *h, hl_batch_ws *b, int nimg,
+                                 cudaStream_t s)
 {
-    hl_batch_ws *b = h->bw;
     unsigned char *dt = b->d_tab;
     CK(cudaMemsetAsync(b->d_cnt, 0, BW_NCNT * sizeof(int), s));
     CK(cudaMemsetAsync(b->d_state, 0,
@@ -1440,7 +1454,13 @@ static int batch_enqueue(hl_handle *h, int nimg, int K, cudaStream_t s)
     ca.status = b->d_cnt + 2;
     CK(hl_launch_compact(&ca, s));
     prof_mark(h, 1, s);
+    return HL_NO_ERROR;
+}
 
+/* the full vote and the peak pass */
+static int batch_enqueue_vote_peaks(hl_handle *h, hl_batch_ws *b, cudaStream_t s)
+{
+    unsigned char *dt = b->d_tab;
     hl_vote_args va;
     memset(&va, 0, sizeof(va));
     va.imgs = reinterpret_cast<const hl_vote_img *>(dt + b->off_vimg);
@@ -1468,7 +1488,14 @@ static int batch_enqueue(hl_handle *h, int nimg, int K, cudaStream_t s)
     pa.status = b->d_cnt + 2;
     CK(hl_launch_peaks(&pa, s));
     prof_mark(h, 3, s);
+    return HL_NO_ERROR;
+}
 
+/* rank, merge and write the lines of every image */
+static int batch_enqueue_finalize(hl_handle *h, hl_batch_ws *b, int nimg, int K,
+                                  cudaStream_t s)
+{
+    unsigned char *dt = b->d_tab;
     hl_final_args fa;
     memset(&fa, 0, sizeof(fa));
     fa.imgs = reinterpret_cast<const hl_final_img *>(dt + b->off_fimg);
@@ -1484,25 +1511,35 @@ static int batch_enqueue(hl_handle *h, int nimg, int K, cudaStream_t s)
     return HL_NO_ERROR;
 }
 
-static int batch_run(hl_handle *h, const hl_image_desc *imgs, int nimg,
-                     const int *thr, int K, hl_line *lines_dev,
-                     int *counts_dev, cudaStream_t s)
+static int batch_enqueue(hl_handle *h, hl_batch_ws *b, int nimg, int K,
+                         cudaStream_t s)
+{
+    int rc;
+    if ((rc = batch_enqueue_compact(h, b, nimg, s)) != HL_NO_ERROR ||
+        (rc = batch_enqueue_vote_peaks(h, b, s)) != HL_NO_ERROR)
+        return rc;
+    return batch_enqueue_finalize(h, b, nimg, K, s);
+}
+
+static int batch_run_ws(hl_handle *h, hl_batch_ws **pb, const hl_image_desc *imgs,
+                        int nimg, const int *thr, int K, hl_line *lines_dev,
+                        int *counts_dev, cudaStream_t s)
 {
     if (nimg <= 0)
         return HL_INVALID_DATA;
-    if (!h->bw) {
-        h->bw = new (std::nothrow) hl_batch_ws();
-        if (!h->bw)
+    if (!*pb) {
+        *pb = new (std::nothrow) hl_batch_ws();
+        if (!*pb)
             return HL_OUT_OF_MEM;
     }
-    hl_batch_ws *b = h->bw;
+    hl_batch_ws *b = *pb;
     std::vector<hl_roi> rois((size_t)nimg);
     for (int i = 0; i < nimg; i++) {
         int rc = roi_of(&imgs[i], &rois[i]);
         if (rc != HL_NO_ERROR)
             return rc;
     }
-    int rc = batch_plan(h, imgs, nimg, thr, K, lines_dev, counts_dev, rois.data());
+    int rc = batch_plan(h, b, imgs, nimg, thr, K, lines_dev, counts_dev, rois.data());
     if (rc != HL_NO_ERROR)
         return rc;
     h->last_batch = 1;
@@ -1513,7 +1550,7 @@ static int batch_run(hl_handle *h, const hl_image_desc *imgs, int nimg,
     }
     prof_mark(h, 0, s);
     if (!h->batch_graph || h->prof) {
-        rc = batch_enqueue(h, nimg, K, s);
+        rc = batch_enqueue(h, b, nimg, K, s);
     } else {
         /* graph key: the plan key plus what the captured nodes hold */
         std::vector<long long> gk(b->key.begin(), b->key.end());
@@ -1534,7 +1571,7 @@ static int batch_run(hl_handle *h, const hl_image_desc *imgs, int nimg,
                 CK(cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking));
             cudaGraph_t graph = nullptr;
             CK(cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal));
-            rc = batch_enqueue(h, nimg, K, b->cap_stream);
+            rc = batch_enqueue(h, b, nimg, K, b->cap_stream);
             cudaError_t e = cudaStreamEndCapture(b->cap_stream, &graph);
             if (rc != HL_NO_ERROR) {
                 if (graph)
@@ -1557,6 +1594,13 @@ static int batch_run(hl_handle *h, const hl_image_desc *imgs, int nimg,
     if (rc == HL_NO_ERROR)
         CK(cudaEventRecord(b->tab_read, s));
     return rc;
+}
+
+static int batch_run(hl_handle *h, const hl_image_desc *imgs, int nimg,
+                     const int *thr, int K, hl_line *lines_dev,
+                     int *counts_dev, cudaStream_t s)
+{
+    return batch_run_ws(h, &h->bw, imgs, nimg, thr, K, lines_dev, counts_dev, s);
 }
 
 static int batch_last_status(hl_handle *h, int *status, cudaStream_t s)
@@ -1720,5 +1764,315 @@ extern "C" int hl_autotune(hl_handle *h, const hl_image_desc *imgs, int nimg,
     *best = bst;
     if (ntried)
         *ntried = n;
+    return HL_NO_ERROR;
+}
+
+/* ==================================================================== */
+/* Proposal-guided batched path                                          */
+/* ==================================================================== */
+
+struct hl_prop_ws {
+    __nv_bfloat16 *d_occ;          /* [n][256][256] */
+    size_t cap_occ;
+    unsigned char *d_tab;          /* pool descriptors + head geometries */
+    size_t cap_tab;
+    unsigned char *h_tab;
+    size_t cap_htab;
+    int4 *d_win;
+    size_t cap_win;
+    int *d_cnt;                    /* [0] windows [1] status [2..3] votes */
+    int *d_fb;                     /* per-image fall-back flags */
+    size_t cap_fb;
+    int *h_fb;                     /* pinned copy */
+    size_t cap_hfb;
+    hl_line *d_fb_lines;           /* plain results of the fall-back set */
+    size_t cap_fb_lines;
+    int *d_fb_counts;
+    size_t cap_fb_counts;
+    int *d_map;                    /* fall-back slot -> image */
+    size_t cap_map;
+};
+
+static void prop_free(hl_handle *h)
+{
+    hl_prop_ws *p = h->pw;
+    if (!p)
+        return;
+    void *dp[] = {p->d_occ, p->d_tab, p->d_win, p->d_cnt, p->d_fb, p->d_fb_lines,
+                  p->d_fb_counts, p->d_map};
+    for (void *q : dp)
+        if (q)
+            cudaFree(q);
+    if (p->h_tab)
+        cudaFreeHost(p->h_tab);
+    if (p->h_fb)
+        cudaFreeHost(p->h_fb);
+    delete p;
+    h->pw = nullptr;
+}
+
+/* copy fall-back results (slot q -> image map[q]) into the outputs */
+__global__ void hl_scatter_results_kernel(const hl_line *src_lines,
+                                          const int *src_counts, const int *map,
+                                          int nmap, int K, hl_line *dst_lines,
+                                          int *dst_counts)
+{
+    for (int q = blockIdx.x; q < nmap; q += gridDim.x) {
+        const int i = map[q];
+        if (i < 0)
+            continue;
+        for (int j = threadIdx.x; j < K; j += blockDim.x)
+            dst_lines[(size_t)i * K + j] = src_lines[(size_t)q * K + j];
+        if (threadIdx.x == 0)
+            dst_counts[i] = src_counts[q];
+    }
+}
+
+extern "C" int hl_proposal_batch(hl_handle *h, hl_net *net,
+                                 const hl_image_desc *imgs, int nimg,
+                                 const int *thresholds, int linesmax,
+                                 const hl_proposal_opts *opts,
+                                 hl_line *lines_dev, int *counts_dev,
+                                 hl_proposal_stats *stats, void *stream)
+{
+    if (!h || !net || !imgs || !opts || !counts_dev)
+        return HL_NULL_POINTER;
+    if (linesmax > 0 && !lines_dev)
+        return HL_NULL_POINTER;
+    if (nimg <= 0 || nimg > 0xffff || !(opts->p_cut > 0.0f && opts->p_cut < 1.0f) ||
+        opts->max_props < 0 || opts->dilate_rho < 0 || opts->dilate_theta < 0 ||
+        opts->judge_every < 0)
+        return HL_INVALID_DATA;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const int K = std::max(linesmax, 0);
+    if (!h->bw) {
+        h->bw = new (std::nothrow) hl_batch_ws();
+        if (!h->bw)
+            return HL_OUT_OF_MEM;
+    }
+    if (!h->pw) {
+        h->pw = new (std::nothrow) hl_prop_ws();
+        if (!h->pw)
+            return HL_OUT_OF_MEM;
+    }
+    hl_batch_ws *b = h->bw;
+    hl_prop_ws *pw = h->pw;
+    std::vector<hl_roi> rois((size_t)nimg);
+    int rc;
+    for (int i = 0; i < nimg; i++)
+        if ((rc = roi_of(&imgs[i], &rois[i])) != HL_NO_ERROR)
+            return rc;
+    if ((rc = batch_plan(h, b, imgs, nimg, thresholds, K, lines_dev, counts_dev,
+                         rois.data())) != HL_NO_ERROR)
+        return rc;
+    h->last_batch = 1;
+
+    /* pool descriptors and head geometries (host), window capacity */
+    const size_t off_geo = align16(sizeof(hl_pool_img) * nimg);
+    const size_t tab = off_geo + sizeof(hl_head_geom) * nimg;
+    size_t max_bins = 1;
+    std::vector<char> force((size_t)nimg, 0);
+    if (!b->tab_event) {
+        CK(cudaEventCreateWithFlags(&b->tab_read, cudaEventDisableTiming));
+        b->tab_event = 1;
+    }
+    CK(cudaEventSynchronize(b->tab_read));   /* pw->h_tab reuse */
+    if ((rc = grow_host(&pw->h_tab, &pw->cap_htab, tab)) != HL_NO_ERROR ||
+        (rc = grow((void **)&pw->d_tab, &pw->cap_tab, tab)) != HL_NO_ERROR ||
+        (rc = grow((void **)&pw->d_occ, &pw->cap_occ,
+                   sizeof(__nv_bfloat16) * 256 * 256 * (size_t)nimg)) != HL_NO_ERROR ||
+        (rc = grow((void **)&pw->d_fb, &pw->cap_fb, sizeof(int) * nimg)) != HL_NO_ERROR ||
+        (rc = grow_host((unsigned char **)&pw->h_fb, &pw->cap_hfb, sizeof(int) * nimg)) !=
+            HL_NO_ERROR)
+        return rc;
+    if (!pw->d_cnt)
+        CK(cudaMalloc(&pw->d_cnt, 8 * sizeof(int)));
+    hl_pool_img *pi = reinterpret_cast<hl_pool_img *>(pw->h_tab);
+    hl_head_geom *hg = reinterpret_cast<hl_head_geom *>(pw->h_tab + off_geo);
+    for (int i = 0; i < nimg; i++) {
+        const int w = rois[i].w, hh = rois[i].h;
+        const int f = std::max(1, (std::max(w, hh) + 255) / 256);
+        pi[i].base = rois[i].base;
+        pi[i].pitch = rois[i].pitch;
+        pi[i].w = w;
+        pi[i].h = hh;
+        pi[i].factor = f;
+        pi[i].pad = 0;
+        hg[i].cell = (float)(4 * f);
+        hg[i].rho_min = (float)b->rho_min[i];
+        hg[i].inv_rw = (float)HL_COARSE_R / (float)b->R[i];
+        hg[i].qh = ((hh + f - 1) / f + 3) / 4;
+        hg[i].qw = ((w + f - 1) / f + 3) / 4;
+        hg[i].pad = 0;
+        const int nk = (h->T + HL_COARSE_T - 1) / HL_COARSE_T + 2;
+        const int nj = (b->R[i] + HL_COARSE_R - 1) / HL_COARSE_R + 2;
+        max_bins = std::max(max_bins, (size_t)nk * nj);
+        const int ntiles = ((w + HL_TILE_W - 1) / HL_TILE_W) * ((hh + HL_TILE_H - 1) / HL_TILE_H);
+        if (ntiles > HL_WIN_MAXTILES)
+            force[i] = 1;
+    }
+    if (max_bins * sizeof(int) > 200u * 1024u)
+        return HL_OP_OVERFLOW;
+    const int cap_win = nimg * std::max(1, opts->max_props) * (2 * opts->dilate_rho + 1) *
+                        (2 * opts->dilate_theta + 1);
+    if ((rc = grow((void **)&pw->d_win, &pw->cap_win, sizeof(int4) * (size_t)cap_win)) !=
+        HL_NO_ERROR)
+        return rc;
+
+    /* device work: compaction, pooling, network, selection, windows, finalize */
+    unsigned char *dt = b->d_tab;
+    CK(cudaMemsetAsync(pw->d_cnt, 0, 8 * sizeof(int), s));
+    CK(cudaMemcpyAsync(pw->d_tab, pw->h_tab, tab, cudaMemcpyHostToDevice, s));
+    if ((rc = batch_enqueue_compact(h, b, nimg, s)) != HL_NO_ERROR)
+        return rc;
+    CK(hl_launch_pool(reinterpret_cast<const hl_pool_img *>(pw->d_tab), nimg, 256, pw->d_occ, s));
+    const float *logits = nullptr;
+    if ((rc = hl_net_run(net, pw->d_occ,
+                         reinterpret_cast<const hl_head_geom *>(pw->d_tab + off_geo), nimg,
+                         &logits, s)) != HL_NO_ERROR)
+        return rc;
+    hl_select_args sa;
+    memset(&sa, 0, sizeof(sa));
+    sa.logits = logits;
+    sa.zcut = logf(opts->p_cut / (1.0f - opts->p_cut));
+    sa.max_props = opts->max_props;
+    sa.dil_t = opts->dilate_theta;
+    sa.dil_r = opts->dilate_rho;
+    sa.force_fallback = 0;
+    sa.fallback = pw->d_fb;
+    sa.win = pw->d_win;
+    sa.nwin = pw->d_cnt + 0;
+    sa.cap = cap_win;
+    sa.status = pw->d_cnt + 1;
+    CK(hl_launch_select(&sa, nimg, s));
+    hl_window_args wa;
+    memset(&wa, 0, sizeof(wa));
+    wa.win = pw->d_win;
+    wa.nwin = pw->d_cnt + 0;
+    wa.cap = cap_win;
+    wa.vimgs = reinterpret_cast<const hl_vote_img *>(dt + b->off_vimg);
+    wa.pimgs = reinterpret_cast<const hl_peak_img *>(dt + b->off_pimg);
+    wa.cosv = h->d_cos;
+    wa.sinv = h->d_sin;
+    wa.T = h->T;
+    wa.irho = (float)(1.0 / h->p.derho);
+    wa.votes = stats ? reinterpret_cast<unsigned long long *>(pw->d_cnt + 2) : nullptr;
+    wa.status = pw->d_cnt + 1;
+    CK(hl_launch_window_vote(&wa, (int)max_bins, std::max(1, h->sms) * 6, s));
+    if ((rc = batch_enqueue_finalize(h, b, nimg, K, s)) != HL_NO_ERROR)
+        return rc;
+    CK(cudaEventRecord(b->tab_read, s));
+
+    /* fall-back and judged images run the plain method */
+    int st_host[4] = {0, 0, 0, 0};
+    CK(cudaMemcpyAsync(pw->h_fb, pw->d_fb, sizeof(int) * nimg, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(st_host, pw->d_cnt, sizeof(st_host), cudaMemcpyDeviceToHost, s));
+    int nst = 0;
+    if ((rc = hl_net_status(net, &nst, s)) != HL_NO_ERROR)
+        return rc;
+    CK(cudaStreamSynchronize(s));
+    if (st_host[1] != 0 || nst != 0)
+        return HL_CUDA_ERROR;
+    std::vector<int> sub, sub_fb;    /* images to run plain; is it a fall-back */
+    for (int i = 0; i < nimg; i++) {
+        const bool fb = pw->h_fb[i] != 0 || force[i];
+        const bool judge = !fb && opts->judge_every > 0 && i % opts->judge_every == 0;
+        if (fb || judge) {
+            sub.push_back(i);
+            sub_fb.push_back(fb ? 1 : 0);
+        }
+    }
+    int n_fb = 0, judged = 0, jl = 0, jf = 0;
+    if (!sub.empty()) {
+        const int ns = (int)sub.size();
+        std::vector<hl_image_desc> sd((size_t)ns);
+        std::vector<int> sthr((size_t)ns);
+        for (int q = 0; q < ns; q++) {
+            sd[q] = imgs[sub[q]];
+            sthr[q] = thresholds ? thresholds[sub[q]] : h->p.threshold;
+        }
+        const size_t KK = (size_t)std::max(K, 1);
+        if ((rc = grow((void **)&pw->d_fb_lines, &pw->cap_fb_lines,
+                       sizeof(hl_line) * KK * ns)) != HL_NO_ERROR ||
+            (rc = grow((void **)&pw->d_fb_counts, &pw->cap_fb_counts, sizeof(int) * ns)) !=
+                HL_NO_ERROR ||
+            (rc = grow((void **)&pw->d_map, &pw->cap_map, sizeof(int) * ns)) != HL_NO_ERROR)
+            return rc;
+        if ((rc = batch_run_ws(h, &h->bw_fb, sd.data(), ns, sthr.data(), K, pw->d_fb_lines,
+                               pw->d_fb_counts, s)) != HL_NO_ERROR)
+            return rc;
+        h->last_batch = 1;
+        std::vector<int> map((size_t)ns, -1);
+        for (int q = 0; q < ns; q++)
+            if (sub_fb[q]) {
+                map[q] = sub[q];
+                n_fb++;
+            }
+        CK(cudaMemcpyAsync(pw->d_map, map.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s));
+        if (n_fb > 0) {
+            hl_scatter_results_kernel<<<std::min(ns, 1024), 128, 0, s>>>(
+                pw->d_fb_lines, pw->d_fb_counts, pw->d_map, ns, K, lines_dev, counts_dev);
+            CK(cudaGetLastError());
+        }
+        int fst = 0;
+        CK(cudaMemcpyAsync(&fst, h->bw_fb->d_cnt + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+        /* recall of the judged images: plain lines found by the proposals */
+        std::vector<hl_line> pl, pp;
+        std::vector<int> pc, qc;
+        const int nj = ns - n_fb;
+        if (nj > 0 && K > 0) {
+            pl.resize(KK * ns);
+            pc.resize(ns);
+            pp.resize(KK * nimg);
+            qc.resize(nimg);
+            CK(cudaMemcpyAsync(pl.data(), pw->d_fb_lines, sizeof(hl_line) * KK * ns,
+                               cudaMemcpyDeviceToHost, s));
+            CK(cudaMemcpyAsync(pc.data(), pw->d_fb_counts, sizeof(int) * ns,
+                               cudaMemcpyDeviceToHost, s));
+            for (int q = 0; q < ns; q++) {
+                if (sub_fb[q])
+                    continue;
+                const int i = sub[q];
+                CK(cudaMemcpyAsync(pp.data() + KK * i, lines_dev + (size_t)i * K,
+                                   sizeof(hl_line) * K, cudaMemcpyDeviceToHost, s));
+                CK(cudaMemcpyAsync(qc.data() + i, counts_dev + i, sizeof(int),
+                                   cudaMemcpyDeviceToHost, s));
+            }
+        }
+        CK(cudaStreamSynchronize(s));
+        if (fst != 0)
+            return HL_CUDA_ERROR;
+        if (nj > 0 && K > 0) {
+            for (int q = 0; q < ns; q++) {
+                if (sub_fb[q])
+                    continue;
+                const int i = sub[q];
+                judged++;
+                const int np = std::min(pc[q], K), nq = std::min(qc[i], K);
+                jl += np;
+                for (int a = 0; a < np; a++) {
+                    const hl_line &L = pl[KK * q + a];
+                    for (int c = 0; c < nq; c++) {
+                        const hl_line &M = pp[KK * i + c];
+                        if (M.angle == L.angle && M.distance == L.distance &&
+                            M.votes == L.votes) {
+                            jf++;
+                            break;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    if (stats) {
+        stats->fallback = n_fb;
+        stats->windows = std::min(st_host[0], cap_win);
+        stats->judged = judged;
+        stats->judged_lines = jl;
+        stats->judged_found = jf;
+        unsigned long long v = 0;
+        memcpy(&v, &st_host[2], sizeof(v));
+        stats->votes = (long long)v;
+    }
     return HL_NO_ERROR;
 }

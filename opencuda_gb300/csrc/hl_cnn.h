@@ -86,4 +86,13 @@ cudaError_t hl_launch_f32_to_bf16(const float *in, long long n, __nv_bfloat16 *o
 cudaError_t hl_launch_weight_layout(const float *w, int cout, int cin, int mode,
                                     __nv_bfloat16 *out, cudaStream_t s);
 
+struct hl_net;
+/* the network's forward pass on device-resident geometry (hl_proposal.cpp);
+ * *logits points into the network's own buffer */
+int hl_net_run(struct hl_net *n, const __nv_bfloat16 *occ,
+               const hl_head_geom *geo_dev, int B, const float **logits,
+               cudaStream_t s);
+/* stream-ordered copy of the network's status word into *st (pinned) */
+int hl_net_status(struct hl_net *n, int *st, cudaStream_t s);
+
 #endif

@@ -540,3 +540,24 @@ extern "C" int hl_occupancy(hl_handle *h, const hl_image_desc *imgs, int nimg,
         e = cudaStreamSynchronize(s);
     return cnn_err(e);
 }
+
+/* Forward pass for the proposal pipeline: geometry already on the device. */
+int hl_net_run(hl_net *n, const __nv_bfloat16 *occ, const hl_head_geom *geo_dev,
+               int B, const float **logits, cudaStream_t s)
+{
+    int rc = net_reserve(n, B);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    CKN(cudaMemcpyAsync(n->geo, geo_dev, (size_t)B * sizeof(hl_head_geom),
+                        cudaMemcpyDeviceToDevice, s));
+    if ((rc = net_forward(n, occ, B, s)) != HL_NO_ERROR)
+        return rc;
+    *logits = n->logits;
+    return HL_NO_ERROR;
+}
+
+int hl_net_status(hl_net *n, int *st, cudaStream_t s)
+{
+    CKN(cudaMemcpyAsync(st, n->status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    return HL_NO_ERROR;
+}

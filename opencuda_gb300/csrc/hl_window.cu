@@ -1,0 +1,223 @@
+/*
+ * hl_window.cu -- the exact vote of the proposal-guided path.
+ *
+ * hl_select_kernel: one CTA per image reads the network's 90 x 128 logits,
+ * keeps the cells above the cutoff (too many: the image falls back to the
+ * full method), grows them by the dilation and appends one window per kept
+ * cell.
+ *
+ * hl_window_vote_kernel: one CTA per window.  A coarse cell (t, r) owns the
+ * fine thetas k with floor(90 k / T) = t and the rho rows j with
+ * floor(128 j / R) = r; the CTA votes those bins plus a one-bin halo with
+ * the plain method's rule (okano_3_0/HoughLine.cu:86-130) from every point of
+ * the tiles that can reach them, then applies the peak rule (:168-213) to the
+ * owned bins with the halo as their neighbours (bins outside the accumulator
+ * count 0).  Counts and neighbours are exact, so a reported peak is a peak of
+ * the full accumulator with its exact vote count; windows own disjoint bins,
+ * so no peak is reported twice.  Peaks go to the image's key list in the
+ * plain path's format and the batched finalize ranks and merges them.
+ */
+#include "hl_device.cuh"
+#include "hl_internal.h"
+#include "hl_window.h"
+
+#define FULL 0xffffffffu
+
+__global__ void __launch_bounds__(512)
+hl_select_kernel(hl_select_args a)
+{
+    __shared__ unsigned mark[HL_COARSE_T * HL_COARSE_R / 32];
+    __shared__ int cnt;
+    const int b = blockIdx.x;
+    const float *z = a.logits + (size_t)b * HL_COARSE_T * HL_COARSE_R;
+    for (int i = threadIdx.x; i < HL_COARSE_T * HL_COARSE_R / 32; i += blockDim.x)
+        mark[i] = 0u;
+    if (threadIdx.x == 0)
+        cnt = 0;
+    __syncthreads();
+    int mine = 0;
+    for (int i = threadIdx.x; i < HL_COARSE_T * HL_COARSE_R; i += blockDim.x)
+        mine += z[i] > a.zcut;
+    atomicAdd(&cnt, mine);
+    __syncthreads();
+    const bool fallback = cnt > a.max_props || a.force_fallback;
+    if (threadIdx.x == 0)
+        a.fallback[b] = fallback ? 1 : 0;
+    if (fallback)
+        return;
+    for (int i = threadIdx.x; i < HL_COARSE_T * HL_COARSE_R; i += blockDim.x) {
+        if (!(z[i] > a.zcut))
+            continue;
+        const int t = i / HL_COARSE_R, r = i % HL_COARSE_R;
+        for (int dt = -a.dil_t; dt <= a.dil_t; dt++) {
+            const int tt = t + dt;
+            if (tt < 0 || tt >= HL_COARSE_T)
+                continue;
+            for (int dr = -a.dil_r; dr <= a.dil_r; dr++) {
+                const int rr = r + dr;
+                if (rr < 0 || rr >= HL_COARSE_R)
+                    continue;
+                const int c = tt * HL_COARSE_R + rr;
+                atomicOr(&mark[c >> 5], 1u << (c & 31));
+            }
+        }
+    }
+    __syncthreads();
+    for (int wd = threadIdx.x; wd < HL_COARSE_T * HL_COARSE_R / 32; wd += blockDim.x) {
+        unsigned m = mark[wd];
+        if (!m)
+            continue;
+        const int n = __popc(m);
+        const int base = atomicAdd(a.nwin, n);
+        int q = 0;
+        while (m) {
+            const int bit = __ffs(m) - 1;
+            m &= m - 1;
+            const int c = wd * 32 + bit;
+            if (base + q < a.cap)
+                a.win[base + q] = make_int4(b, c / HL_COARSE_R, c % HL_COARSE_R, 0);
+            else
+                atomicOr(a.status, HL_ST_CAND_OVERFLOW);
+            q++;
+        }
+    }
+}
+
+cudaError_t hl_launch_select(const hl_select_args *a, int nimg, cudaStream_t s)
+{
+    hl_select_kernel<<<nimg, 512, 0, s>>>(*a);
+    return cudaGetLastError();
+}
+
+/* fine range [lo, hi) of coarse index c of n coarse cells over m fine bins:
+ * the bins j with floor(n j / m) = c */
+__device__ __forceinline__ void fine_range(int c, int n, int m, int *lo, int *hi)
+{
+    *lo = (int)(((long long)c * m + n - 1) / n);
+    *hi = (int)(((long long)(c + 1) * m + n - 1) / n);
+}
+
+template <bool UNIT>
+__global__ void __launch_bounds__(256)
+hl_window_vote_kernel(hl_window_args a)
+{
+    extern __shared__ int wacc[];            /* [nk][nj] haloed window */
+    __shared__ unsigned tmask[HL_WIN_MAXTILES / 32];
+    __shared__ int4 cur;
+    const int nwin = min(*a.nwin, a.cap);
+    for (int wi = blockIdx.x; wi < nwin; wi += gridDim.x) {
+        __syncthreads();
+        if (threadIdx.x == 0)
+            cur = a.win[wi];
+        __syncthreads();
+        const int b = cur.x, t = cur.y, r = cur.z;
+        const hl_vote_img im = a.vimgs[b];
+        const hl_peak_img pk = a.pimgs[b];
+        int k_lo, k_hi, j_lo, j_hi;
+        fine_range(t, HL_COARSE_T, a.T, &k_lo, &k_hi);
+        fine_range(r, HL_COARSE_R, im.R, &j_lo, &j_hi);
+        if (k_hi <= k_lo || j_hi <= j_lo)
+            continue;
+        /* haloed ranges, clipped to the accumulator */
+        const int hk0 = max(k_lo - 1, 0), hk1 = min(k_hi + 1, a.T);
+        const int hj0 = max(j_lo - 1, 0), hj1 = min(j_hi + 1, im.R);
+        const int nk = hk1 - hk0, nj = hj1 - hj0;
+        for (int i = threadIdx.x; i < nk * nj; i += blockDim.x)
+            wacc[i] = 0;
+        /* tile filter over the image's tiles (one bit each) */
+        const float c0 = a.cosv[hk0], s0 = a.sinv[hk0];
+        const float c1 = a.cosv[hk1 - 1], s1 = a.sinv[hk1 - 1];
+        const float lo_bin = (float)(im.rho_min + hj0);
+        const float hi_bin = (float)(im.rho_min + hj1 - 1);
+        const int ntl = min(im.ntiles, HL_WIN_MAXTILES);
+        for (int base = 0; base < ntl; base += blockDim.x) {
+            const int tl = base + threadIdx.x;
+            const bool hit = tl < ntl && tile_hits(tl, im.tiles_x, im.w, im.h, c0, s0,
+                                                   c1, s1, lo_bin, hi_bin, a.irho);
+            const unsigned m = __ballot_sync(FULL, hit);
+            if ((threadIdx.x & 31) == 0 && base + threadIdx.x < HL_WIN_MAXTILES)
+                tmask[(base + threadIdx.x) >> 5] = m;
+        }
+        __syncthreads();
+        /* vote: each warp takes hit tiles in turn, its lanes the tile's points */
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        for (int wd = warp; wd < (ntl + 31) / 32; wd += blockDim.x >> 5) {
+            unsigned m = tmask[wd];
+            while (m) {
+                const int tl = wd * 32 + __ffs(m) - 1;
+                m &= m - 1;
+                const int p0 = im.tile_off[tl], p1 = im.tile_off[tl + 1];
+                for (int p = p0 + lane; p < p1; p += 32) {
+                    const float2 xy = im.pts[p];
+                    for (int k = hk0; k < hk1; k++) {
+                        const int j = rho_of<UNIT>(xy.x, xy.y, a.cosv[k], a.sinv[k],
+                                                   a.irho) - im.rho_min - hj0;
+                        if ((unsigned)j < (unsigned)nj)
+                            atomicAdd(&wacc[(k - hk0) * nj + j], 1);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        /* peaks among the owned bins */
+        const int ok = k_hi - k_lo, oj = j_hi - j_lo;
+        for (int i = threadIdx.x; i < ok * oj; i += blockDim.x) {
+            const int k = k_lo + i / oj, j = j_lo + i % oj;
+            const int lk = k - hk0, lj = j - hj0;
+            const int v = wacc[lk * nj + lj];
+            bool is = false;
+            if (v > pk.threshold) {
+                const int W = (k > 0) ? wacc[(lk - 1) * nj + lj] : 0;
+                const int E = (k + 1 < a.T) ? wacc[(lk + 1) * nj + lj] : 0;
+                const int N = (j > 0) ? wacc[lk * nj + lj - 1] : 0;
+                const int S = (j + 1 < im.R) ? wacc[lk * nj + lj + 1] : 0;
+                /* okano_3_0/HoughLine.cu:195-199 */
+                is = v > W && v >= E && v > N && v >= S;
+            }
+            if (is) {
+                const unsigned idx = (unsigned)j * (unsigned)a.T + (unsigned)k;
+                const unsigned long long key =
+                    ((unsigned long long)(unsigned)v << 32) | (unsigned)(~idx);
+                const int pos = atomicAdd(pk.ncand, 1);
+                if (pos < pk.cap)
+                    pk.keys[pos] = key;
+                else
+                    atomicOr(a.status, HL_ST_CAND_OVERFLOW);
+            }
+        }
+        if (a.votes && threadIdx.x == 0) {
+            /* executed votes: every point of every hit tile times the thetas */
+            long long n = 0;
+            for (int wd = 0; wd < (ntl + 31) / 32; wd++) {
+                unsigned m = tmask[wd];
+                while (m) {
+                    const int tl = wd * 32 + __ffs(m) - 1;
+                    m &= m - 1;
+                    n += im.tile_off[tl + 1] - im.tile_off[tl];
+                }
+            }
+            atomicAdd(a.votes, (unsigned long long)(n * nk));
+        }
+    }
+}
+
+cudaError_t hl_launch_window_vote(const hl_window_args *a, int max_win_bins, int grid,
+                                  cudaStream_t s)
+{
+    const size_t smem = sizeof(int) * (size_t)max_win_bins;
+    cudaError_t e;
+    if (a->irho == 1.0f) {
+        e = cudaFuncSetAttribute(hl_window_vote_kernel<true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess)
+            return e;
+        hl_window_vote_kernel<true><<<grid, 256, smem, s>>>(*a);
+    } else {
+        e = cudaFuncSetAttribute(hl_window_vote_kernel<false>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess)
+            return e;
+        hl_window_vote_kernel<false><<<grid, 256, smem, s>>>(*a);
+    }
+    return cudaGetLastError();
+}

@@ -1,0 +1,46 @@
+/*
+ * hl_window.h -- argument blocks of the proposal-guided vote (not part of
+ * the C ABI).
+ */
+#ifndef HL_WINDOW_H
+#define HL_WINDOW_H
+
+#include "hl_internal.h"
+
+/* coarse grid of the proposal head */
+#define HL_COARSE_T 90
+#define HL_COARSE_R 128
+/* tiles one window may filter (64 Mpixel ROIs) */
+#define HL_WIN_MAXTILES 16384
+
+typedef struct hl_select_args {
+    const float *logits;   /* [nimg][90][128] */
+    float zcut;            /* logit of the probability cutoff */
+    int max_props;         /* more cells above the cutoff: fall back */
+    int dil_t, dil_r;      /* window dilation in coarse cells */
+    int force_fallback;
+    int *fallback;         /* out [nimg] */
+    int4 *win;             /* out: {image, t, r, 0} */
+    int *nwin;             /* window counter (zeroed before) */
+    int cap;
+    int *status;
+} hl_select_args;
+
+typedef struct hl_window_args {
+    const int4 *win;
+    const int *nwin;
+    int cap;
+    const hl_vote_img *vimgs;
+    const hl_peak_img *pimgs;
+    const float *cosv, *sinv;
+    int T;
+    float irho;
+    unsigned long long *votes;   /* executed votes, or NULL */
+    int *status;
+} hl_window_args;
+
+cudaError_t hl_launch_select(const hl_select_args *a, int nimg, cudaStream_t s);
+cudaError_t hl_launch_window_vote(const hl_window_args *a, int max_win_bins,
+                                  int grid, cudaStream_t s);
+
+#endif

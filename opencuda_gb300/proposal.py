@@ -113,3 +113,40 @@ def line_targets(lines_per_image, geo) -> np.ndarray:
             ri = min(max(int(np.floor((d - g.rho_min) * g.inv_rw)), 0), HEAD_R - 1)
             t[i, ti, ri] = 1.0
     return t
+
+
+def proposal_batch(hl, net: HoughNet, images, linesmax: int, thresholds=None,
+                   p_cut: float = 0.5, max_props: int = 96, dilate_theta: int = 0,
+                   dilate_rho: int = 1, judge_every: int = 0, stream=None):
+    """hl_proposal_batch over a list of device Images: (rc, [[LineParam]],
+    stats dict)."""
+    import torch
+    from .houghline import LineParam
+    n = len(images)
+    descs = (_lib.hl_image_desc * n)(*[im.desc() for im in images])
+    K = max(linesmax, 0)
+    lines = torch.zeros(max(n * K * 3, 1), dtype=torch.int32, device="cuda")
+    counts = torch.zeros(n, dtype=torch.int32, device="cuda")
+    thr = None
+    if thresholds is not None:
+        thr = (C.c_int * n)(*[int(t) for t in thresholds])
+    opts = _lib.hl_proposal_opts(p_cut, max_props, dilate_theta, dilate_rho, judge_every)
+    st = _lib.hl_proposal_stats()
+    L = _lib.load()
+    rc = L.hl_proposal_batch(hl.handle, net.handle, descs, n, thr, linesmax, C.byref(opts),
+                             C.c_void_p(lines.data_ptr()), C.c_void_p(counts.data_ptr()),
+                             C.byref(st), hl._stream(stream))
+    if rc != 0:
+        return rc, [], {}
+    raw = lines.cpu().numpy()[: n * K * 3].reshape(n, K, 3) if K else None
+    cnt = counts.cpu().numpy()
+    res = []
+    for i in range(n):
+        out = []
+        for j in range(int(cnt[i])):
+            a = float(np.array([raw[i, j, 0]], np.int32).view(np.float32)[0])
+            out.append(LineParam(a, int(raw[i, j, 1]), int(raw[i, j, 2])))
+        res.append(out)
+    stats = {k: getattr(st, k) for k in ("fallback", "windows", "judged", "judged_lines",
+                                         "judged_found", "votes")}
+    return rc, res, stats
