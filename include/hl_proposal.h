@@ -87,7 +87,8 @@ int hl_occupancy(hl_handle *h, const hl_image_desc *imgs, int nimg,
  * hl_batch's contract (DEVICE images, per-image thresholds, linesmax lines
  * per image into DEVICE arrays), but the exact vote runs only in the coarse
  * cells the network scores above p_cut (grown by dilate_theta / dilate_rho
- * cells): every reported line is a peak of the full accumulator with its
+ * cells; with top_m > 0 also in the image's top_m cells whatever their
+ * score): every reported line is a peak of the full accumulator with its
  * exact vote count; lines the proposals miss are absent.  An image with more
  * than max_props cells above the cutoff (a cluttered scene), or too large
  * for the window kernel, runs the full plain method instead.  Every
@@ -100,6 +101,7 @@ typedef struct hl_proposal_opts {
     int dilate_theta;
     int dilate_rho;
     int judge_every;
+    int top_m;          /* also vote each image's top_m cells (0: none) */
 } hl_proposal_opts;
 
 typedef struct hl_proposal_stats {

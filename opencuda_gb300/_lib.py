@@ -67,7 +67,7 @@ class hl_coarse_geom(C.Structure):
 
 class hl_proposal_opts(C.Structure):
     _fields_ = [("p_cut", C.c_float), ("max_props", C.c_int), ("dilate_theta", C.c_int),
-                ("dilate_rho", C.c_int), ("judge_every", C.c_int)]
+                ("dilate_rho", C.c_int), ("judge_every", C.c_int), ("top_m", C.c_int)]
 
 
 class hl_proposal_stats(C.Structure):

@@ -1841,7 +1841,7 @@ extern "C" int hl_proposal_batch(hl_handle *h, hl_net *net,
         return HL_NULL_POINTER;
     if (nimg <= 0 || nimg > 0xffff || !(opts->p_cut > 0.0f && opts->p_cut < 1.0f) ||
         opts->max_props < 0 || opts->dilate_rho < 0 || opts->dilate_theta < 0 ||
-        opts->judge_every < 0)
+        opts->judge_every < 0 || opts->top_m < 0 || opts->top_m > 1024)
         return HL_INVALID_DATA;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     const int K = std::max(linesmax, 0);
@@ -1913,8 +1913,8 @@ extern "C" int hl_proposal_batch(hl_handle *h, hl_net *net,
     }
     if (max_bins * sizeof(int) > 200u * 1024u)
         return HL_OP_OVERFLOW;
-    const int cap_win = nimg * std::max(1, opts->max_props) * (2 * opts->dilate_rho + 1) *
-                        (2 * opts->dilate_theta + 1);
+    const int cap_win = nimg * (std::max(1, opts->max_props) + std::max(0, opts->top_m) + 64) *
+                        (2 * opts->dilate_rho + 1) * (2 * opts->dilate_theta + 1);
     if ((rc = grow((void **)&pw->d_win, &pw->cap_win, sizeof(int4) * (size_t)cap_win)) !=
         HL_NO_ERROR)
         return rc;
@@ -1936,6 +1936,7 @@ extern "C" int hl_proposal_batch(hl_handle *h, hl_net *net,
     sa.logits = logits;
     sa.zcut = logf(opts->p_cut / (1.0f - opts->p_cut));
     sa.max_props = opts->max_props;
+    sa.top_m = opts->top_m;
     sa.dil_t = opts->dilate_theta;
     sa.dil_r = opts->dilate_rho;
     sa.force_fallback = 0;

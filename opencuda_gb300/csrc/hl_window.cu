@@ -45,8 +45,52 @@ hl_select_kernel(hl_select_args a)
         a.fallback[b] = fallback ? 1 : 0;
     if (fallback)
         return;
+    /* selection level: the cutoff, lowered to about the image's top_m-th
+     * logit (bisection on the value keeps count(z > lo) >= top_m) */
+    float level = a.zcut;
+    if (a.top_m > 0) {
+        __shared__ float red[2][16];
+        __shared__ int s_cnt;
+        float mn = 3.0e38f, mx = -3.0e38f;
+        for (int i = threadIdx.x; i < HL_COARSE_T * HL_COARSE_R; i += blockDim.x) {
+            mn = fminf(mn, z[i]);
+            mx = fmaxf(mx, z[i]);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            mn = fminf(mn, __shfl_xor_sync(FULL, mn, o));
+            mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, o));
+        }
+        if ((threadIdx.x & 31) == 0) {
+            red[0][threadIdx.x >> 5] = mn;
+            red[1][threadIdx.x >> 5] = mx;
+        }
+        __syncthreads();
+        float lo = red[0][0], hi = red[1][0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+            lo = fminf(lo, red[0][w]);
+            hi = fmaxf(hi, red[1][w]);
+        }
+        lo -= 1.0f;   /* count(z > lo) = all cells >= top_m */
+        for (int it = 0; it < 24; it++) {
+            const float mid = 0.5f * (lo + hi);
+            __syncthreads();
+            if (threadIdx.x == 0)
+                s_cnt = 0;
+            __syncthreads();
+            int c = 0;
+            for (int i = threadIdx.x; i < HL_COARSE_T * HL_COARSE_R; i += blockDim.x)
+                c += z[i] > mid;
+            atomicAdd(&s_cnt, c);
+            __syncthreads();
+            if (s_cnt >= a.top_m)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        level = fminf(level, lo);
+    }
     for (int i = threadIdx.x; i < HL_COARSE_T * HL_COARSE_R; i += blockDim.x) {
-        if (!(z[i] > a.zcut))
+        if (!(z[i] > level))
             continue;
         const int t = i / HL_COARSE_R, r = i % HL_COARSE_R;
         for (int dt = -a.dil_t; dt <= a.dil_t; dt++) {

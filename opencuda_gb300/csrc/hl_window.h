@@ -17,6 +17,7 @@ typedef struct hl_select_args {
     const float *logits;   /* [nimg][90][128] */
     float zcut;            /* logit of the probability cutoff */
     int max_props;         /* more cells above the cutoff: fall back */
+    int top_m;             /* also take each image's top_m cells (0: none) */
     int dil_t, dil_r;      /* window dilation in coarse cells */
     int force_fallback;
     int *fallback;         /* out [nimg] */

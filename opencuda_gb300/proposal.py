@@ -117,7 +117,8 @@ def line_targets(lines_per_image, geo) -> np.ndarray:
 
 def proposal_batch(hl, net: HoughNet, images, linesmax: int, thresholds=None,
                    p_cut: float = 0.5, max_props: int = 96, dilate_theta: int = 0,
-                   dilate_rho: int = 1, judge_every: int = 0, stream=None):
+                   dilate_rho: int = 1, judge_every: int = 0, top_m: int = 0,
+                   stream=None):
     """hl_proposal_batch over a list of device Images: (rc, [[LineParam]],
     stats dict)."""
     import torch
@@ -130,7 +131,8 @@ def proposal_batch(hl, net: HoughNet, images, linesmax: int, thresholds=None,
     thr = None
     if thresholds is not None:
         thr = (C.c_int * n)(*[int(t) for t in thresholds])
-    opts = _lib.hl_proposal_opts(p_cut, max_props, dilate_theta, dilate_rho, judge_every)
+    opts = _lib.hl_proposal_opts(p_cut, max_props, dilate_theta, dilate_rho, judge_every,
+                                 top_m)
     st = _lib.hl_proposal_stats()
     L = _lib.load()
     rc = L.hl_proposal_batch(hl.handle, net.handle, descs, n, thr, linesmax, C.byref(opts),
