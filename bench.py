@@ -200,6 +200,94 @@ def batched_workload(L, HoughLine, Image, dev, sp, reps: int):
             "vote_shape": {"window_rows": best[0], "threads": best[1]}}
 
 
+def gpu_scenes(L, Image, dev, kind: int, n: int, seed: int):
+    """n seeded scenes of a workload spec generated on the GPU (the same
+    bytes as the host generator), each in its own pitched buffer."""
+    import torch
+    _lib = _lib_mod()
+    ps = (_lib.hl_scene_params * n)()
+    _lib.check(L.hl_synth_spec(kind, seed, n, ps), "hl_synth_spec")
+    imgs, descs = [], (_lib.hl_image_desc * n)()
+    for i in range(n):
+        w, h = ps[i].width, ps[i].height
+        pitch = (w + 511) // 512 * 512
+        buf = torch.empty((h, pitch), dtype=torch.uint8, device=dev)
+        descs[i] = _lib.hl_image_desc(buf.data_ptr(), pitch, w, h, 0, 0, w, h)
+        im = Image(buf[:, :w])
+        im._buf = buf
+        imgs.append(im)
+    _lib.check(L.hl_synth_scenes_device(ps, n, descs, None), "hl_synth_scenes_device")
+    return imgs
+
+
+def proposal_workload(L, HoughLine, Image, dev, sp, kind: int, n: int, reps: int):
+    """Proposal-guided batched HoughLine against the plain batched path on
+    the same images: spec 4 = 2048 x 2048 scenes (8-48 segments, 1-4% noise),
+    spec 5 = uneven 512-4096 scenes, 30% cluttered (fall back to plain).
+    Theta step 0.5 deg, threshold 0.15 * max(w, h), top-32.  Both timed with
+    CUDA events around whole batch calls (the proposal call synchronises
+    once to decide its fall-back set); recall = plain top-32 lines the
+    proposal path also reports, over all images."""
+    import torch
+    from opencuda_gb300.proposal import WEIGHTS, HoughNet, proposal_batch
+    K, det = 32, math.pi / 360
+    imgs = gpu_scenes(L, Image, dev, kind, n, 4321 + kind)
+    thr = [int(0.15 * max(im.width, im.height)) for im in imgs]
+    hl = HoughLine(detheta=det)
+    hl.set_batch_graph(True)
+    net = HoughNet()
+    net.load(WEIGHTS)
+    _lib = _lib_mod()
+    descs = (_lib.hl_image_desc * n)(*[d.desc() for d in imgs])
+    th = (C.c_int * n)(*thr)
+    lines = torch.empty(n * K * 3, dtype=torch.int32, device=dev)
+    counts = torch.zeros(n, dtype=torch.int32, device=dev)
+    opts = dict(p_cut=0.9, max_props=400, dilate_theta=1, dilate_rho=1, top_m=64)
+
+    def plain():
+        rc = L.hl_batch_async(hl.handle, descs, n, th, K, C.c_void_p(lines.data_ptr()),
+                              C.c_void_p(counts.data_ptr()), sp)
+        if rc != 0:
+            raise RuntimeError(f"hl_batch_async returned {rc}")
+
+    def prop():
+        rc, _, st = proposal_batch(hl, net, imgs, K, thr, stream=sp, **opts)
+        if rc != 0:
+            raise RuntimeError(f"hl_proposal_batch returned {rc}")
+        return st
+
+    def timed(f):
+        for _ in range(2):
+            f()
+        torch.cuda.synchronize(dev)
+        ms = []
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            f()
+            e1.record()
+            torch.cuda.synchronize(dev)
+            ms.append(e0.elapsed_time(e1))
+        return statistics.median(ms)
+    t_plain = timed(plain)
+    t_prop = timed(prop)
+    rc, _, st = proposal_batch(hl, net, imgs, K, thr, stream=sp, judge_every=1, **opts)
+    if rc != 0:
+        raise RuntimeError(f"hl_proposal_batch returned {rc}")
+    return {"workload": ("proposal-guided vs plain batched HoughLine: "
+                         + ("2048x2048 scenes, 8-48 segments, 1-4% noise" if kind == 4 else
+                            "uneven 512-4096 scenes, 30% cluttered")
+                         + f", {n} images, T=360, thr 0.15*max(w,h), top-32"),
+            "images": n, "plain_images_per_s": n / (t_plain / 1e3),
+            "proposal_images_per_s": n / (t_prop / 1e3),
+            "speedup": t_plain / t_prop,
+            "recall_top32": st["judged_found"] / max(st["judged_lines"], 1),
+            "fallback_rate": st["fallback"] / n, "windows_per_image": st["windows"] / n,
+            "executed_votes_per_image": st["votes"] / n, "selection": opts,
+            "network": "6 conv3x3 (tcgen05), 32 ch, trained on 64K GPU-generated scenes"}
+
+
 def _lib_mod():
     from opencuda_gb300 import _lib
     return _lib
@@ -385,6 +473,9 @@ def run_gb300(args):
     }
     if not args.no_batch:
         line["batched"] = batched_workload(L, HoughLine, Image, dev, sp, min(max(args.steps, 5), 50))
+    if not args.no_batch and not args.no_proposal:
+        line["proposal"] = [proposal_workload(L, HoughLine, Image, dev, sp, 4, 128, 5),
+                            proposal_workload(L, HoughLine, Image, dev, sp, 5, 1024, 3)]
     if ws == 1 and not args.no_cpu_baseline:
         n, el, v, cores = cpu_reference_images(imgs_host, args.cpu_budget)
         line["cpu_baseline"] = {"value": n / el, "unit": "images/s", "cores": cores,
@@ -410,6 +501,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the batched (256 uneven images) measurement")
+    ap.add_argument("--no-proposal", action="store_true",
+                    help="skip the proposal-guided measurements")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
