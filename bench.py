@@ -55,6 +55,20 @@ def dist_env():
     return ws, rank, local
 
 
+def reduce_over_ranks(times, votes: float, ws: int, device):
+    """Timings: the slowest rank's (max); votes: the whole job's (sum)."""
+    import torch
+    t = torch.tensor(list(times) + [votes], dtype=torch.float64, device=device)
+    if ws > 1:
+        import torch.distributed as dist
+        tt = t[:-1].clone()
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        vt = t[-1:].clone()
+        dist.all_reduce(vt, op=dist.ReduceOp.SUM)
+        t = torch.cat([tt, vt])
+    return tuple(float(x) for x in t.tolist())
+
+
 def make_images(rank: int, n: int):
     import cases
     return [cases.synth(2, 1234 + 1000 * rank + i, 0) for i in range(n)]
@@ -417,14 +431,8 @@ def run_gb300(args):
     torch.cuda.synchronize(dev)
     e2e_ms = sum(a.elapsed_time(b) for a, b in e2e_ev)
 
-    # max over ranks
-    t = torch.tensor([dev_ms, e2e_ms, stage[1], float(votes)], dtype=torch.float64, device=dev)
-    if ws > 1:
-        torch.distributed.all_reduce(t[:3], op=torch.distributed.ReduceOp.MAX)
-        vt = t[3:].clone()
-        torch.distributed.all_reduce(vt, op=torch.distributed.ReduceOp.SUM)
-        t[3] = vt[0]
-    dev_ms, e2e_ms, vote_ms, votes_all = (float(x) for x in t.tolist())
+    dev_ms, e2e_ms, vote_ms, votes_all = reduce_over_ranks(
+        [dev_ms, e2e_ms, stage[1]], float(votes), ws, dev)
     if rank != 0:
         if ws > 1:
             torch.distributed.destroy_process_group()
