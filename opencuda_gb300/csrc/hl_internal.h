@@ -128,7 +128,7 @@ typedef struct hl_peak_img {
 } hl_peak_img;
 
 /* rows of an accumulator one peak-pass chunk covers */
-#define HL_PEAK_ROWS 8
+#define HL_PEAK_ROWS 16
 
 typedef struct hl_peak_args {
     const hl_peak_img *imgs;  /* per image, or NULL: the one image img0 */

@@ -144,6 +144,68 @@ __device__ int lookback(unsigned long long *state, int tile, int total,
     return excl;
 }
 
+/* Groups a launch may have for the all-predecessor prefix (below). */
+#define LB_FULL_MAX 2048
+
+/* Exclusive prefix of group g as the plain sum of every predecessor's own
+ * count (all threads of the CTA call it; each group publishes only its count,
+ * flag AGG, and never an inclusive prefix).  With every group of a launch
+ * resident at once -- a 4096 x 4096 image has 1024 groups -- the chained
+ * look-back forwards inclusive prefixes only 32 groups per memory round
+ * trip; here a group waits just for its slowest predecessor to publish, and
+ * 256 threads read up to 1024 predecessors in one round trip.  Waits are
+ * bounded as in lookback(). */
+__device__ int prefix_all(const unsigned long long *state, int g, unsigned epoch,
+                          int *status, int *s_red)
+{
+    const int tid = threadIdx.x;
+    int spins = 0;
+    while (true) {
+        int sum = 0;
+        bool bad = false;
+        for (int j0 = 0; j0 < g; j0 += 4 * HL_COMPACT_THREADS) {
+            unsigned long long st[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int j = j0 + u * HL_COMPACT_THREADS + tid;
+                st[u] = (j < g) ? lb_load(&state[j]) : 0ull;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int j = j0 + u * HL_COMPACT_THREADS + tid;
+                if (j < g) {
+                    if ((unsigned)(st[u] >> 34) != epoch || ((st[u] >> 32) & 3u) == 0u)
+                        bad = true;
+                    else
+                        sum += (int)(unsigned)(st[u] & 0xffffffffu);
+                }
+            }
+        }
+        if (!__syncthreads_or(bad)) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                sum += __shfl_xor_sync(FULL, sum, o);
+            if ((tid & 31) == 0)
+                s_red[tid >> 5] = sum;
+            __syncthreads();
+            int t = 0;
+            for (int w = 0; w < HL_COMPACT_THREADS / 32; w++)
+                t += s_red[w];
+            __syncthreads();
+            return t;
+        }
+        bool quit = ++spins > LB_SPIN_LIMIT;
+        if (!quit && (spins & 255) == 0)
+            quit = (*(volatile int *)status & HL_ST_LOOKBACK_TIMEOUT) != 0;
+        if (__syncthreads_or(quit)) {
+            if (tid == 0)
+                atomicOr(status, HL_ST_LOOKBACK_TIMEOUT);
+            return 0;
+        }
+        __nanosleep(64);
+    }
+}
+
 /* Tiles per CTA: one look-back and four 16-byte loads in flight per thread
  * for every 16 KB of image. */
 #define CT_GROUP HL_COMPACT_GROUP
@@ -156,6 +218,9 @@ hl_compact_kernel(hl_compact_args a)
     __shared__ unsigned long long s_wsum[HL_COMPACT_THREADS / 32];
     __shared__ int s_tbase[CT_GROUP];
     __shared__ int s_tcnt[CT_GROUP];
+    __shared__ unsigned long long s_tot4;
+    __shared__ int s_excl;
+    __shared__ int s_red[HL_COMPACT_THREADS / 32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int ngroups = a.imgs ? a.ngroups : (a.ntiles + CT_GROUP - 1) / CT_GROUP;
 
@@ -253,9 +318,28 @@ hl_compact_kernel(hl_compact_args a)
             const int cq = (int)((tot4 >> (16 * q)) & 0xffffu);
             total += cq + (cq & pad);
         }
-        const int excl = lookback(a.tile_state, ggrp, total, a.epoch, a.status);
-        if (lane == 0) {
-            int run = excl;
+        if (ngroups > LB_FULL_MAX) {
+            const int excl = lookback(a.tile_state, ggrp, total, a.epoch, a.status);
+            if (lane == 0)
+                s_excl = excl;
+        } else if (lane == 0) {
+            lb_store(&a.tile_state[ggrp], lb_pack(a.epoch, LB_AGG, (unsigned)total));
+        }
+        if (lane == 0)
+            s_tot4 = tot4;
+    }
+    __syncthreads();
+    if (ngroups <= LB_FULL_MAX) {
+        const int excl = prefix_all(a.tile_state, ggrp, a.epoch, a.status, s_red);
+        if (tid == 0)
+            s_excl = excl;
+        __syncthreads();
+    }
+    {
+        const int pad = a.pts_f2 ? 1 : 0;
+        const unsigned long long tot4 = s_tot4;
+        if (tid == 0) {
+            int run = s_excl;
 #pragma unroll
             for (int q = 0; q < CT_GROUP; q++) {
                 const int tile = grp * CT_GROUP + q;
