@@ -215,19 +215,21 @@ hl_conv3x3_kernel(hl_conv_args a)
 
     for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
         /* A operand: row m = output pixel tile * 128 + m */
-        for (int e = tid; e < CNN_TILE_M * KG; e += CNN_THREADS) {
-            const int m = e / KG, q = e % KG;
-            const int p = tile * CNN_TILE_M + m;
-            uint4 val = make_uint4(0u, 0u, 0u, 0u);
-            if (p < a.B * HWo) {
-                const int bimg = p / HWo, r = p % HWo;
-                const int oy = r / a.Wo, ox = r % a.Wo;
-                if (CIN == 32) {
+        if (CIN == 32) {
+            /* one 16-byte cp.async per (row, K group): every copy of the
+             * tile in flight at once, zero-filled outside the image */
+            for (int e = tid; e < CNN_TILE_M * KG; e += CNN_THREADS) {
+                const int m = e / KG, q = e % KG;
+                const int p = tile * CNN_TILE_M + m;
+                bool ok = false;
+                const __nv_bfloat16 *src = a.x;
+                if (p < a.B * HWo) {
+                    const int bimg = p / HWo, r = p % HWo;
+                    const int oy = r / a.Wo, ox = r % a.Wo;
                     /* K group q = tap q / 4, channels (q % 4) * 8 .. +7 */
                     const int tap = q >> 2, c0 = (q & 3) * 8;
                     const int ky = tap / 3, kx = tap % 3;
                     int iy, ix;
-                    bool ok;
                     if (MODE == GATHER_CONV) {
                         iy = oy * a.stride - 1 + ky;
                         ix = ox * a.stride - 1 + kx;
@@ -240,9 +242,22 @@ hl_conv3x3_kernel(hl_conv_args a)
                              iy < a.H && ix < a.W;
                     }
                     if (ok)
-                        val = *reinterpret_cast<const uint4 *>(
-                            a.x + (((size_t)bimg * a.H + iy) * a.W + ix) * 32 + c0);
-                } else {
+                        src = a.x + (((size_t)bimg * a.H + iy) * a.W + ix) * 32 + c0;
+                }
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
+                             ::"r"(cnn_smem_u32(&sm.a[m >> 3][q][(m & 7) * 16])),
+                             "l"(src), "r"(ok ? 16 : 0)
+                             : "memory");
+            }
+            asm volatile("cp.async.wait_all;" ::: "memory");
+        } else {
+            for (int e = tid; e < CNN_TILE_M * KG; e += CNN_THREADS) {
+                const int m = e / KG, q = e % KG;
+                const int p = tile * CNN_TILE_M + m;
+                uint4 val = make_uint4(0u, 0u, 0u, 0u);
+                if (p < a.B * HWo) {
+                    const int bimg = p / HWo, r = p % HWo;
+                    const int oy = r / a.Wo, ox = r % a.Wo;
                     /* CIN = 1: k = tap, 9 taps then zeros */
                     __nv_bfloat16 v8[8];
 #pragma unroll
@@ -260,8 +275,8 @@ hl_conv3x3_kernel(hl_conv_args a)
                     }
                     val = *reinterpret_cast<const uint4 *>(v8);
                 }
+                *reinterpret_cast<uint4 *>(&sm.a[m >> 3][q][(m & 7) * 16]) = val;
             }
-            *reinterpret_cast<uint4 *>(&sm.a[m >> 3][q][(m & 7) * 16]) = val;
         }
         /* make the generic-proxy writes visible to the tensor cores */
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -343,7 +358,9 @@ static cudaError_t launch_conv(const hl_conv_args *a, int sms, cudaStream_t s)
     if (e != cudaSuccess)
         return e;
     const int ntiles = (a->B * a->Ho * a->Wo + CNN_TILE_M - 1) / CNN_TILE_M;
-    const int grid = std::max(1, std::min(ntiles, sms * 2));
+    /* CTAs per SM: 32-channel inputs hold ~92 KB of operands (two fit);
+     * one-channel inputs ~5 KB (eight fit, 8 x 32 TMEM columns) */
+    const int grid = std::max(1, std::min(ntiles, sms * (CIN == 1 ? 8 : 2)));
     hl_conv3x3_kernel<CIN, N, MODE><<<grid, CNN_THREADS, smem, s>>>(*a);
     return cudaGetLastError();
 }
