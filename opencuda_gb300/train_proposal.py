@@ -140,7 +140,8 @@ def main(argv=None):
         np.save(args.out, net.get_params())
     settings = [(0.9, 400, 0, 1, 48), (0.9, 400, 0, 1, 64), (0.9, 400, 1, 1, 64),
                 (0.9, 400, 0, 1, 96), (0.9, 400, 1, 1, 96), (0.5, 600, 1, 1, 128)]
-    evaluate(net, args.eval, 99991, settings)
+    if args.eval > 0:
+        evaluate(net, args.eval, 99991, settings)
     return 0
 
 
