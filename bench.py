@@ -214,6 +214,48 @@ def batched_workload(L, HoughLine, Image, dev, sp, reps: int):
             "vote_shape": {"window_rows": best[0], "threads": best[1]}}
 
 
+def latency_512(L, HoughLine, Image, dev, reps: int = 300):
+    """The 512 x 512 single-image configuration (8 segments, 1% salt, theta
+    step 1 deg, threshold 100, top-16): latency-bound.  Host wall time per
+    synchronous call through the C ABI (image resident on the device, lines
+    returned to the host), for hl_plain (five launches and one copy) and for
+    the same image through hl_batch with CUDA-graph replay."""
+    import cases
+    img = cases.synth(1, 1234, 0)
+    d = Image.from_host(img, device=dev)
+    hl = HoughLine(detheta=math.pi / 180, threshold=100)
+    _lib = _lib_mod()
+    desc = d.desc()
+    lm = C.c_int()
+    out = (_lib.hl_line * 16)()
+
+    def plain():
+        lm.value = 16
+        rc = L.hl_plain(hl.handle, C.byref(desc), C.byref(lm), out, None)
+        if rc != 0:
+            raise RuntimeError(f"hl_plain returned {rc}")
+    descs = (_lib.hl_image_desc * 1)(desc)
+    cnt = (C.c_int * 1)()
+    hl.set_batch_graph(True)
+
+    def batched():
+        rc = L.hl_batch(hl.handle, descs, 1, None, 16, out, cnt, None)
+        if rc != 0:
+            raise RuntimeError(f"hl_batch returned {rc}")
+
+    def wall(f):
+        for _ in range(20):
+            f()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            f()
+        return (time.perf_counter() - t0) / reps * 1e6
+    return {"workload": "plain HoughLine 512x512, T=180, R=1449, thr 100, top-16 "
+                        "(image on the device, lines to the host, synchronous)",
+            "hl_plain_us_per_image": wall(plain),
+            "hl_batch_graph_us_per_image": wall(batched), "calls": reps}
+
+
 def gpu_scenes(L, Image, dev, kind: int, n: int, seed: int):
     """n seeded scenes of a workload spec generated on the GPU (the same
     bytes as the host generator), each in its own pitched buffer."""
@@ -479,6 +521,7 @@ def run_gb300(args):
         "clocks": ck,
         "wall_s_timed_loop": t_wall,
     }
+    line["latency_512"] = latency_512(L, HoughLine, Image, dev)
     if not args.no_batch:
         line["batched"] = batched_workload(L, HoughLine, Image, dev, sp, min(max(args.steps, 5), 50))
     if not args.no_batch and not args.no_proposal:
