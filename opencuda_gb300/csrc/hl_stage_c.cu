@@ -66,7 +66,9 @@ __global__ void __launch_bounds__(256) hl_peaks_kernel(hl_peak_args a)
         const int nrow = min(HL_PEAK_ROWS, im.R - row0);
         const int total = nrow * q4;
         const int4 *src = reinterpret_cast<const int4 *>(im.acc) + (size_t)row0 * q4;
-        /* four 16-byte loads in flight per thread, then the four checks */
+        /* four 16-byte loads in flight per thread; the common case (no
+         * value above the threshold in the warp) is 16 compares and one
+         * vote, the neighbour reads and the key append run out of line */
         for (int e0 = 0; e0 < total; e0 += 4 * blockDim.x) {
             int4 v4[4];
 #pragma unroll
@@ -74,24 +76,32 @@ __global__ void __launch_bounds__(256) hl_peaks_kernel(hl_peak_args a)
                 const int e = e0 + u * blockDim.x + threadIdx.x;
                 v4[u] = (e < total) ? __ldcs(src + e) : make_int4(0, 0, 0, 0);
             }
+            unsigned cand = 0u;
 #pragma unroll
             for (int u = 0; u < 4; u++) {
+                cand |= (unsigned)(v4[u].x > im.threshold) << (4 * u);
+                cand |= (unsigned)(v4[u].y > im.threshold) << (4 * u + 1);
+                cand |= (unsigned)(v4[u].z > im.threshold) << (4 * u + 2);
+                cand |= (unsigned)(v4[u].w > im.threshold) << (4 * u + 3);
+            }
+            if (!__any_sync(FULL, cand != 0u))
+                continue;
+#pragma unroll 1
+            for (int i = 0; i < 16; i++) {
+                const int u = i >> 2, q = i & 3;
                 const int e = e0 + u * blockDim.x + threadIdx.x;
-                const int row = row0 + ((e < total) ? e / q4 : 0);
-                const int k4 = (e < total) ? (e % q4) * 4 : 0;
-                const int vv[4] = {v4[u].x, v4[u].y, v4[u].z, v4[u].w};
-#pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const int k = k4 + q;
-                    bool is = false;
-                    unsigned long long key = 0;
-                    if (e < total && k < a.T && vv[q] > im.threshold) {
+                bool is = false;
+                unsigned long long key = 0;
+                if ((cand >> i) & 1u) {
+                    const int row = row0 + e / q4;
+                    const int k = (e % q4) * 4 + q;
+                    if (k < a.T) {
                         const int32_t *p = im.acc + (size_t)row * a.Tp + k;
+                        const int x = p[0];
                         const int W = (k > 0) ? p[-1] : 0;
                         const int E = (k + 1 < a.T) ? p[1] : 0;
                         const int N = (row > 0) ? p[-a.Tp] : 0;
                         const int S = (row + 1 < im.R) ? p[a.Tp] : 0;
-                        const int x = vv[q];
                         /* okano_3_0/HoughLine.cu:195-199 */
                         if (x > W && x >= E && x > N && x >= S) {
                             is = true;
@@ -99,8 +109,8 @@ __global__ void __launch_bounds__(256) hl_peaks_kernel(hl_peak_args a)
                             key = ((unsigned long long)(unsigned)x << 32) | (unsigned)(~idx);
                         }
                     }
-                    push_key(is, key, im, a.status);
                 }
+                push_key(is, key, im, a.status);
             }
         }
     }
