@@ -1120,6 +1120,7 @@ struct hl_batch_ws {
     int ngroups, ntiles, nitems, nchunks, grid, threads, win_rows;
     size_t npts_cap, acc_ints, nkeys;
     std::vector<size_t> acc_off, key_off;
+    std::vector<size_t> pts_base;  /* each image's first point */
     std::vector<int> key_cap_i, tile_base, group_base, nwin, rho_min, R,
         ref_numrho;
     std::vector<int> split_img;    /* images whose accumulator is added to */
@@ -1267,7 +1268,8 @@ static int batch_plan(hl_handle *h, hl_batch_ws *b, const hl_image_desc *imgs,
         b->ref_numrho.assign(nimg, 0);
         b->group_img.clear();
         b->chunks.clear();
-        size_t acc = 0, keys = 0, pts = 16;
+        size_t acc = 0, keys = 0, pts = 0;
+        b->pts_base.assign(nimg, 0);
         int tiles = 0, groups = 0;
         std::vector<double> allw;
         std::vector<int2> blocks;
@@ -1281,9 +1283,12 @@ static int batch_plan(hl_handle *h, hl_batch_ws *b, const hl_image_desc *imgs,
             b->group_base[i] = groups;
             for (int q = 0; q < ng; q++)
                 b->group_img.push_back(i);
-            tiles += nt;
+            tiles += nt + 1;   /* the image's tile offsets and its end */
             groups += ng;
-            pts += (size_t)rois[i].w * rois[i].h + (size_t)nt;
+            /* room for every pixel and one pad per tile, kept even so every
+             * image's point list starts on 16 bytes */
+            b->pts_base[i] = pts;
+            pts += ((size_t)rois[i].w * rois[i].h + (size_t)nt + 16 + 1) & ~(size_t)1;
             b->acc_off[i] = acc;
             acc += (size_t)g.numrho * h->Tp;
             /* peak-key capacity: the bound of ensure_acc, at most 2^17 */
@@ -1397,7 +1402,8 @@ static int batch_plan(hl_handle *h, hl_batch_ws *b, const hl_image_desc *imgs,
         ci[i].group_base = b->group_base[i];
         ci[i].ngroups = (nt + HL_COMPACT_GROUP - 1) / HL_COMPACT_GROUP;
         ci[i].pad = 0;
-        vi[i].pts = b->d_pts;
+        ci[i].pts_base = (long long)b->pts_base[i];
+        vi[i].pts = b->d_pts + b->pts_base[i];
         vi[i].tile_off = b->d_tile_off + b->tile_base[i];
         vi[i].ntiles = nt;
         vi[i].tiles_x = g.tiles_x;

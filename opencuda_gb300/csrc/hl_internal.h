@@ -44,14 +44,16 @@ typedef struct hl_roi {
 } hl_roi;
 
 /* One image of a batched compaction: its tiles occupy [tile_base, +ntiles)
- * of the batch's tile_off array and its 4-tile groups [group_base, +ngroups)
- * of the batch's group space; the point list and the look-back run over the
- * whole batch, so the images' points are laid end to end. */
+ * of the batch's tile_off array, its 4-tile groups [group_base, +ngroups) of
+ * the batch's group space, and its points start at pts_base of the batch's
+ * point array (room for every pixel plus one pad per tile).  Prefixes and
+ * tile offsets are per image: an image's groups wait only for each other. */
 typedef struct hl_compact_img {
     hl_roi roi;
     int tiles_x, ntiles;
     int tile_base, group_base, ngroups;
     int pad;
+    long long pts_base;
 } hl_compact_img;
 
 typedef struct hl_compact_args {

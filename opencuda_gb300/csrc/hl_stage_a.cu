@@ -236,6 +236,7 @@ hl_compact_kernel(hl_compact_args a)
             s_im.tile_base = 0;
             s_im.group_base = 0;
             s_im.ngroups = ngroups;
+            s_im.pts_base = 0;
         } else if (g >= 0 && g < ngroups) {
             s_im = a.imgs[a.group_img[g]];
         }
@@ -318,19 +319,22 @@ hl_compact_kernel(hl_compact_args a)
             const int cq = (int)((tot4 >> (16 * q)) & 0xffffu);
             total += cq + (cq & pad);
         }
-        if (ngroups > LB_FULL_MAX) {
-            const int excl = lookback(a.tile_state, ggrp, total, a.epoch, a.status);
+        /* the prefix runs over the image's own groups */
+        unsigned long long *st = a.tile_state + s_im.group_base;
+        if (s_im.ngroups > LB_FULL_MAX) {
+            const int excl = lookback(st, grp, total, a.epoch, a.status);
             if (lane == 0)
                 s_excl = excl;
         } else if (lane == 0) {
-            lb_store(&a.tile_state[ggrp], lb_pack(a.epoch, LB_AGG, (unsigned)total));
+            lb_store(&st[grp], lb_pack(a.epoch, LB_AGG, (unsigned)total));
         }
         if (lane == 0)
             s_tot4 = tot4;
     }
     __syncthreads();
-    if (ngroups <= LB_FULL_MAX) {
-        const int excl = prefix_all(a.tile_state, ggrp, a.epoch, a.status, s_red);
+    if (s_im.ngroups <= LB_FULL_MAX) {
+        const int excl = prefix_all(a.tile_state + s_im.group_base, grp, a.epoch,
+                                    a.status, s_red);
         if (tid == 0)
             s_excl = excl;
         __syncthreads();
@@ -369,9 +373,9 @@ hl_compact_kernel(hl_compact_args a)
             const int bb = __ffs(mm) - 1;
             mm &= mm - 1;
             if (a.pts_f2)
-                a.pts_f2[pos] = make_float2((float)(xq + bb), (float)yq);
+                a.pts_f2[s_im.pts_base + pos] = make_float2((float)(xq + bb), (float)yq);
             else
-                a.pts[pos] = (uint32_t)(xq + bb) | yy;
+                a.pts[s_im.pts_base + pos] = (uint32_t)(xq + bb) | yy;
             pos++;
         }
     }
@@ -379,7 +383,7 @@ hl_compact_kernel(hl_compact_args a)
     /* the sentinel (1e30, 0) never votes inside an accumulator: its rho is
      * 1e30 * cos(theta_k), and cosf of a float angle is never 0 */
     if (a.pts_f2 && tid < CT_GROUP && (s_tcnt[tid] & 1))
-        a.pts_f2[s_tbase[tid] + s_tcnt[tid]] = make_float2(1.0e30f, 0.0f);
+        a.pts_f2[s_im.pts_base + s_tbase[tid] + s_tcnt[tid]] = make_float2(1.0e30f, 0.0f);
 }
 
 cudaError_t hl_launch_compact(const hl_compact_args *a, cudaStream_t s)
