@@ -357,12 +357,13 @@ static void vote_shape(const hl_handle *h, int R, int *rows, int *nwin,
         nw = (R + std::min(h->win_rows_override, maxr) - 1) /
              std::min(h->win_rows_override, maxr);
     } else {
-        /* windows of about 1152 rows (the fastest measured at 4096 x 4096,
-         * T = 720: fewer tile-filter passes than smaller windows, and heavy
-         * blocks are split into parts anyway), unless that leaves fewer
-         * blocks than SMs: then about two blocks per SM, 256 rows at least */
+        /* windows as tall as one CTA's shared memory allows (the fastest
+         * measured at 4096 x 4096, T = 720: fewer tile-filter passes and
+         * less vote waste than smaller windows; heavy blocks are split into
+         * parts anyway), unless that leaves fewer blocks than SMs: then
+         * about two blocks per SM, 256 rows at least */
         int nmin = (R + maxr - 1) / maxr;
-        nw = std::max(nmin, (R + 1151) / 1152);
+        nw = nmin;
         if (nw * slices < std::max(h->sms, 1)) {
             int want = (2 * std::max(h->sms, 1) + slices - 1) / slices;
             int nmax = std::max(1, R / 256);

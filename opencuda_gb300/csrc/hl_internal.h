@@ -110,11 +110,11 @@ typedef struct hl_vote_args {
 /* Tiles the allocation-free compaction entry point can serve. */
 #define HL_NOALLOC_MAX_TILES 65536
 
-/* Vote-kernel staging: points per ring slot (a batch is 32 points per
+/* Vote-kernel staging: points per ring slot (a batch is 64 points per
  * consumer warp, at most 31 warps), ring slots, tiles per coarse-filter
  * group. */
-#define HL_VOTE_CHUNK 1024
-#define HL_VOTE_SLOTS 4
+#define HL_VOTE_CHUNK 2048
+#define HL_VOTE_SLOTS 3
 #define HL_VOTE_TG 4096
 /* largest rho window (rows) one CTA can hold next to its staging */
 int hl_vote_max_rows(void);

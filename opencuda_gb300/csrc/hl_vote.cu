@@ -22,11 +22,11 @@
  * because the compaction pads every tile to an even number of float2
  * entries.  The runs, laid end to end, form the item's point stream.  Then
  * the CTA splits into one producer warp and consumer warps that meet only on
- * mbarriers: a batch is 32 points per consumer warp, batch b the stream
+ * mbarriers: a batch is 64 points per consumer warp, batch b the stream
  * range [b*B, (b+1)*B); the producer's lanes each copy one run's part of it
  * into a ring of HL_VOTE_SLOTS shared-memory slots with cp.async.bulk (TMA
  * bulk copies completing on the slot's full barrier), so a slot holds its
- * batch gap-free; consumer warp i votes points [32i, 32i + 32) of the slot
+ * batch gap-free; consumer warp i votes points [64i, 64i + 64) of the slot
  * straight from shared memory and arrives on the slot's empty barrier, which
  * the producer waits on before refilling it.  No block-wide barrier
  * separates batches.
@@ -257,8 +257,8 @@ hl_vote_kernel(hl_vote_args a)
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nthr = blockDim.x, nwarps = nthr >> 5;
     const int ncons = nwarps - 1;               /* consumer warps 1..nwarps-1 */
-    /* points per batch: 32 per consumer warp (at most SLOT_CAP) */
-    const int batch = 32 * ncons;
+    /* points per batch: 64 per consumer warp (at most SLOT_CAP) */
+    const int batch = 64 * ncons;
     const int nslices = a.Tp / HL_SLICE;
 
     if (tid == 0) {
@@ -493,15 +493,20 @@ hl_vote_kernel(hl_vote_args a)
                         atomicOr(a.status, HL_ST_VOTE_TIMEOUT);
                     }
                     seq++;
-                    /* this warp's share: points [32 cw, 32 cw + 32) */
-                    const int m = min(32, total - b * batch - 32 * cw);
-                    const float2 *pts = sm.raw[slot] + 32 * cw;
-                    if (cv == CV_FLOOR)
+                    /* this warp's share: points [64 cw, 64 cw + 64), two
+                     * 32-point halves */
+                    const int m = min(64, total - b * batch - 64 * cw);
+                    const float2 *pts = sm.raw[slot] + 64 * cw;
+                    if (cv == CV_FLOOR) {
                         vote_share<UNIT, CV_FLOOR>(pts, m, c, s, a.irho, vbase, acc_l, lrows);
-                    else if (cv == CV_CEIL)
+                        vote_share<UNIT, CV_FLOOR>(pts + 32, m - 32, c, s, a.irho, vbase, acc_l, lrows);
+                    } else if (cv == CV_CEIL) {
                         vote_share<UNIT, CV_CEIL>(pts, m, c, s, a.irho, vbase, acc_l, lrows);
-                    else
+                        vote_share<UNIT, CV_CEIL>(pts + 32, m - 32, c, s, a.irho, vbase, acc_l, lrows);
+                    } else {
                         vote_share<UNIT, CV_EXACT>(pts, m, c, s, a.irho, vbase, acc_l, lrows);
+                        vote_share<UNIT, CV_EXACT>(pts + 32, m - 32, c, s, a.irho, vbase, acc_l, lrows);
+                    }
                     __syncwarp();
                     if (lane == 0)
                         mbar_arrive(&sm.empty[slot]);
