@@ -16,6 +16,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <functional>
+#include <queue>
 #include <new>
 #include <vector>
 
@@ -61,10 +63,20 @@ struct hl_handle {
 
     /* vote work items: heaviest-first order (cached per geometry) and the
      * persistent-CTA counter base */
-    int2 *order_dev;
+    int4 *order_dev;
     size_t cap_order;
     int order_w, order_h, order_rows, order_R, order_T, order_ctas;
-    int order_n, order_split;
+    int order_n, order_nmerge, order_nslots;
+    /* the split blocks (summed from their parts' scratch slots) */
+    hl_merge_region *d_merge;
+    size_t cap_merge;
+    int4 *d_scratch;
+    size_t cap_scratch;
+    /* admitted-tile masks of the cached geometry (see hl_tile_mask_kernel) */
+    unsigned *d_tmask;
+    size_t cap_tmask;
+    int masks_dirty;
+    double order_detheta;
     double order_derho;
     unsigned work_base;
 
@@ -136,6 +148,16 @@ static int grow(void **ptr, size_t *cap, size_t need_bytes)
     }
     *cap = nb;
     return HL_NO_ERROR;
+}
+
+/* grow() that raises *moved when the buffer was (re)allocated */
+static int grow_tracked(void **ptr, size_t *cap, size_t need_bytes, int *moved)
+{
+    const void *old = *ptr;
+    int rc = grow(ptr, cap, need_bytes);
+    if (rc == HL_NO_ERROR && *ptr != old)
+        *moved = 1;
+    return rc;
 }
 
 static int check_params(const hl_params *p)
@@ -217,7 +239,8 @@ extern "C" int hl_destroy(hl_handle *h)
     batch_free(h);
     void *ptrs[] = {h->d_cos, h->d_sin, h->d_pts, h->d_tile_state,
                     h->d_tile_off, h->d_acc, h->d_keys, h->d_aux,
-                    h->d_result, h->d_counters, h->order_dev};
+                    h->d_result, h->d_counters, h->order_dev,
+                    h->d_merge, h->d_scratch, h->d_tmask};
     for (void *q : ptrs)
         if (q)
             cudaFree(q);
@@ -378,85 +401,195 @@ static void vote_shape(const hl_handle *h, int R, int *rows, int *nwin,
     *threads = h->threads_override > 0 ? h->threads_override : 1024;
 }
 
-/* Work items of the vote kernel, heaviest first.  The weight of a (slice,
- * window) block is the share of the ROI whose rho at the slice's middle
- * angle falls in the window, estimated on a 64 x 64 grid of cell centres.
- * A block heavier than a third of one CTA's fair share (total / ctas) is
- * split into parts that each vote a contiguous share of the point stream
- * (at most 16 parts).  Cached per geometry; *split tells whether any block
- * was split (the accumulator must then start at zero). */
-static int vote_items(hl_handle *h, int w, int hh, int rho_min, int R,
-                      int rows, int nwin, int ctas, const int2 **dev_items,
-                      int *nitems_out, int *split)
+/* Weight of every (slice, window) block of a w x hh ROI: the area of the
+ * tiles that the vote kernel's tile filter (tile_hits) admits for it.  The
+ * kernel votes every point of an admitted tile with all 32 lanes (a last,
+ * partial slice too: its lanes past T vote into the padding), so with a
+ * uniform point density this is its work, waste included.  Per slice
+ * each tile's rho range over the slice (corners at both end angles, plus
+ * x + y when the corner's direction lies inside the slice, three bins of
+ * slack) gives the run of windows it reaches. */
+static void block_weights_tiles(const hl_handle *h, int w, int hh, int rho_min,
+                                int R, int rows, int nwin,
+                                std::vector<double> &wt)
 {
     const int slices = h->Tp / HL_SLICE;
-    const int nblocks = slices * nwin;
-    if (h->order_dev && h->order_w == w && h->order_h == hh &&
-        h->order_rows == rows && h->order_R == R && h->order_T == h->T &&
-        h->order_derho == h->p.derho && h->order_ctas == ctas) {
-        *dev_items = h->order_dev;
-        *nitems_out = h->order_n;
-        *split = h->order_split;
-        return HL_NO_ERROR;
-    }
-    std::vector<double> wt((size_t)nblocks, 0.0);
-    const int G = 64;
-    double total = 0.0;
+    const int tx_n = (w + HL_TILE_W - 1) / HL_TILE_W;
+    const int ty_n = (hh + HL_TILE_H - 1) / HL_TILE_H;
+    const double irho = 1.0 / h->p.derho;
+    wt.assign((size_t)slices * nwin, 0.0);
     for (int sl = 0; sl < slices; sl++) {
         const int k0 = sl * HL_SLICE;
-        const int k1 = std::min(k0 + HL_SLICE, h->T) - 1;
         if (k0 >= h->T)
             continue;
-        const double th = 0.5 * (k0 + k1) * h->p.detheta;
-        const double c = cos(th), s = sin(th);
-        for (int gy = 0; gy < G; gy++) {
-            const double y = (gy + 0.5) * hh / G;
-            for (int gx = 0; gx < G; gx++) {
-                const double x = (gx + 0.5) * w / G;
-                const int row = (int)floor((x * c + y * s) / h->p.derho) - rho_min;
-                const int wn = std::min(std::max(row / rows, 0), nwin - 1);
-                wt[(size_t)sl + (size_t)slices * wn] += (k1 - k0 + 1);
-                total += (k1 - k0 + 1);
+        const int k1 = std::min(k0 + HL_SLICE, h->T) - 1;
+        const double c0 = cos(k0 * h->p.detheta), s0 = sin(k0 * h->p.detheta);
+        const double c1 = cos(k1 * h->p.detheta), s1 = sin(k1 * h->p.detheta);
+        for (int ty = 0; ty < ty_n; ty++) {
+            const double ya = (double)ty * HL_TILE_H;
+            const double yb = std::min(ya + HL_TILE_H - 1, hh - 1.0);
+            for (int tx = 0; tx < tx_n; tx++) {
+                const double xa = (double)tx * HL_TILE_W;
+                const double xb = std::min(xa + HL_TILE_W - 1, w - 1.0);
+                double mn = 1e300, mx = -1e300;
+                for (int i = 0; i < 4; i++) {
+                    const double x = (i & 1) ? xb : xa, y = (i & 2) ? yb : ya;
+                    const double f0 = x * c0 + y * s0, f1 = x * c1 + y * s1;
+                    mn = std::min(mn, std::min(f0, f1));
+                    double hi = std::max(f0, f1);
+                    if (c0 * y - s0 * x >= 0.0 && x * s1 - y * c1 >= 0.0)
+                        hi = std::max(hi, x + y);
+                    mx = std::max(mx, hi);
+                }
+                const double lo_r = mn * irho - 3.0 - rho_min;
+                const double hi_r = mx * irho + 3.0 - rho_min;
+                if (hi_r < 0.0 || lo_r > R - 1.0)
+                    continue;
+                int wlo = nwin > 1 ? (int)floor(std::max(lo_r, 0.0) / rows) : 0;
+                int whi = nwin > 1 ? (int)floor(std::min(hi_r, R - 1.0) / rows) : 0;
+                wlo = std::min(std::max(wlo, 0), nwin - 1);
+                whi = std::min(std::max(whi, wlo), nwin - 1);
+                const double area = (xb - xa + 1.0) * (yb - ya + 1.0);
+                for (int wn = wlo; wn <= whi; wn++)
+                    wt[(size_t)sl + (size_t)slices * wn] += area;
             }
         }
     }
-    const double cap = total / (3.0 * std::max(ctas, 1));
-    struct part_t { double wt; int blk, part, nparts; };
-    std::vector<part_t> parts;
-    parts.reserve((size_t)nblocks * 2);
-    int any_split = 0;
-    for (int b = 0; b < nblocks; b++) {
+}
+
+/* Split plan of the vote blocks (weights wt, ctas persistent CTAs): a block
+ * heavier than cap = total / (capf * ctas) is cut into ceil(wt / cap) parts
+ * (at most 16).  Then one pass over a list schedule of the parts (each CTA
+ * takes the next part, heaviest first, when it is free -- the vote kernel's
+ * own order): a part that would start after 60% of the estimated makespan and
+ * weighs more than cap / 4 is halved (part p of n becomes parts 2p and 2p + 1
+ * of 2n, the same range of the block's batches), so the last parts to start
+ * are small and the CTAs finish together.  Returns the parts heaviest first;
+ * pieces[b] counts block b's parts. */
+struct vote_part { double wt; int blk, part, nparts; };
+static std::vector<vote_part> plan_parts(const std::vector<double> &wt, int ctas,
+                                         double capf, std::vector<int> &pieces)
+{
+    double total = 0.0;
+    for (double v : wt)
+        total += v;
+    const double cap = total / (capf * std::max(ctas, 1));
+    std::vector<vote_part> parts;
+    parts.reserve(wt.size() * 2);
+    for (size_t b = 0; b < wt.size(); b++) {
         int np = 1;
         if (cap > 0.0 && wt[b] > cap)
             np = std::min(16, (int)ceil(wt[b] / cap));
-        if (np > 1)
-            any_split = 1;
         for (int q = 0; q < np; q++)
-            parts.push_back({wt[b] / np, b, q, np});
+            parts.push_back({wt[b] / np, (int)b, q, np});
     }
-    std::stable_sort(parts.begin(), parts.end(),
-                     [](const part_t &a, const part_t &b) { return a.wt > b.wt; });
-    const int n = (int)parts.size();
-    std::vector<int2> items((size_t)n);
-    for (int i = 0; i < n; i++)
-        items[i] = make_int2(parts[i].blk, parts[i].part | (parts[i].nparts << 16));
-    int rc = grow((void **)&h->order_dev, &h->cap_order, sizeof(int2) * (size_t)n);
+    const auto heavier = [](const vote_part &a, const vote_part &c) { return a.wt > c.wt; };
+    std::stable_sort(parts.begin(), parts.end(), heavier);
+    {
+        typedef std::pair<double, int> slot_t;
+        std::priority_queue<slot_t, std::vector<slot_t>, std::greater<slot_t>> free_at;
+        for (int c = 0; c < std::max(ctas, 1); c++)
+            free_at.push({0.0, c});
+        std::vector<double> start(parts.size());
+        double makespan = 0.0;
+        for (size_t i = 0; i < parts.size(); i++) {
+            slot_t f = free_at.top();
+            free_at.pop();
+            start[i] = f.first;
+            makespan = std::max(makespan, f.first + parts[i].wt);
+            free_at.push({f.first + parts[i].wt, f.second});
+        }
+        std::vector<vote_part> out;
+        out.reserve(parts.size() * 2);
+        for (size_t i = 0; i < parts.size(); i++) {
+            const vote_part &p = parts[i];
+            if (start[i] > 0.6 * makespan && p.wt > 0.25 * cap && p.nparts <= 16) {
+                out.push_back({p.wt / 2, p.blk, 2 * p.part, 2 * p.nparts});
+                out.push_back({p.wt / 2, p.blk, 2 * p.part + 1, 2 * p.nparts});
+            } else {
+                out.push_back(p);
+            }
+        }
+        parts.swap(out);
+    }
+    std::stable_sort(parts.begin(), parts.end(), heavier);
+    pieces.assign(wt.size(), 0);
+    for (const vote_part &p : parts)
+        pieces[p.blk]++;
+    return parts;
+}
+
+/* Work items of the vote kernel, heaviest first, weighted by
+ * block_weights_tiles.  A block heavier than half of one CTA's fair share
+ * (total / ctas; a third and a quarter measured slower at 4096 x 4096) is
+ * split into parts that each vote a contiguous share of the point stream
+ * (at most 16 parts), each voting into its own scratch slot; the merge
+ * launch after the vote sums a split block's slots.  Cached per geometry with
+ * the list of split blocks; fills va's items and scratch. */
+static int vote_items(hl_handle *h, int w, int hh, int rho_min, int R,
+                      int rows, int nwin, int ctas, hl_vote_args *va)
+{
+    const int slices = h->Tp / HL_SLICE;
+    const int nblocks = slices * nwin;
+    if (!(h->order_dev && h->order_w == w && h->order_h == hh &&
+          h->order_rows == rows && h->order_R == R && h->order_T == h->T &&
+          h->order_derho == h->p.derho && h->order_detheta == h->p.detheta &&
+          h->order_ctas == ctas)) {
+        h->masks_dirty = 1;
+        std::vector<double> wt;
+        block_weights_tiles(h, w, hh, rho_min, R, rows, nwin, wt);
+        std::vector<int> pieces;
+        const std::vector<vote_part> parts = plan_parts(wt, ctas, 2.0, pieces);
+        /* scratch slots and merge regions of the split blocks */
+        std::vector<hl_merge_region> merge;
+        std::vector<int> slot0((size_t)nblocks, 0), used((size_t)nblocks, 0);
+        int nslots = 0;
+        for (int b = 0; b < nblocks; b++) {
+            if (pieces[b] <= 1)
+                continue;
+            const int w0 = (b / slices) * rows, k0 = (b % slices) * HL_SLICE;
+            const long long off = (long long)w0 * h->Tp + k0;
+            slot0[b] = nslots;
+            merge.push_back({off / 4, std::min(rows, R - w0), k0, nslots, pieces[b], {0, 0}});
+            nslots += pieces[b];
+        }
+        const int n = (int)parts.size();
+        std::vector<int4> items((size_t)n);
+        for (int i = 0; i < n; i++) {
+            const vote_part &p = parts[i];
+            const int slot = pieces[p.blk] > 1 ? slot0[p.blk] + used[p.blk]++ : 0;
+            items[i] = make_int4(p.blk, p.part | (p.nparts << 16), slot, 0);
+        }
+        int rc = grow((void **)&h->order_dev, &h->cap_order, sizeof(int4) * (size_t)n);
+        if (rc == HL_NO_ERROR && !merge.empty())
+            rc = grow((void **)&h->d_merge, &h->cap_merge,
+                      sizeof(hl_merge_region) * merge.size());
+        if (rc != HL_NO_ERROR)
+            return rc;
+        CK(cudaMemcpy(h->order_dev, items.data(), sizeof(int4) * (size_t)n,
+                      cudaMemcpyHostToDevice));
+        if (!merge.empty())
+            CK(cudaMemcpy(h->d_merge, merge.data(), sizeof(hl_merge_region) * merge.size(),
+                          cudaMemcpyHostToDevice));
+        h->order_w = w;
+        h->order_h = hh;
+        h->order_rows = rows;
+        h->order_R = R;
+        h->order_T = h->T;
+        h->order_derho = h->p.derho;
+        h->order_detheta = h->p.detheta;
+        h->order_ctas = ctas;
+        h->order_n = n;
+        h->order_nmerge = (int)merge.size();
+        h->order_nslots = nslots;
+    }
+    int rc = grow((void **)&h->d_scratch, &h->cap_scratch,
+                  sizeof(int4) * (size_t)std::max(h->order_nslots, 1) * rows * (HL_SLICE / 4));
     if (rc != HL_NO_ERROR)
         return rc;
-    CK(cudaMemcpy(h->order_dev, items.data(), sizeof(int2) * (size_t)n,
-                  cudaMemcpyHostToDevice));
-    h->order_w = w;
-    h->order_h = hh;
-    h->order_rows = rows;
-    h->order_R = R;
-    h->order_T = h->T;
-    h->order_derho = h->p.derho;
-    h->order_ctas = ctas;
-    h->order_n = n;
-    h->order_split = any_split;
-    *dev_items = h->order_dev;
-    *nitems_out = n;
-    *split = any_split;
+    va->items = h->order_dev;
+    va->nitems = h->order_n;
+    va->scratch = h->d_scratch;
     return HL_NO_ERROR;
 }
 
@@ -541,7 +674,55 @@ static int run_ab(hl_handle *h, const hl_roi &roi, const hl_geom &g,
                   cudaStream_t s, int *launches)
 {
     const int ntiles = g.tiles_x * g.tiles_y;
+
+    /* the vote plan first: its split blocks' regions are cleared by the
+     * compaction launch, and its tile masks are computed once per geometry */
+    hl_vote_args va;
+    memset(&va, 0, sizeof(va));
+    va.imgs = nullptr;
+    va.img0.pts = reinterpret_cast<const float2 *>(h->d_pts);
+    va.img0.tile_off = h->d_tile_off;
+    va.img0.ntiles = ntiles;
+    va.img0.tiles_x = g.tiles_x;
+    va.img0.w = roi.w;
+    va.img0.h = roi.h;
+    va.img0.rho_min = g.rho_min;
+    va.img0.R = g.numrho;
+    va.img0.pad = 0;
+    va.img0.acc = h->d_acc;
+    va.cosv = h->d_cos;
+    va.sinv = h->d_sin;
+    va.T = h->T;
+    va.Tp = h->Tp;
+    int threads;
+    vote_shape(h, g.numrho, &va.win_rows, &va.img0.nwin, &threads);
+    va.irho = (float)(1.0 / h->p.derho);   /* okano_3_0/HoughLine.cu:107 */
+    va.status = h->d_counters + 1;
+    /* persistent CTAs: as many as fit (one per SM at 1024 threads) */
+    const size_t smem = hl_vote_smem_bytes(va.win_rows);
+    const int per_sm = std::max(1, std::min(2048 / threads,
+                                            (int)((228u * 1024u) / (smem + 1024))));
+    const int ctas = std::max(h->sms, 1) * per_sm;
+    int rc = vote_items(h, roi.w, roi.h, g.rho_min, g.numrho, va.win_rows,
+                        va.img0.nwin, ctas, &va);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    const size_t mwords = hl_tile_mask_words(h->Tp / HL_SLICE, va.img0.nwin, ntiles);
+    const void *old_mask = h->d_tmask;
+    if ((rc = grow((void **)&h->d_tmask, &h->cap_tmask, sizeof(unsigned) * mwords)) !=
+        HL_NO_ERROR)
+        return rc;
+    if (h->d_tmask != old_mask)
+        h->masks_dirty = 1;
+    va.img0.tmask = h->d_tmask;
+    if (h->masks_dirty) {
+        CK(hl_launch_tile_masks(&va, 1, mwords, s));
+        (*launches)++;
+        h->masks_dirty = 0;
+    }
+
     hl_compact_args ca;
+    memset(&ca, 0, sizeof(ca));
     ca.roi = roi;
     ca.tiles_x = g.tiles_x;
     ca.ntiles = ntiles;
@@ -569,38 +750,6 @@ static int run_ab(hl_handle *h, const hl_roi &roi, const hl_geom &g,
     (*launches)++;
     prof_mark(h, 1, s);
 
-    hl_vote_args va;
-    va.imgs = nullptr;
-    va.img0.pts = reinterpret_cast<const float2 *>(h->d_pts);
-    va.img0.tile_off = h->d_tile_off;
-    va.img0.ntiles = ntiles;
-    va.img0.tiles_x = g.tiles_x;
-    va.img0.w = roi.w;
-    va.img0.h = roi.h;
-    va.img0.rho_min = g.rho_min;
-    va.img0.R = g.numrho;
-    va.img0.pad = 0;
-    va.img0.acc = h->d_acc;
-    va.cosv = h->d_cos;
-    va.sinv = h->d_sin;
-    va.T = h->T;
-    va.Tp = h->Tp;
-    int threads;
-    vote_shape(h, g.numrho, &va.win_rows, &va.img0.nwin, &threads);
-    va.irho = (float)(1.0 / h->p.derho);   /* okano_3_0/HoughLine.cu:107 */
-    va.status = h->d_counters + 1;
-    /* persistent CTAs: as many as fit (one per SM at 1024 threads) */
-    const size_t smem = hl_vote_smem_bytes(va.win_rows);
-    const int per_sm = std::max(1, std::min(2048 / threads,
-                                            (int)((228u * 1024u) / (smem + 1024))));
-    const int ctas = std::max(h->sms, 1) * per_sm;
-    int split = 0;
-    int rc = vote_items(h, roi.w, roi.h, g.rho_min, g.numrho, va.win_rows,
-                        va.img0.nwin, ctas, &va.items, &va.nitems, &split);
-    if (rc != HL_NO_ERROR)
-        return rc;
-    if (split)   /* parts of a split block add into the accumulator */
-        CK(cudaMemsetAsync(h->d_acc, 0, sizeof(int32_t) * (size_t)g.numrho * h->Tp, s));
     const int grid = std::min(va.nitems, ctas);
     va.work = reinterpret_cast<unsigned *>(h->d_counters + 9);
     va.work_base = h->work_base;
@@ -608,6 +757,18 @@ static int run_ab(hl_handle *h, const hl_roi &roi, const hl_geom &g,
     /* every CTA takes one ticket per item plus one that finds no item */
     h->work_base += (unsigned)(va.nitems + grid);
     (*launches)++;
+    if (h->order_nmerge > 0) {
+        hl_merge_args ma;
+        ma.acc = reinterpret_cast<int4 *>(h->d_acc);
+        ma.pitch4 = h->Tp / 4;
+        ma.T = h->T;
+        ma.scratch = h->d_scratch;
+        ma.slot4 = (long long)va.win_rows * (HL_SLICE / 4);
+        ma.regs = h->d_merge;
+        ma.nreg = h->order_nmerge;
+        CK(hl_launch_merge(&ma, va.win_rows, s));
+        (*launches)++;
+    }
     prof_mark(h, 2, s);
     return HL_NO_ERROR;
 }
@@ -784,6 +945,7 @@ extern "C" int hl_compact(hl_handle *h, const hl_image_desc *img,
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     const int ntiles = g.tiles_x * g.tiles_y;
     hl_compact_args ca;
+    memset(&ca, 0, sizeof(ca));
     ca.roi = roi;
     ca.tiles_x = g.tiles_x;
     ca.ntiles = ntiles;
@@ -1097,6 +1259,11 @@ struct hl_batch_ws {
     size_t cap_acc;
     unsigned long long *d_keys;
     size_t cap_keys;
+    int4 *d_scratch;               /* split parts' slots: win_rows x HL_SLICE */
+    size_t cap_scratch;
+    unsigned *d_tmask;             /* every image's admitted-tile masks */
+    size_t cap_tmask;
+    int masks_dirty;               /* the plan changed: recompute them */
     int *d_ncand;                  /* per image, zero between calls */
     size_t cap_ncand;
     int *d_cnt;
@@ -1117,15 +1284,18 @@ struct hl_batch_ws {
     std::vector<int> key;
     size_t tab_bytes;
     size_t off_cimg, off_gimg, off_vimg, off_items, off_pimg, off_chunks,
-        off_fimg;
+        off_fimg, off_merge;
     int ngroups, ntiles, nitems, nchunks, grid, threads, win_rows;
     size_t npts_cap, acc_ints, nkeys;
     std::vector<size_t> acc_off, key_off;
     std::vector<size_t> pts_base;  /* each image's first point */
     std::vector<int> key_cap_i, tile_base, group_base, nwin, rho_min, R,
         ref_numrho;
-    std::vector<int> split_img;    /* images whose accumulator is added to */
-    std::vector<int2> items;
+    std::vector<int4> items;
+    std::vector<hl_merge_region> merge; /* the split blocks */
+    int nslots;                    /* scratch slots of their parts */
+    std::vector<size_t> tmask_off; /* each image's first mask word */
+    size_t tmask_words, max_mask_words;
     std::vector<int2> chunks;
     std::vector<int> group_img;
 
@@ -1152,7 +1322,8 @@ static void batch_ws_free(hl_batch_ws *b)
     if (!b)
         return;
     void *dp[] = {b->d_pts, b->d_state, b->d_tile_off, b->d_acc, b->d_keys,
-                  b->d_ncand, b->d_cnt, b->d_tab, b->d_lines, b->d_counts};
+                  b->d_ncand, b->d_cnt, b->d_tab, b->d_lines, b->d_counts,
+                  b->d_scratch, b->d_tmask};
     for (void *q : dp)
         if (q)
             cudaFree(q);
@@ -1209,7 +1380,7 @@ static void batch_block_weights(const hl_handle *h, int w, int hh, int rho_min,
                 const double x = (gx + 0.5) * w / G;
                 const int row = (int)floor((x * c + y * sn) / h->p.derho) - rho_min;
                 const int wn = std::min(std::max(row / rows, 0), nwin - 1);
-                wt[(size_t)sl + (size_t)slices * wn] += cell * (k1 - k0 + 1);
+                wt[(size_t)sl + (size_t)slices * wn] += cell;   /* 32 lanes per point */
             }
         }
     }
@@ -1250,6 +1421,12 @@ static int batch_plan(hl_handle *h, hl_batch_ws *b, const hl_image_desc *imgs,
     key.push_back(rows);
     key.push_back(threads);
     key.push_back(h->T);
+    {   /* derho sets every image's rho range */
+        unsigned long long bits;
+        memcpy(&bits, &h->p.derho, sizeof(bits));
+        key.push_back((int)(bits & 0xffffffffu));
+        key.push_back((int)(bits >> 32));
+    }
     for (int i = 0; i < nimg; i++) {
         key.push_back(rois[i].w);
         key.push_back(rois[i].h);
@@ -1272,10 +1449,13 @@ static int batch_plan(hl_handle *h, hl_batch_ws *b, const hl_image_desc *imgs,
         size_t acc = 0, keys = 0, pts = 0;
         b->pts_base.assign(nimg, 0);
         int tiles = 0, groups = 0;
+        b->tmask_off.assign(nimg, 0);
+        b->tmask_words = 0;
+        b->max_mask_words = 0;
+        b->masks_dirty = 1;
         std::vector<double> allw;
         std::vector<int2> blocks;
         std::vector<double> wt;
-        double total = 0.0;
         for (int i = 0; i < nimg; i++) {
             const hl_geom &g = gs[i];
             const int nt = g.tiles_x * g.tiles_y;
@@ -1302,6 +1482,12 @@ static int batch_plan(hl_handle *h, hl_batch_ws *b, const hl_image_desc *imgs,
             b->R[i] = g.numrho;
             b->ref_numrho[i] = g.ref_numrho;
             b->nwin[i] = (g.numrho + rows - 1) / rows;
+            {
+                const size_t mw = hl_tile_mask_words(slices, b->nwin[i], nt);
+                b->tmask_off[i] = b->tmask_words;
+                b->tmask_words += mw;
+                b->max_mask_words = std::max(b->max_mask_words, mw);
+            }
             for (int r0 = 0; r0 < g.numrho; r0 += HL_PEAK_ROWS)
                 b->chunks.push_back(make_int2(i, r0));
             if ((size_t)slices * b->nwin[i] > 0xffff)
@@ -1311,36 +1497,38 @@ static int batch_plan(hl_handle *h, hl_batch_ws *b, const hl_image_desc *imgs,
             for (size_t q = 0; q < wt.size(); q++) {
                 blocks.push_back(make_int2(i, (int)q));
                 allw.push_back(wt[q]);
-                total += wt[q];
             }
         }
         if (nimg > 0xffff)
             return HL_OP_OVERFLOW;   /* the item packs the image in 16 bits */
-        /* items: heaviest first; a block heavier than a third of one CTA's
-         * share is split (its image's accumulator is then cleared first) */
-        const double cap = total / (3.0 * std::max(ctas, 1));
-        struct part_t { double wt; int img, blk, part, nparts; };
-        std::vector<part_t> parts;
-        std::vector<char> split((size_t)nimg, 0);
+        /* items: plan_parts over every image's blocks (a block heavier
+         * than a third of one CTA's share is split); the parts of a split
+         * block vote into scratch slots, summed into it by the merge
+         * launch */
+        std::vector<int> pieces;
+        const std::vector<vote_part> parts = plan_parts(allw, ctas, 3.0, pieces);
+        b->merge.clear();
+        std::vector<int> slot0(blocks.size(), 0), used(blocks.size(), 0);
+        int nslots = 0;
         for (size_t q = 0; q < blocks.size(); q++) {
-            int np = 1;
-            if (cap > 0.0 && allw[q] > cap)
-                np = std::min(16, (int)ceil(allw[q] / cap));
-            if (np > 1)
-                split[blocks[q].x] = 1;
-            for (int pp = 0; pp < np; pp++)
-                parts.push_back({allw[q] / np, blocks[q].x, blocks[q].y, pp, np});
+            if (pieces[q] <= 1)
+                continue;
+            const int im = blocks[q].x, blk = blocks[q].y;
+            const int w0 = (blk / slices) * rows, k0 = (blk % slices) * HL_SLICE;
+            const long long off = (long long)b->acc_off[im] + (long long)w0 * h->Tp + k0;
+            slot0[q] = nslots;
+            b->merge.push_back({off / 4, std::min(rows, b->R[im] - w0), k0, nslots, pieces[q],
+                                {0, 0}});
+            nslots += pieces[q];
         }
-        std::stable_sort(parts.begin(), parts.end(),
-                         [](const part_t &a, const part_t &c) { return a.wt > c.wt; });
         b->items.resize(parts.size());
-        for (size_t q = 0; q < parts.size(); q++)
-            b->items[q] = make_int2(parts[q].blk | (parts[q].img << 16),
-                                    parts[q].part | (parts[q].nparts << 16));
-        b->split_img.clear();
-        for (int i = 0; i < nimg; i++)
-            if (split[i])
-                b->split_img.push_back(i);
+        for (size_t q = 0; q < parts.size(); q++) {
+            const vote_part &p = parts[q];
+            const int slot = pieces[p.blk] > 1 ? slot0[p.blk] + used[p.blk]++ : 0;
+            b->items[q] = make_int4(blocks[p.blk].y | (blocks[p.blk].x << 16),
+                                    p.part | (p.nparts << 16), slot, 0);
+        }
+        b->nslots = nslots;
         b->ngroups = groups;
         b->ntiles = tiles;
         b->nitems = (int)b->items.size();
@@ -1354,7 +1542,8 @@ static int batch_plan(hl_handle *h, hl_batch_ws *b, const hl_image_desc *imgs,
         b->off_cimg = o;   o = align16(o + sizeof(hl_compact_img) * nimg);
         b->off_gimg = o;   o = align16(o + sizeof(int) * (size_t)groups);
         b->off_vimg = o;   o = align16(o + sizeof(hl_vote_img) * nimg);
-        b->off_items = o;  o = align16(o + sizeof(int2) * b->items.size());
+        b->off_items = o;  o = align16(o + sizeof(int4) * b->items.size());
+        b->off_merge = o;  o = align16(o + sizeof(hl_merge_region) * b->merge.size());
         b->off_pimg = o;   o = align16(o + sizeof(hl_peak_img) * nimg);
         b->off_chunks = o; o = align16(o + sizeof(int2) * b->chunks.size());
         b->off_fimg = o;   o = align16(o + sizeof(hl_final_img) * nimg);
@@ -1371,7 +1560,13 @@ static int batch_plan(hl_handle *h, hl_batch_ws *b, const hl_image_desc *imgs,
         (rc = grow((void **)&b->d_acc, &b->cap_acc, sizeof(int32_t) * b->acc_ints)) != HL_NO_ERROR ||
         (rc = grow((void **)&b->d_keys, &b->cap_keys,
                    sizeof(unsigned long long) * b->nkeys)) != HL_NO_ERROR ||
-        (rc = grow((void **)&b->d_tab, &b->cap_tab, b->tab_bytes)) != HL_NO_ERROR)
+        (rc = grow((void **)&b->d_tab, &b->cap_tab, b->tab_bytes)) != HL_NO_ERROR ||
+        (rc = grow((void **)&b->d_scratch, &b->cap_scratch,
+                   sizeof(int4) * (size_t)std::max(b->nslots, 1) * b->win_rows *
+                       (HL_SLICE / 4))) != HL_NO_ERROR ||
+        (rc = grow_tracked((void **)&b->d_tmask, &b->cap_tmask,
+                           sizeof(unsigned) * std::max(b->tmask_words, (size_t)1),
+                           &b->masks_dirty)) != HL_NO_ERROR)
         return rc;
     if (b->cap_ncand < sizeof(int) * (size_t)nimg || !b->d_ncand) {
         if ((rc = grow((void **)&b->d_ncand, &b->cap_ncand, sizeof(int) * (size_t)nimg)) !=
@@ -1414,6 +1609,7 @@ static int batch_plan(hl_handle *h, hl_batch_ws *b, const hl_image_desc *imgs,
         vi[i].R = g.numrho;
         vi[i].nwin = b->nwin[i];
         vi[i].pad = 0;
+        vi[i].tmask = b->d_tmask + b->tmask_off[i];
         vi[i].acc = b->d_acc + b->acc_off[i];
         pi[i].acc = b->d_acc + b->acc_off[i];
         pi[i].keys = b->d_keys + b->key_off[i];
@@ -1432,7 +1628,9 @@ static int batch_plan(hl_handle *h, hl_batch_ws *b, const hl_image_desc *imgs,
         fi[i].count_out = counts_dev + i;
     }
     memcpy(t + b->off_gimg, b->group_img.data(), sizeof(int) * b->group_img.size());
-    memcpy(t + b->off_items, b->items.data(), sizeof(int2) * b->items.size());
+    memcpy(t + b->off_items, b->items.data(), sizeof(int4) * b->items.size());
+    if (!b->merge.empty())
+        memcpy(t + b->off_merge, b->merge.data(), sizeof(hl_merge_region) * b->merge.size());
     memcpy(t + b->off_chunks, b->chunks.data(), sizeof(int2) * b->chunks.size());
     return HL_NO_ERROR;
 }
@@ -1447,9 +1645,6 @@ static int batch_enqueue_compact(hl_handle *h, hl_batch_ws *b, int nimg,
     CK(cudaMemsetAsync(b->d_state, 0,
                        sizeof(unsigned long long) * ((size_t)b->ngroups + 1), s));
     CK(cudaMemcpyAsync(dt, b->h_tab, b->tab_bytes, cudaMemcpyHostToDevice, s));
-    for (int i : b->split_img)
-        CK(cudaMemsetAsync(b->d_acc + b->acc_off[i], 0,
-                           sizeof(int32_t) * (size_t)b->R[i] * h->Tp, s));
 
     hl_compact_args ca;
     memset(&ca, 0, sizeof(ca));
@@ -1485,11 +1680,23 @@ static int batch_enqueue_vote_peaks(hl_handle *h, hl_batch_ws *b, cudaStream_t s
     va.win_rows = b->win_rows;
     va.irho = (float)(1.0 / h->p.derho);   /* okano_3_0/HoughLine.cu:107 */
     va.status = b->d_cnt + 2;
-    va.items = reinterpret_cast<const int2 *>(dt + b->off_items);
+    va.items = reinterpret_cast<const int4 *>(dt + b->off_items);
     va.nitems = b->nitems;
+    va.scratch = b->d_scratch;
     va.work = reinterpret_cast<unsigned *>(b->d_cnt + 1);
     va.work_base = 0;
     CK(hl_launch_vote(&va, b->threads, b->grid, s));
+    if (!b->merge.empty()) {
+        hl_merge_args ma;
+        ma.acc = reinterpret_cast<int4 *>(b->d_acc);
+        ma.pitch4 = h->Tp / 4;
+        ma.T = h->T;
+        ma.scratch = b->d_scratch;
+        ma.slot4 = (long long)b->win_rows * (HL_SLICE / 4);
+        ma.regs = reinterpret_cast<const hl_merge_region *>(dt + b->off_merge);
+        ma.nreg = (int)b->merge.size();
+        CK(hl_launch_merge(&ma, b->win_rows, s));
+    }
     prof_mark(h, 2, s);
 
     hl_peak_args pa;
@@ -1562,6 +1769,23 @@ static int batch_run_ws(hl_handle *h, hl_batch_ws **pb, const hl_image_desc *img
         CK(cudaEventCreateWithFlags(&b->tab_read, cudaEventDisableTiming));
         b->tab_event = 1;
     }
+    if (b->masks_dirty) {
+        /* tile masks of the new plan, outside the (captured) pipeline: the
+         * image table they read is the one the pipeline uploads again */
+        CK(cudaMemcpyAsync(b->d_tab + b->off_vimg, b->h_tab + b->off_vimg,
+                           sizeof(hl_vote_img) * (size_t)nimg, cudaMemcpyHostToDevice, s));
+        hl_vote_args va;
+        memset(&va, 0, sizeof(va));
+        va.imgs = reinterpret_cast<const hl_vote_img *>(b->d_tab + b->off_vimg);
+        va.cosv = h->d_cos;
+        va.sinv = h->d_sin;
+        va.T = h->T;
+        va.Tp = h->Tp;
+        va.win_rows = b->win_rows;
+        va.irho = (float)(1.0 / h->p.derho);
+        CK(hl_launch_tile_masks(&va, nimg, b->max_mask_words, s));
+        b->masks_dirty = 0;
+    }
     prof_mark(h, 0, s);
     if (!h->batch_graph || h->prof) {
         rc = batch_enqueue(h, b, nimg, K, s);
@@ -1576,6 +1800,8 @@ static int batch_run_ws(hl_handle *h, hl_batch_ws **pb, const hl_image_desc *img
         gk.push_back((long long)(uintptr_t)b->d_tab);
         gk.push_back((long long)(uintptr_t)b->h_tab);
         gk.push_back((long long)(uintptr_t)b->d_keys);
+        gk.push_back((long long)(uintptr_t)b->d_tmask);
+        gk.push_back((long long)(uintptr_t)b->d_scratch);
         if (!b->gexec || gk != b->gkey) {
             if (b->gexec) {
                 cudaGraphExecDestroy(b->gexec);

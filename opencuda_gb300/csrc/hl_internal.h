@@ -75,10 +75,15 @@ typedef struct hl_compact_args {
     int *status;
 } hl_compact_args;
 
+
 /* One image of a vote launch. */
 typedef struct hl_vote_img {
     const float2 *pts;        /* (x, y) of every edge point, tile-major */
     const int *tile_off;      /* the image's [ntiles + 1] tile offsets */
+    /* admitted tiles of every (slice, window) block: bit t % 32 of word
+     * [block][t / 32] (hl_launch_tile_masks; they depend on the geometry
+     * only) */
+    unsigned *tmask;
     int ntiles, tiles_x;
     int w, h;                 /* ROI size (tile clipping) */
     int rho_min, R;
@@ -98,14 +103,37 @@ typedef struct hl_vote_args {
     /* persistent scheduling: work items are taken in the order items[]
      * (heaviest first) from a monotonically increasing counter.  An item is
      * one part of a (slice, window) block of one image: .x = block | image
-     * << 16 with block = slice + nslices * window, .y = part | nparts << 16;
-     * a block split into several parts adds its partial counts into a zeroed
-     * accumulator with red.global */
-    const int2 *items;
+     * << 16 with block = slice + nslices * window, .y = part | nparts << 16,
+     * .z = the part's scratch slot when nparts > 1, .w = 0.  A whole block
+     * is stored into the accumulator; a part of a split block stores its
+     * counts to its slot, and hl_merge_kernel adds the parts' slots into the
+     * block afterwards. */
+    const int4 *items;
     int nitems;
     unsigned *work;           /* counter */
     unsigned work_base;       /* its value at launch */
+    int4 *scratch;            /* slots of win_rows x HL_SLICE counts */
 } hl_vote_args;
+
+/* A split vote block: its accumulator region (rows x 8 int4 from off4, rows
+ * pitch4 apart, first theta k0) is the sum of nparts scratch slots from
+ * slot0 on. */
+typedef struct hl_merge_region {
+    long long off4;
+    int rows, k0;
+    int slot0, nparts;
+    int pad[2];
+} hl_merge_region;
+
+typedef struct hl_merge_args {
+    int4 *acc;
+    int pitch4;
+    int T;
+    const int4 *scratch;
+    long long slot4;          /* int4 per scratch slot */
+    const hl_merge_region *regs;
+    int nreg;
+} hl_merge_args;
 
 /* Tiles the allocation-free compaction entry point can serve. */
 #define HL_NOALLOC_MAX_TILES 65536
@@ -170,6 +198,16 @@ typedef struct hl_final_args {
 cudaError_t hl_launch_trig(float *cosv, float *sinv, int T, int Tp,
                            double detheta, cudaStream_t s);
 cudaError_t hl_launch_compact(const hl_compact_args *a, cudaStream_t s);
+/* Tile masks of every image of a vote launch (nimg images: a->imgs, or
+ * a->img0 when it is NULL); the vote kernel reads them. */
+cudaError_t hl_launch_tile_masks(const hl_vote_args *a, int nimg,
+                                 size_t max_words, cudaStream_t s);
+/* words of an image's tile mask */
+static inline size_t hl_tile_mask_words(int nslices, int nwin, int ntiles)
+{
+    return (size_t)nslices * nwin * ((ntiles + 31) / 32);
+}
+cudaError_t hl_launch_merge(const hl_merge_args *a, int max_rows, cudaStream_t s);
 cudaError_t hl_launch_vote(const hl_vote_args *a, int threads, int grid,
                            cudaStream_t s);
 size_t hl_vote_smem_bytes(int win_rows);

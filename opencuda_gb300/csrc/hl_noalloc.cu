@@ -16,6 +16,8 @@
  */
 #include <mutex>
 
+#include <string.h>
+
 #include "hl_internal.h"
 
 /* [0] tile ticket, [1] status word, [2 ..] one look-back state per tile */
@@ -76,6 +78,7 @@ extern "C" int hl_compact_noalloc(const hl_image_desc *img, uint32_t *pts_dev,
                         s) != cudaSuccess)
         return HL_CUDA_ERROR;
     hl_compact_args ca;
+    memset(&ca, 0, sizeof(ca));
     ca.roi.base = img->data + (size_t)img->roi_y1 * img->pitch + img->roi_x1;
     ca.roi.pitch = (long)img->pitch;
     ca.roi.w = w;

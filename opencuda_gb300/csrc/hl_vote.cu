@@ -15,24 +15,28 @@
  * one address (the aggregation a warp-aggregated atomic would buy is built
  * into the layout).
  *
- * Pipeline.  Persistent CTAs take items heaviest-first from a global counter.
- * For an item, all threads mark the 128x32 compaction tiles whose rho
- * interval over the slice meets the window and turn the marks into runs of
- * tiles -- contiguous ranges of the tile-major point list, 16-byte aligned
- * because the compaction pads every tile to an even number of float2
- * entries.  The runs, laid end to end, form the item's point stream.  Then
- * the CTA splits into one producer warp and consumer warps that meet only on
- * mbarriers: a batch is 64 points per consumer warp, batch b the stream
+ * Pipeline.  Persistent CTAs of one producer warp and consumer warps that
+ * meet only on mbarriers.  The producer takes items heaviest-first from a
+ * global counter.  For an item it reads the block's tile mask -- the 128x32
+ * compaction tiles whose rho interval over the slice meets the window,
+ * computed once per geometry by hl_tile_mask_kernel -- and turns it into
+ * runs of tiles: contiguous ranges of the tile-major point list, 16-byte
+ * aligned because the compaction pads every tile to an even number of
+ * float2 entries.  The runs, laid end to end, form the item's point stream.
+ * It publishes the item as a segment (double-buffered descriptor) and
+ * streams it: a batch is 64 points per consumer warp, batch b the stream
  * range [b*B, (b+1)*B); the producer's lanes each copy one run's part of it
  * into a ring of HL_VOTE_SLOTS shared-memory slots with cp.async.bulk (TMA
  * bulk copies completing on the slot's full barrier), so a slot holds its
  * batch gap-free; consumer warp i votes points [64i, 64i + 64) of the slot
  * straight from shared memory and arrives on the slot's empty barrier, which
- * the producer waits on before refilling it.  No block-wide barrier
- * separates batches.
- * At the end of the item the block is stored with coalesced 128-byte rows
- * into acc[R][Tp]; every bin is written exactly once, so the global
- * accumulator needs no clearing.
+ * the producer waits on before refilling it.  The producer moves on to the
+ * next item as soon as the current one is issued, so its setup and first
+ * copies overlap the consumers' last batches.
+ * When an item is voted the consumers store the block with coalesced
+ * 128-byte rows into acc[R][Tp] (a part of a split block: into its scratch
+ * slot, summed into the block by hl_merge_kernel) and clear it; every bin is
+ * written exactly once, so the accumulator needs no clearing.
  *
  * Per point and consumer warp: half a broadcast shared load (16-byte loads
  * of point pairs), two multiplies, two adds (the second one rounds to an
@@ -41,9 +45,11 @@
  * per vote.
  *
  * Bounds: every vote's row is clamped to the window's dump row (lanes past
- * the last theta to row 0 of their padding column, zeroed before the store),
- * mbarrier waits are bounded (a time-out sets a status bit that the host
- * reads with the result; every warp still reaches the same block barriers).
+ * the last theta to row 0 of their padding column, zeroed before the store).
+ * After the start there is no block-wide barrier, and every mbarrier wait is
+ * bounded: a time-out sets a status bit that the host reads with the result
+ * and an abort flag on which every other waiting warp gives up too; the
+ * producer then waits (bounded) for its copies in flight before exiting.
  */
 #include "hl_internal.h"
 #include "hl_device.cuh"
@@ -213,21 +219,55 @@ __device__ __forceinline__ void vote_share(const float2 *pts, int m, float c,
         vote_batch<UNIT, CV>(pts, m, 0, 1, c, s, irho, base, acc_l, lim);
 }
 
+/* Bounded wait that also gives up as soon as another warp of the CTA has
+ * given up (*abort_flag set).  A time-out sets the flag and the status bit;
+ * false means: leave the kernel. */
+__device__ __forceinline__ bool mbar_wait_ab(unsigned long long *bar,
+                                             unsigned parity, int *abort_flag,
+                                             int *status)
+{
+    const unsigned a = smem_u32(bar);
+    for (int i = 0; i < MBAR_WAIT_LIMIT; i++) {
+        unsigned ok;
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], "
+            "%2, %3; selp.u32 %0, 1, 0, p; }"
+            : "=r"(ok)
+            : "r"(a), "r"(parity), "r"(1000u)
+            : "memory");
+        if (ok)
+            return true;
+        if (*(volatile int *)abort_flag)
+            return false;
+    }
+    if ((threadIdx.x & 31) == 0)
+        atomicOr(status, HL_ST_VOTE_TIMEOUT);
+    *(volatile int *)abort_flag = 1;
+    return false;
+}
+
+/* One segment of the producer's stream: one tile group (HL_VOTE_TG tiles)
+ * of a work item, or the end of the work (item < 0). */
+struct VoteSeg {
+    int32_t *acc;                      /* the image's accumulator */
+    int item;                          /* slice + nslices * window, or -1 */
+    int part, nparts, slot;            /* see hl_vote_args.items */
+    int rho_min, R;                    /* the image's rho range */
+    int total;                         /* points in the segment's runs */
+    int b_lo, b_hi;                    /* this part's batches of them */
+    int first, last;                   /* first / last segment of the item */
+    float c[HL_SLICE], s[HL_SLICE];    /* cos / sin of the slice's thetas */
+};
+
 struct VoteSmem {
-    hl_vote_img im;                    /* the current item's image */
     unsigned long long full[HL_VOTE_SLOTS];
     unsigned long long empty[HL_VOTE_SLOTS];
-    int item;
-    int part;
-    int nruns;
-    int timeout;
-    int total;                         /* points in the group's runs */
-    unsigned mask[HL_VOTE_TG / 32];
-    unsigned sw[HL_VOTE_TG / 32];      /* run starts per mask word */
-    unsigned ew[HL_VOTE_TG / 32];      /* run ends per mask word */
-    int ws[HL_VOTE_TG / 32];           /* runs starting before the word */
-    int we[HL_VOTE_TG / 32];
-    int run_s[HL_VOTE_TG / 2];
+    unsigned long long seg_full[2];    /* producer -> consumers */
+    unsigned long long seg_empty[2];   /* consumers -> producer */
+    unsigned long long cbar;           /* barrier of the consumer threads */
+    int abort;                         /* a warp gave up waiting */
+    VoteSeg seg[2];
+    int run_s[HL_VOTE_TG / 2];         /* producer: the segment's runs */
     int run_e[HL_VOTE_TG / 2];
     int rpre[HL_VOTE_TG / 2];          /* stream position of each run */
     alignas(16) float2 raw[HL_VOTE_SLOTS][SLOT_CAP];
@@ -247,6 +287,283 @@ int hl_vote_max_rows(void)
     return (int)((cap - VOTE_FIXED) / (HL_SLICE * sizeof(int)) - 1) & ~7;
 }
 
+/* Admitted tiles of every (slice, window) block of an image: one warp per
+ * mask word, lane = tile (tile_hits; every tile when the image has a single
+ * window).  They depend on the geometry only, so callers compute them once
+ * per geometry. */
+__global__ void hl_tile_mask_kernel(hl_vote_args a)
+{
+    const hl_vote_img im = a.imgs ? a.imgs[blockIdx.y] : a.img0;
+    const int words = (im.ntiles + 31) >> 5;
+    const int nslices = a.Tp / HL_SLICE;
+    const long long nw = (long long)nslices * im.nwin * words;
+    const int lane = threadIdx.x & 31;
+    const long long wstep = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long wd = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+         wd < nw; wd += wstep) {
+        const int blk = (int)(wd / words), wi = (int)(wd % words);
+        const int slice = blk % nslices, win = blk / nslices;
+        const int k0 = slice * HL_SLICE;
+        const int klast = min(k0 + HL_SLICE - 1, a.T - 1);
+        const int w0 = win * a.win_rows;
+        const int rows = min(a.win_rows, im.R - w0);
+        const int t = wi * 32 + lane;
+        bool hit = false;
+        if (t < im.ntiles)
+            hit = im.nwin <= 1 ||
+                  tile_hits(t, im.tiles_x, im.w, im.h, a.cosv[k0], a.sinv[k0],
+                            a.cosv[klast], a.sinv[klast],
+                            (float)(im.rho_min + w0),
+                            (float)(im.rho_min + w0 + rows - 1), a.irho);
+        const unsigned m = __ballot_sync(FULL, hit);
+        if (lane == 0)
+            im.tmask[wd] = m;
+    }
+}
+
+/* barrier of the consumer threads (every one arrives; bounded wait) */
+__device__ __forceinline__ bool cons_sync(VoteSmem &sm, unsigned &par,
+                                          int *status)
+{
+    mbar_arrive(&sm.cbar);
+    const bool ok = mbar_wait_ab(&sm.cbar, par, &sm.abort, status);
+    par ^= 1u;
+    return ok;
+}
+
+/* Producer warp: takes items, turns each tile group of an item into a
+ * segment (runs of admitted tiles -> point ranges -> batches), publishes the
+ * segment and streams its batches into the ring.  It runs ahead of the
+ * consumers by up to the ring's depth, so the next item's setup and first
+ * copies overlap the current item's last votes. */
+__device__ __forceinline__ void vote_producer(const hl_vote_args &a,
+                                              VoteSmem &sm, int batch)
+{
+    const int lane = threadIdx.x & 31;
+    const int nslices = a.Tp / HL_SLICE;
+    unsigned seq = 0;    /* batches issued */
+    unsigned nseg = 0;   /* segments published */
+    bool ok = true;
+    while (ok) {
+        unsigned t = 0;
+        if (lane == 0)
+            t = atomicAdd(a.work, 1u) - a.work_base;
+        t = __shfl_sync(FULL, t, 0);
+        const bool have = t < (unsigned)a.nitems;
+        int4 it = make_int4(-1, 0, 0, 0);
+        hl_vote_img im = a.img0;
+        if (have) {
+            it = a.items[t];
+            if (a.imgs)
+                im = a.imgs[(unsigned)it.x >> 16];
+        }
+        const int item = have ? (it.x & 0xffff) : -1;
+        const int part = it.y & 0xffff, nparts = max(it.y >> 16, 1);
+        const int k0 = have ? (item % nslices) * HL_SLICE : 0;
+        const float cl = have ? a.cosv[k0 + lane] : 0.0f;
+        const float sl = have ? a.sinv[k0 + lane] : 0.0f;
+        const int ntiles = have ? im.ntiles : 0;
+        const int words = (ntiles + 31) >> 5;
+        const unsigned *mk = have ? im.tmask + (size_t)item * words : nullptr;
+        int tg = 0;
+        do {
+            const int tg_n = min(HL_VOTE_TG, ntiles - tg);
+            int total = 0, nruns = 0;
+            if (have) {
+                /* runs of the group's mask words, four words per lane */
+                constexpr int WPL = HL_VOTE_TG / 32 / 32;
+                unsigned m[WPL], st[WPL], en[WPL];
+                int cs = 0, ce = 0;
+#pragma unroll
+                for (int q = 0; q < WPL; q++) {
+                    const int wd = lane * WPL + q;
+                    m[q] = wd * 32 < tg_n ? mk[(tg >> 5) + wd] : 0u;
+                }
+                unsigned prev = __shfl_up_sync(FULL, m[WPL - 1], 1);
+                unsigned next = __shfl_down_sync(FULL, m[0], 1);
+                if (lane == 0)
+                    prev = 0u;
+                if (lane == 31)
+                    next = 0u;
+#pragma unroll
+                for (int q = 0; q < WPL; q++) {
+                    const unsigned pv = q > 0 ? m[q - 1] : prev;
+                    const unsigned nx = q + 1 < WPL ? m[q + 1] : next;
+                    st[q] = m[q] & ~((m[q] << 1) | (pv >> 31));
+                    en[q] = m[q] & ~((m[q] >> 1) | ((nx & 1u) << 31));
+                    cs += __popc(st[q]);
+                    ce += __popc(en[q]);
+                }
+                int is = cs, ie = ce;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t1 = __shfl_up_sync(FULL, is, o);
+                    const int t2 = __shfl_up_sync(FULL, ie, o);
+                    if (lane >= o) {
+                        is += t1;
+                        ie += t2;
+                    }
+                }
+                nruns = __shfl_sync(FULL, is, 31);
+                is -= cs;
+                ie -= ce;
+                /* tile indices of the run ends, then their point offsets
+                 * (four loads in flight per lane) */
+#pragma unroll
+                for (int q = 0; q < WPL; q++) {
+                    const int base = (lane * WPL + q) * 32;
+                    for (unsigned x = st[q]; x; x &= x - 1)
+                        sm.run_s[is++] = base + __ffs(x) - 1;
+                    for (unsigned x = en[q]; x; x &= x - 1)
+                        sm.run_e[ie++] = base + __ffs(x);
+                }
+                __syncwarp();
+                const int *toff = im.tile_off + tg;
+                for (int r0 = 0; r0 < nruns; r0 += 128) {
+                    int vs[4], ve[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const int r = r0 + 32 * u + lane;
+                        if (r < nruns) {
+                            vs[u] = toff[sm.run_s[r]];
+                            ve[u] = toff[sm.run_e[r]];
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const int r = r0 + 32 * u + lane;
+                        if (r < nruns) {
+                            sm.run_s[r] = vs[u];
+                            sm.run_e[r] = ve[u];
+                        }
+                    }
+                }
+                __syncwarp();
+                /* stream positions: a chunk of runs per lane, warp scan */
+                const int per = (nruns + 31) / 32;
+                const int ra = min(nruns, lane * per), rb = min(nruns, ra + per);
+                int sum = 0;
+                for (int r = ra; r < rb; r++)
+                    sum += sm.run_e[r] - sm.run_s[r];
+                int incl = sum;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t1 = __shfl_up_sync(FULL, incl, o);
+                    if (lane >= o)
+                        incl += t1;
+                }
+                int pos = incl - sum;
+                for (int r = ra; r < rb; r++) {
+                    sm.rpre[r] = pos;
+                    pos += sm.run_e[r] - sm.run_s[r];
+                }
+                total = __shfl_sync(FULL, incl, 31);
+                __syncwarp();
+            }
+            const int nb_all = (total + batch - 1) / batch;
+            const int b_lo = (int)((long long)nb_all * part / nparts);
+            const int b_hi = (int)((long long)nb_all * (part + 1) / nparts);
+
+            /* publish the segment once the consumers are done with the one
+             * that last used its slot */
+            const int ds = (int)(nseg & 1u);
+            if (nseg >= 2 &&
+                !mbar_wait_ab(&sm.seg_empty[ds], ((nseg >> 1) - 1u) & 1u, &sm.abort,
+                              a.status)) {
+                ok = false;
+                break;
+            }
+            VoteSeg &g = sm.seg[ds];
+            g.c[lane] = cl;
+            g.s[lane] = sl;
+            if (lane == 0) {
+                g.acc = im.acc;
+                g.item = item;
+                g.part = part;
+                g.nparts = nparts;
+                g.slot = it.z;
+                g.rho_min = im.rho_min;
+                g.R = im.R;
+                g.total = total;
+                g.b_lo = b_lo;
+                g.b_hi = b_hi;
+                g.first = tg == 0;
+                g.last = tg + HL_VOTE_TG >= ntiles;
+            }
+            __syncwarp();
+            if (lane == 0)
+                mbar_arrive(&sm.seg_full[ds]);
+            nseg++;
+            if (!have)
+                break;
+
+            /* batch b is stream range [b * batch, ...): lane i copies the
+             * part of run r0 + i overlapping it; a ballot finds the first run
+             * of the next batch */
+            int r0 = 0;
+            {
+                const int s_first = b_lo * batch;
+                int lo = 0, hi = max(nruns - 1, 0);
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (sm.rpre[mid] + (sm.run_e[mid] - sm.run_s[mid]) <= s_first)
+                        lo = mid + 1;
+                    else
+                        hi = mid;
+                }
+                r0 = lo;
+            }
+            for (int b = b_lo; b < b_hi && ok; b++) {
+                const int slot = (int)(seq % HL_VOTE_SLOTS);
+                if (seq >= HL_VOTE_SLOTS &&
+                    !mbar_wait_ab(&sm.empty[slot], ((seq / HL_VOTE_SLOTS) - 1u) & 1u,
+                                  &sm.abort, a.status)) {
+                    ok = false;
+                    break;
+                }
+                const int s0 = b * batch;
+                const int e0 = min(total, s0 + batch);
+                if (lane == 0)
+                    mbar_expect_tx(&sm.full[slot], (unsigned)(e0 - s0) * 8u);
+                __syncwarp();
+                /* runs from r0 on: every run ending at or before e0 lies
+                 * wholly in this batch; the first one reaching past e0 is
+                 * shared with the next batch and ends the scan */
+                int nextr = nruns;
+                for (int rb = r0; rb < nruns; rb += 32) {
+                    const int r = rb + lane;
+                    bool past = false;
+                    if (r < nruns) {
+                        const int rs = sm.rpre[r];
+                        const int re = rs + (sm.run_e[r] - sm.run_s[r]);
+                        const int ps = max(s0, rs), pe = min(e0, re);
+                        if (pe > ps)
+                            bulk_g2s(&sm.raw[slot][ps - s0], im.pts + sm.run_s[r] + (ps - rs),
+                                     (unsigned)(pe - ps) * 8u, &sm.full[slot]);
+                        past = re > e0;
+                    }
+                    const unsigned pm = __ballot_sync(FULL, past);
+                    if (pm) {
+                        nextr = rb + __ffs(pm) - 1;
+                        break;
+                    }
+                }
+                r0 = nextr;
+                seq++;
+            }
+            tg += HL_VOTE_TG;
+        } while (ok && tg < ntiles);
+        if (!have)
+            break;
+    }
+    if (!ok) {
+        /* gave up: wait (bounded) for the copies still in flight before
+         * the CTA may exit */
+        for (unsigned b = seq - min(seq, (unsigned)HL_VOTE_SLOTS); b < seq; b++)
+            mbar_wait_sleep(&sm.full[b % HL_VOTE_SLOTS], (b / HL_VOTE_SLOTS) & 1u);
+    }
+}
+
 template <bool UNIT>
 __global__ void __launch_bounds__(1024, 1)
 hl_vote_kernel(hl_vote_args a)
@@ -261,291 +578,187 @@ hl_vote_kernel(hl_vote_args a)
     const int batch = 64 * ncons;
     const int nslices = a.Tp / HL_SLICE;
 
+    /* the block and its dump row start at zero; after each item the
+     * consumers clear what it used */
+    {
+        int4 *z = reinterpret_cast<int4 *>(s_acc);
+        for (int i = tid; i < (a.win_rows + 1) * (HL_SLICE / 4); i += nthr)
+            z[i] = make_int4(0, 0, 0, 0);
+    }
     if (tid == 0) {
         for (int i = 0; i < HL_VOTE_SLOTS; i++) {
             mbar_init(&sm.full[i], 1);
             mbar_init(&sm.empty[i], (unsigned)ncons);
         }
+        for (int i = 0; i < 2; i++) {
+            mbar_init(&sm.seg_full[i], 1);
+            mbar_init(&sm.seg_empty[i], (unsigned)ncons);
+        }
+        mbar_init(&sm.cbar, (unsigned)(32 * ncons));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        sm.timeout = 0;
+        sm.abort = 0;
     }
-    /* running batch index, the same sequence on the producer and consumers:
-     * slot = seq % SLOTS, phase = (seq / SLOTS) & 1 */
-    unsigned seq = 0;
+    /* the only block-wide barrier: from here on the producer and the
+     * consumers meet on mbarriers, every wait bounded */
     __syncthreads();
+    if (warp == 0) {
+        vote_producer(a, sm, batch);
+        return;
+    }
 
+    const int cw = warp - 1;
+    const int ctid = tid - 32, nct = nthr - 32;
+    const unsigned acc_l = smem_u32(s_acc) + 4u * lane;
+    int4 *src4 = reinterpret_cast<int4 *>(s_acc);
+    unsigned seq = 0, nseg = 0, cpar = 0;
+    /* the current item */
+    float c = 0.0f, s = 0.0f;
+    int cv = CV_EXACT, vbase = 0, rows = 0, w0 = 0, k0 = 0;
+    unsigned lrows = 0;
+    int32_t *acc_g = nullptr;
+    int nparts = 1, pslot = 0;
     while (true) {
-        if (tid == 0) {
-            const unsigned t = atomicAdd(a.work, 1u) - a.work_base;
-            if (t < (unsigned)a.nitems) {
-                const int2 it = a.items[t];
-                sm.item = it.x & 0xffff;
-                sm.part = it.y;
-                sm.im = a.imgs ? a.imgs[(unsigned)it.x >> 16] : a.img0;
-            } else {
-                sm.item = -1;
-            }
+        const int ds = (int)(nseg & 1u);
+        if (!mbar_wait_ab(&sm.seg_full[ds], (nseg >> 1) & 1u, &sm.abort, a.status))
+            return;
+        nseg++;
+        const VoteSeg &g = sm.seg[ds];
+        const int item = g.item;
+        const int total = g.total, b_lo = g.b_lo, b_hi = g.b_hi;
+        const bool last = g.last;
+        if (item >= 0 && g.first) {
+            const int slice = item % nslices, win = item / nslices;
+            k0 = slice * HL_SLICE;
+            c = g.c[lane];
+            s = g.s[lane];
+            w0 = win * a.win_rows;
+            rows = min(a.win_rows, g.R - w0);
+            const int row_base = g.rho_min + w0;   /* rho bin of local row 0 */
+            lrows = (k0 + lane < a.T) ? (unsigned)rows : 0u;
+            cv = row_base >= 1 ? CV_FLOOR
+                               : (row_base + rows - 1 <= -1 ? CV_CEIL : CV_EXACT);
+            vbase = cv == CV_EXACT ? row_base : RHO_MAGIC_BITS + row_base;
+            acc_g = g.acc;
+            nparts = g.nparts;
+            pslot = g.slot;
         }
-        __syncthreads();
-        const int item = sm.item;
+        __syncwarp();
+        if (lane == 0)
+            mbar_arrive(&sm.seg_empty[ds]);
         if (item < 0)
-            break;
-        const int part = sm.part & 0xffff, nparts = max(sm.part >> 16, 1);
-        const int slice = item % nslices, win = item / nslices;
-        const int k0 = slice * HL_SLICE, k = k0 + lane;
-        const float c = a.cosv[k], s = a.sinv[k];   /* table padded to Tp */
-        const int w0 = win * a.win_rows;
-        const int rows = min(a.win_rows, sm.im.R - w0);
-        const int row_base = sm.im.rho_min + w0;   /* rho bin of local row 0 */
-        const unsigned lrows = (k < a.T) ? (unsigned)rows : 0u;
-        const int cv = row_base >= 1 ? CV_FLOOR
-                       : (row_base + rows - 1 <= -1 ? CV_CEIL : CV_EXACT);
-        const int vbase = cv == CV_EXACT ? row_base : RHO_MAGIC_BITS + row_base;
-        const int klast = min(k0 + HL_SLICE - 1, a.T - 1);
-        const float c0 = a.cosv[k0], s0 = a.sinv[k0];
-        const float c1 = a.cosv[klast], s1 = a.sinv[klast];
-        const float lo_bin = (float)row_base;
-        const float hi_bin = (float)(row_base + rows - 1);
-        const bool filter = sm.im.nwin > 1;
-        const int ntiles = sm.im.ntiles, tiles_x = sm.im.tiles_x;
-        const int img_w = sm.im.w, img_h = sm.im.h;
-        const int *tile_off = sm.im.tile_off;
-        const float2 *pts_g = sm.im.pts;
-        int32_t *acc_g = sm.im.acc;
-        const unsigned acc_l = smem_u32(s_acc) + 4u * lane;
+            return;
 
-        {
-            int4 *z = reinterpret_cast<int4 *>(s_acc);
-            const int4 zero = make_int4(0, 0, 0, 0);
-            for (int i = tid; i < rows * (HL_SLICE / 4); i += nthr)
-                z[i] = zero;
-        }
-
-        for (int tg = 0; tg < ntiles; tg += HL_VOTE_TG) {
-            const int tg_n = min(HL_VOTE_TG, ntiles - tg);
-            /* coarse filter: one bit per tile of the group */
-            for (int wd = warp; wd < HL_VOTE_TG / 32; wd += nwarps) {
-                const int tl = wd * 32 + lane;
-                bool hit = false;
-                if (tl < tg_n)
-                    hit = !filter || tile_hits(tg + tl, tiles_x, img_w, img_h, c0,
-                                               s0, c1, s1, lo_bin, hi_bin,
-                                               a.irho);
-                const unsigned m = __ballot_sync(FULL, hit);
-                if (lane == 0)
-                    sm.mask[wd] = m;
-            }
-            __syncthreads();
-            /* run boundaries per word and their prefix counts (warp 0, four
-             * words per lane) */
-            if (warp == 0) {
-                constexpr int WPL = HL_VOTE_TG / 32 / 32;
-                int cs = 0, ce = 0;
-                unsigned st[WPL], en[WPL];
-#pragma unroll
-                for (int q = 0; q < WPL; q++) {
-                    const int wd = lane * WPL + q;
-                    const unsigned m = sm.mask[wd];
-                    const unsigned prev = (wd > 0) ? sm.mask[wd - 1] : 0u;
-                    const unsigned next = (wd + 1 < HL_VOTE_TG / 32) ? sm.mask[wd + 1] : 0u;
-                    st[q] = m & ~((m << 1) | (prev >> 31));
-                    en[q] = m & ~((m >> 1) | ((next & 1u) << 31));
-                    cs += __popc(st[q]);
-                    ce += __popc(en[q]);
-                }
-                int is = cs, ie = ce;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int t1 = __shfl_up_sync(FULL, is, o);
-                    const int t2 = __shfl_up_sync(FULL, ie, o);
-                    if (lane >= o) {
-                        is += t1;
-                        ie += t2;
-                    }
-                }
-                is -= cs;
-                ie -= ce;
-#pragma unroll
-                for (int q = 0; q < WPL; q++) {
-                    const int wd = lane * WPL + q;
-                    sm.sw[wd] = st[q];
-                    sm.ew[wd] = en[q];
-                    sm.ws[wd] = is;
-                    sm.we[wd] = ie;
-                    is += __popc(st[q]);
-                    ie += __popc(en[q]);
-                }
-                if (lane == 31)
-                    sm.nruns = is;
-            }
-            __syncthreads();
-            /* run endpoints -> point ranges, one tile per thread */
-            for (int tl = tid; tl < tg_n; tl += nthr) {
-                const int wd = tl >> 5, b = tl & 31;
-                const unsigned below = (1u << b) - 1u;
-                if ((sm.sw[wd] >> b) & 1u)
-                    sm.run_s[sm.ws[wd] + __popc(sm.sw[wd] & below)] = tile_off[tg + tl];
-                if ((sm.ew[wd] >> b) & 1u)
-                    sm.run_e[sm.we[wd] + __popc(sm.ew[wd] & below)] = tile_off[tg + tl + 1];
-            }
-            __syncthreads();
-
-            /* stream positions of the runs (warp 0: a chunk of runs per
-             * lane, then a warp scan of the chunk sums) */
-            if (warp == 0) {
-                const int nr = sm.nruns;
-                const int per = (nr + 31) / 32;
-                const int r0 = min(nr, lane * per), r1 = min(nr, r0 + per);
-                int sum = 0;
-                for (int r = r0; r < r1; r++)
-                    sum += sm.run_e[r] - sm.run_s[r];
-                int incl = sum;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int t = __shfl_up_sync(FULL, incl, o);
-                    if (lane >= o)
-                        incl += t;
-                }
-                int pos = incl - sum;
-                for (int r = r0; r < r1; r++) {
-                    sm.rpre[r] = pos;
-                    pos += sm.run_e[r] - sm.run_s[r];
-                }
-                if (lane == 31)
-                    sm.total = incl;
-            }
-            __syncthreads();
-            const int total = sm.total;
-            const int nb_all = (total + batch - 1) / batch;
-            /* this part's share of the batches */
-            const int b_lo = (int)((long long)nb_all * part / nparts);
-            const int b_hi = (int)((long long)nb_all * (part + 1) / nparts);
-            const int nruns = sm.nruns;
-
-            if (warp == 0) {
-                /* producer warp: batch b is stream range [b*CHUNK, ...);
-                 * lane i copies the part of run r0 + i overlapping it, and a
-                 * ballot finds the first run of the next batch */
-                int r0 = 0;
-                {
-                    /* first run ending after this part's first point */
-                    const int s_first = b_lo * batch;
-                    int lo = 0, hi = max(nruns - 1, 0);
-                    while (lo < hi) {
-                        const int mid = (lo + hi) >> 1;
-                        if (sm.rpre[mid] + (sm.run_e[mid] - sm.run_s[mid]) <= s_first)
-                            lo = mid + 1;
-                        else
-                            hi = mid;
-                    }
-                    r0 = lo;
-                }
-                for (int b = b_lo; b < b_hi; b++) {
-                    const int slot = (int)(seq % HL_VOTE_SLOTS);
-                    if (lane == 0 && seq >= HL_VOTE_SLOTS && !*(volatile int *)&sm.timeout &&
-                        !mbar_wait_sleep(&sm.empty[slot], ((seq / HL_VOTE_SLOTS) - 1u) & 1u)) {
-                        sm.timeout = 1;
-                        atomicOr(a.status, HL_ST_VOTE_TIMEOUT);
-                    }
-                    const int s0 = b * batch;
-                    const int e0 = min(total, s0 + batch);
-                    if (lane == 0)
-                        mbar_expect_tx(&sm.full[slot], (unsigned)(e0 - s0) * 8u);
-                    __syncwarp();
-                    /* runs from r0 on: every run ending at or before e0 lies
-                     * wholly in this batch; the first one reaching past e0
-                     * is shared with the next batch and ends the scan (the
-                     * runs after it start at or beyond e0) */
-                    int next = nruns;
-                    for (int rb = r0; rb < nruns; rb += 32) {
-                        const int r = rb + lane;
-                        bool past = false;
-                        if (r < nruns) {
-                            const int rs = sm.rpre[r];
-                            const int re = rs + (sm.run_e[r] - sm.run_s[r]);
-                            const int ps = max(s0, rs), pe = min(e0, re);
-                            if (pe > ps)
-                                bulk_g2s(&sm.raw[slot][ps - s0],
-                                         pts_g + sm.run_s[r] + (ps - rs),
-                                         (unsigned)(pe - ps) * 8u, &sm.full[slot]);
-                            past = re > e0;
-                        }
-                        const unsigned pm = __ballot_sync(FULL, past);
-                        if (pm) {
-                            next = rb + __ffs(pm) - 1;
-                            break;
-                        }
-                    }
-                    r0 = next;
-                    seq++;
-                }
+        /* vote every point of the segment's batches, freeing each slot */
+        for (int b = b_lo; b < b_hi; b++) {
+            const int slot = (int)(seq % HL_VOTE_SLOTS);
+            if (!mbar_wait_ab(&sm.full[slot], (seq / HL_VOTE_SLOTS) & 1u, &sm.abort,
+                              a.status))
+                return;
+            seq++;
+            /* this warp's share: points [64 cw, 64 cw + 64), two 32-point
+             * halves */
+            const int m = min(64, total - b * batch - 64 * cw);
+            const float2 *pts = sm.raw[slot] + 64 * cw;
+            if (cv == CV_FLOOR) {
+                vote_share<UNIT, CV_FLOOR>(pts, m, c, s, a.irho, vbase, acc_l, lrows);
+                vote_share<UNIT, CV_FLOOR>(pts + 32, m - 32, c, s, a.irho, vbase, acc_l, lrows);
+            } else if (cv == CV_CEIL) {
+                vote_share<UNIT, CV_CEIL>(pts, m, c, s, a.irho, vbase, acc_l, lrows);
+                vote_share<UNIT, CV_CEIL>(pts + 32, m - 32, c, s, a.irho, vbase, acc_l, lrows);
             } else {
-                /* consumer warps: vote every point of a batch, then free
-                 * the slot */
-                const int cw = warp - 1;
-                for (int b = b_lo; b < b_hi; b++) {
-                    const int slot = (int)(seq % HL_VOTE_SLOTS);
-                    /* after a time-out nobody waits any more */
-                    const bool ok = *(volatile int *)&sm.timeout ||
-                                    mbar_wait_sleep(&sm.full[slot], (seq / HL_VOTE_SLOTS) & 1u);
-                    if (!ok && lane == 0) {
-                        sm.timeout = 1;
-                        atomicOr(a.status, HL_ST_VOTE_TIMEOUT);
-                    }
-                    seq++;
-                    /* this warp's share: points [64 cw, 64 cw + 64), two
-                     * 32-point halves */
-                    const int m = min(64, total - b * batch - 64 * cw);
-                    const float2 *pts = sm.raw[slot] + 64 * cw;
-                    if (cv == CV_FLOOR) {
-                        vote_share<UNIT, CV_FLOOR>(pts, m, c, s, a.irho, vbase, acc_l, lrows);
-                        vote_share<UNIT, CV_FLOOR>(pts + 32, m - 32, c, s, a.irho, vbase, acc_l, lrows);
-                    } else if (cv == CV_CEIL) {
-                        vote_share<UNIT, CV_CEIL>(pts, m, c, s, a.irho, vbase, acc_l, lrows);
-                        vote_share<UNIT, CV_CEIL>(pts + 32, m - 32, c, s, a.irho, vbase, acc_l, lrows);
-                    } else {
-                        vote_share<UNIT, CV_EXACT>(pts, m, c, s, a.irho, vbase, acc_l, lrows);
-                        vote_share<UNIT, CV_EXACT>(pts + 32, m - 32, c, s, a.irho, vbase, acc_l, lrows);
-                    }
-                    __syncwarp();
-                    if (lane == 0)
-                        mbar_arrive(&sm.empty[slot]);
-                }
+                vote_share<UNIT, CV_EXACT>(pts, m, c, s, a.irho, vbase, acc_l, lrows);
+                vote_share<UNIT, CV_EXACT>(pts + 32, m - 32, c, s, a.irho, vbase, acc_l, lrows);
             }
-            __syncthreads();
+            __syncwarp();
+            if (lane == 0)
+                mbar_arrive(&sm.empty[slot]);
         }
+        if (!last)
+            continue;
 
-        /* store the block: row i of the window -> acc[(w0 + i) * Tp + k0 ..] */
-        int4 *dst4 = reinterpret_cast<int4 *>(acc_g);
-        const int4 *src4 = reinterpret_cast<const int4 *>(s_acc);
+        /* the item is voted: store the block, row i of the window ->
+         * acc[(w0 + i) * Tp + k0 ..], then clear it for the next item */
+        if (!cons_sync(sm, cpar, a.status))
+            return;
+        /* a whole block goes to acc (row 0 of the padding columns, thetas
+         * >= T, holds dumped votes and is stored as zero), a part of a
+         * split block to its scratch slot as it is; each thread stores and
+         * clears the same elements */
         const int tp4 = a.Tp >> 2;
-        /* row 0 of the padding columns (thetas >= T) holds dumped votes */
-        if (nparts == 1) {
-            for (int i = tid; i < rows * (HL_SLICE / 4); i += nthr) {
+        const int n4 = rows * (HL_SLICE / 4);
+        int4 *dst4 = nparts == 1 ? reinterpret_cast<int4 *>(acc_g) + (size_t)w0 * tp4 + (k0 >> 2)
+                                 : a.scratch + (size_t)pslot * a.win_rows * (HL_SLICE / 4);
+        const int dpitch = nparts == 1 ? tp4 : HL_SLICE / 4;
+        for (int i = ctid; i < n4 + HL_SLICE / 4; i += nct) {
+            if (i < n4) {
                 const int rr = i >> 3, q = i & 7;
                 int4 v = src4[i];
-                if (rr == 0) {
+                if (rr == 0 && nparts == 1) {
                     const int kq = k0 + 4 * q;
                     if (kq >= a.T) v.x = 0;
                     if (kq + 1 >= a.T) v.y = 0;
                     if (kq + 2 >= a.T) v.z = 0;
                     if (kq + 3 >= a.T) v.w = 0;
                 }
-                dst4[(size_t)(w0 + rr) * tp4 + (k0 >> 2) + q] = v;
+                dst4[(size_t)rr * dpitch + q] = v;
             }
-        } else {
-            /* one part of a split block: add its nonzero counts into the
-             * zeroed accumulator */
-            for (int i = tid; i < rows * HL_SLICE; i += nthr) {
-                const int v = s_acc[i];
-                if (v && k0 + (i & 31) < a.T)
-                    atomicAdd(&acc_g[(size_t)(w0 + (i >> 5)) * a.Tp + k0 + (i & 31)], v);
-            }
+            src4[i] = make_int4(0, 0, 0, 0);
         }
-        __syncthreads();
-        if (sm.timeout)
-            break;
+        if (!cons_sync(sm, cpar, a.status))
+            return;
     }
+}
+
+/* The blocks voted in parts: block region = sum of its parts' scratch
+ * slots, row 0 of the padding columns (thetas >= T) stored as zero.  One
+ * CTA per 256 int4 of a region (grid.y = region); every slot is read once,
+ * from L2 where the vote launch just wrote it. */
+__global__ void __launch_bounds__(256)
+hl_merge_kernel(hl_merge_args a)
+{
+    const hl_merge_region r = a.regs[blockIdx.y];
+    const int i = blockIdx.x * 256 + threadIdx.x;
+    if (i >= r.rows * (HL_SLICE / 4))
+        return;
+    const int4 *src = a.scratch + (size_t)r.slot0 * a.slot4 + i;
+    int4 v = __ldcg(src);
+    for (int p = 1; p < r.nparts; p++) {
+        const int4 o = __ldcg(src + (size_t)p * a.slot4);
+        v.x += o.x;
+        v.y += o.y;
+        v.z += o.z;
+        v.w += o.w;
+    }
+    const int rr = i >> 3, q = i & 7;
+    if (rr == 0) {
+        const int kq = r.k0 + 4 * q;
+        if (kq >= a.T) v.x = 0;
+        if (kq + 1 >= a.T) v.y = 0;
+        if (kq + 2 >= a.T) v.z = 0;
+        if (kq + 3 >= a.T) v.w = 0;
+    }
+    a.acc[r.off4 + (size_t)rr * a.pitch4 + q] = v;
+}
+
+cudaError_t hl_launch_merge(const hl_merge_args *a, int max_rows, cudaStream_t s)
+{
+    if (a->nreg <= 0)
+        return cudaSuccess;
+    const unsigned gx = (unsigned)((max_rows * (HL_SLICE / 4) + 255) / 256);
+    hl_merge_kernel<<<dim3(gx, (unsigned)a->nreg), 256, 0, s>>>(*a);
+    return cudaGetLastError();
+}
+
+cudaError_t hl_launch_tile_masks(const hl_vote_args *a, int nimg, size_t max_words,
+                                 cudaStream_t s)
+{
+    if (nimg <= 0 || max_words == 0)
+        return cudaSuccess;
+    size_t blocks = (max_words * 32 + 255) / 256;
+    if (blocks > 4096)
+        blocks = 4096;
+    hl_tile_mask_kernel<<<dim3((unsigned)blocks, (unsigned)nimg), 256, 0, s>>>(*a);
+    return cudaGetLastError();
 }
 
 cudaError_t hl_launch_vote(const hl_vote_args *a, int threads, int grid,

@@ -95,6 +95,25 @@ def test_full_4096_against_golden_and_oracle(hl_mod):
     assert [l.astuple() for l in lines] == wl
 
 
+def test_split_blocks_across_geometries(hl_mod):
+    """Heavy (slice, window) blocks are voted in parts that add into their
+    accumulator region, which the compaction launch clears: one handle over a
+    run of geometries (each a different split plan, the first one twice, the
+    accumulator buffer reused) still gives the oracle's accumulator every
+    time."""
+    HoughLine, Image = hl_mod
+    hl = HoughLine(detheta=math.pi / 720)
+    c, s = hl.trig_table()
+    seq = [(4096, 4096, 0, 0), (4096, 4096, 0, 0), (3000, 1800, 0, 0),
+           (2500, 2500, 300, 512), (4096, 4096, 0, 0)]
+    for i, (w, h, rows, threads) in enumerate(seq):
+        img = cases.synth_custom(w, h, 40, 200, 3000, 20000, 50 + i)
+        assert hl.set_vote_shape(rows, threads) == 0
+        acc, _ = hl.accumulator(Image.from_host(img))
+        want, _, _ = O.vote_image(img, c, s)
+        assert np.array_equal(acc.cpu().numpy(), want), (w, h, rows, threads)
+
+
 @pytest.mark.parametrize("rows,threads", [(64, 256), (200, 512), (1000, 1024), (1400, 512)])
 def test_vote_shapes_agree(hl_mod, rows, threads):
     """Rho windows narrower than the rho range exercise the tile filter."""
