@@ -457,9 +457,11 @@ static void block_weights_tiles(const hl_handle *h, int w, int hh, int rho_min,
     }
 }
 
-/* Split plan of the vote blocks (weights wt, ctas persistent CTAs): a block
- * heavier than cap = total / (capf * ctas) is cut into ceil(wt / cap) parts
- * (at most 16).  Then one pass over a list schedule of the parts (each CTA
+/* Split plan of the vote blocks (weights wt in pixels of admitted tiles,
+ * ctas persistent CTAs): a block heavier than cap = total / (capf * ctas) is
+ * cut into ceil(wt / cap) parts (at most 16, none below HL_MIN_PART pixels:
+ * a part's fixed cost -- its scratch slot, written and merged -- would
+ * outweigh its votes).  Then one pass over a list schedule of the parts (each CTA
  * takes the next part, heaviest first, when it is free -- the vote kernel's
  * own order): a part that would start after 60% of the estimated makespan and
  * weighs more than cap / 4 is halved (part p of n becomes parts 2p and 2p + 1
@@ -467,6 +469,7 @@ static void block_weights_tiles(const hl_handle *h, int w, int hh, int rho_min,
  * are small and the CTAs finish together.  Returns the parts heaviest first;
  * pieces[b] counts block b's parts. */
 struct vote_part { double wt; int blk, part, nparts; };
+#define HL_MIN_PART (256.0 * 1024.0)
 static std::vector<vote_part> plan_parts(const std::vector<double> &wt, int ctas,
                                          double capf, std::vector<int> &pieces)
 {
@@ -480,6 +483,7 @@ static std::vector<vote_part> plan_parts(const std::vector<double> &wt, int ctas
         int np = 1;
         if (cap > 0.0 && wt[b] > cap)
             np = std::min(16, (int)ceil(wt[b] / cap));
+        np = std::max(1, std::min(np, (int)(wt[b] / HL_MIN_PART)));
         for (int q = 0; q < np; q++)
             parts.push_back({wt[b] / np, (int)b, q, np});
     }
@@ -503,7 +507,8 @@ static std::vector<vote_part> plan_parts(const std::vector<double> &wt, int ctas
         out.reserve(parts.size() * 2);
         for (size_t i = 0; i < parts.size(); i++) {
             const vote_part &p = parts[i];
-            if (start[i] > 0.6 * makespan && p.wt > 0.25 * cap && p.nparts <= 16) {
+            if (start[i] > 0.6 * makespan && p.wt > 0.25 * cap && p.nparts <= 16 &&
+                p.wt >= 2.0 * HL_MIN_PART) {
                 out.push_back({p.wt / 2, p.blk, 2 * p.part, 2 * p.nparts});
                 out.push_back({p.wt / 2, p.blk, 2 * p.part + 1, 2 * p.nparts});
             } else {
@@ -698,6 +703,7 @@ static int run_ab(hl_handle *h, const hl_roi &roi, const hl_geom &g,
     vote_shape(h, g.numrho, &va.win_rows, &va.img0.nwin, &threads);
     va.irho = (float)(1.0 / h->p.derho);   /* okano_3_0/HoughLine.cu:107 */
     va.status = h->d_counters + 1;
+    va.part16 = hl_part16_ok(h->p.derho, roi.w, roi.h);
     /* persistent CTAs: as many as fit (one per SM at 1024 threads) */
     const size_t smem = hl_vote_smem_bytes(va.win_rows);
     const int per_sm = std::max(1, std::min(2048 / threads,
@@ -763,9 +769,10 @@ static int run_ab(hl_handle *h, const hl_roi &roi, const hl_geom &g,
         ma.pitch4 = h->Tp / 4;
         ma.T = h->T;
         ma.scratch = h->d_scratch;
-        ma.slot4 = (long long)va.win_rows * (HL_SLICE / 4);
+        ma.slot4 = hl_slot4(va.win_rows, va.part16);
         ma.regs = h->d_merge;
         ma.nreg = h->order_nmerge;
+        ma.part16 = va.part16;
         CK(hl_launch_merge(&ma, va.win_rows, s));
         (*launches)++;
     }
@@ -1294,6 +1301,7 @@ struct hl_batch_ws {
     std::vector<int4> items;
     std::vector<hl_merge_region> merge; /* the split blocks */
     int nslots;                    /* scratch slots of their parts */
+    int part16;                    /* 16-bit slots (hl_part16_ok for all) */
     std::vector<size_t> tmask_off; /* each image's first mask word */
     size_t tmask_words, max_mask_words;
     std::vector<int2> chunks;
@@ -1529,6 +1537,9 @@ static int batch_plan(hl_handle *h, hl_batch_ws *b, const hl_image_desc *imgs,
                                     p.part | (p.nparts << 16), slot, 0);
         }
         b->nslots = nslots;
+        b->part16 = 1;
+        for (int i = 0; i < nimg; i++)
+            b->part16 &= hl_part16_ok(h->p.derho, rois[i].w, rois[i].h);
         b->ngroups = groups;
         b->ntiles = tiles;
         b->nitems = (int)b->items.size();
@@ -1683,6 +1694,7 @@ static int batch_enqueue_vote_peaks(hl_handle *h, hl_batch_ws *b, cudaStream_t s
     va.items = reinterpret_cast<const int4 *>(dt + b->off_items);
     va.nitems = b->nitems;
     va.scratch = b->d_scratch;
+    va.part16 = b->part16;
     va.work = reinterpret_cast<unsigned *>(b->d_cnt + 1);
     va.work_base = 0;
     CK(hl_launch_vote(&va, b->threads, b->grid, s));
@@ -1692,9 +1704,10 @@ static int batch_enqueue_vote_peaks(hl_handle *h, hl_batch_ws *b, cudaStream_t s
         ma.pitch4 = h->Tp / 4;
         ma.T = h->T;
         ma.scratch = b->d_scratch;
-        ma.slot4 = (long long)b->win_rows * (HL_SLICE / 4);
+        ma.slot4 = hl_slot4(b->win_rows, b->part16);
         ma.regs = reinterpret_cast<const hl_merge_region *>(dt + b->off_merge);
         ma.nreg = (int)b->merge.size();
+        ma.part16 = b->part16;
         CK(hl_launch_merge(&ma, b->win_rows, s));
     }
     prof_mark(h, 2, s);

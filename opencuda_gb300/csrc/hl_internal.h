@@ -113,6 +113,9 @@ typedef struct hl_vote_args {
     unsigned *work;           /* counter */
     unsigned work_base;       /* its value at launch */
     int4 *scratch;            /* slots of win_rows x HL_SLICE counts */
+    /* nonzero: a slot holds 16-bit counts (two per word; the host sets it
+     * when no bin can reach 2^16 votes, see hl_part16_ok), half the bytes */
+    int part16;
 } hl_vote_args;
 
 /* A split vote block: its accumulator region (rows x 8 int4 from off4, rows
@@ -133,7 +136,25 @@ typedef struct hl_merge_args {
     long long slot4;          /* int4 per scratch slot */
     const hl_merge_region *regs;
     int nreg;
+    int part16;               /* slots hold 16-bit counts (hl_vote_args) */
 } hl_merge_args;
+
+/* Can a split part's counts be kept in 16 bits?  A bin of one rho bin width
+ * derho (the rho-0 bin spans two, truncation toward zero) holds the pixels of
+ * a strip of width <= 2 derho across the ROI: fewer than (2 derho + 2)(w + h)
+ * of them. */
+static inline int hl_part16_ok(double derho, int w, int h)
+{
+    return (2.0 * derho + 2.0) * ((double)w + (double)h) < 65535.0;
+}
+/* int4 per scratch slot of a launch */
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+static inline long long hl_slot4(int win_rows, int part16)
+{
+    return (long long)win_rows * (HL_SLICE / 4) / (part16 ? 2 : 1);
+}
 
 /* Tiles the allocation-free compaction entry point can serve. */
 #define HL_NOALLOC_MAX_TILES 65536

@@ -687,20 +687,27 @@ hl_vote_kernel(hl_vote_args a)
         const int tp4 = a.Tp >> 2;
         const int n4 = rows * (HL_SLICE / 4);
         int4 *dst4 = nparts == 1 ? reinterpret_cast<int4 *>(acc_g) + (size_t)w0 * tp4 + (k0 >> 2)
-                                 : a.scratch + (size_t)pslot * a.win_rows * (HL_SLICE / 4);
-        const int dpitch = nparts == 1 ? tp4 : HL_SLICE / 4;
+                                 : a.scratch + (size_t)pslot * hl_slot4(a.win_rows, a.part16);
+        const bool pack = nparts > 1 && a.part16;
         for (int i = ctid; i < n4 + HL_SLICE / 4; i += nct) {
             if (i < n4) {
                 const int rr = i >> 3, q = i & 7;
                 int4 v = src4[i];
-                if (rr == 0 && nparts == 1) {
-                    const int kq = k0 + 4 * q;
-                    if (kq >= a.T) v.x = 0;
-                    if (kq + 1 >= a.T) v.y = 0;
-                    if (kq + 2 >= a.T) v.z = 0;
-                    if (kq + 3 >= a.T) v.w = 0;
+                if (nparts == 1) {
+                    if (rr == 0) {
+                        const int kq = k0 + 4 * q;
+                        if (kq >= a.T) v.x = 0;
+                        if (kq + 1 >= a.T) v.y = 0;
+                        if (kq + 2 >= a.T) v.z = 0;
+                        if (kq + 3 >= a.T) v.w = 0;
+                    }
+                    dst4[(size_t)rr * tp4 + q] = v;
+                } else if (pack) {
+                    reinterpret_cast<int2 *>(dst4)[i] =
+                        make_int2((v.x & 0xffff) | (v.y << 16), (v.z & 0xffff) | (v.w << 16));
+                } else {
+                    dst4[i] = v;
                 }
-                dst4[(size_t)rr * dpitch + q] = v;
             }
             src4[i] = make_int4(0, 0, 0, 0);
         }
@@ -720,14 +727,25 @@ hl_merge_kernel(hl_merge_args a)
     const int i = blockIdx.x * 256 + threadIdx.x;
     if (i >= r.rows * (HL_SLICE / 4))
         return;
-    const int4 *src = a.scratch + (size_t)r.slot0 * a.slot4 + i;
-    int4 v = __ldcg(src);
-    for (int p = 1; p < r.nparts; p++) {
-        const int4 o = __ldcg(src + (size_t)p * a.slot4);
-        v.x += o.x;
-        v.y += o.y;
-        v.z += o.z;
-        v.w += o.w;
+    int4 v = make_int4(0, 0, 0, 0);
+    if (a.part16) {
+        const int2 *src = reinterpret_cast<const int2 *>(a.scratch + (size_t)r.slot0 * a.slot4) + i;
+        for (int p = 0; p < r.nparts; p++) {
+            const int2 o = __ldcg(src + (size_t)p * 2 * a.slot4);
+            v.x += o.x & 0xffff;
+            v.y += (unsigned)o.x >> 16;
+            v.z += o.y & 0xffff;
+            v.w += (unsigned)o.y >> 16;
+        }
+    } else {
+        const int4 *src = a.scratch + (size_t)r.slot0 * a.slot4 + i;
+        for (int p = 0; p < r.nparts; p++) {
+            const int4 o = __ldcg(src + (size_t)p * a.slot4);
+            v.x += o.x;
+            v.y += o.y;
+            v.z += o.z;
+            v.w += o.w;
+        }
     }
     const int rr = i >> 3, q = i & 7;
     if (rr == 0) {

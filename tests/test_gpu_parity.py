@@ -104,14 +104,17 @@ def test_split_blocks_across_geometries(hl_mod):
     HoughLine, Image = hl_mod
     hl = HoughLine(detheta=math.pi / 720)
     c, s = hl.trig_table()
-    seq = [(4096, 4096, 0, 0), (4096, 4096, 0, 0), (3000, 1800, 0, 0),
-           (2500, 2500, 300, 512), (4096, 4096, 0, 0)]
-    for i, (w, h, rows, threads) in enumerate(seq):
+    # derho 3 at 4096 x 4096: a bin could pass 2^16 votes in principle, so
+    # the parts keep 32-bit counts (16-bit ones everywhere else)
+    seq = [(4096, 4096, 0, 0, 1.0), (4096, 4096, 0, 0, 1.0), (3000, 1800, 0, 0, 1.0),
+           (2500, 2500, 300, 512, 1.0), (4096, 4096, 0, 0, 3.0), (4096, 4096, 0, 0, 1.0)]
+    for i, (w, h, rows, threads, derho) in enumerate(seq):
         img = cases.synth_custom(w, h, 40, 200, 3000, 20000, 50 + i)
         assert hl.set_vote_shape(rows, threads) == 0
+        assert hl.setDeRho(derho) == 0
         acc, _ = hl.accumulator(Image.from_host(img))
-        want, _, _ = O.vote_image(img, c, s)
-        assert np.array_equal(acc.cpu().numpy(), want), (w, h, rows, threads)
+        want, _, _ = O.vote_image(img, c, s, derho)
+        assert np.array_equal(acc.cpu().numpy(), want), (w, h, rows, threads, derho)
 
 
 @pytest.mark.parametrize("rows,threads", [(64, 256), (200, 512), (1000, 1024), (1400, 512)])
