@@ -751,8 +751,17 @@ static int run_ab(hl_handle *h, const hl_roi &roi, const hl_geom &g,
     ca.count = h->d_counters + 2;
     ca.status = h->d_counters + 1;
     prof_mark(h, 0, s);
-    CK(hl_launch_compact(&ca, s));
-    h->ticket_base += (unsigned)((ntiles + HL_COMPACT_GROUP - 1) / HL_COMPACT_GROUP);
+    {
+        /* about one CTA per SM when they fit at once, else one per group */
+        const int nct = hl_compact_persist_ctas(ntiles, h->sms);
+        if (nct > 0) {
+            CK(hl_launch_compact_persist(&ca, nct, s));
+            h->ticket_base += (unsigned)nct;
+        } else {
+            CK(hl_launch_compact(&ca, s));
+            h->ticket_base += (unsigned)((ntiles + HL_COMPACT_GROUP - 1) / HL_COMPACT_GROUP);
+        }
+    }
     (*launches)++;
     prof_mark(h, 1, s);
 
@@ -974,8 +983,17 @@ extern "C" int hl_compact(hl_handle *h, const hl_image_desc *img,
     ca.tile_off = tile_off_dev;
     ca.count = count_dev;
     ca.status = h->d_counters + 1;
-    CK(hl_launch_compact(&ca, s));
-    h->ticket_base += (unsigned)((ntiles + HL_COMPACT_GROUP - 1) / HL_COMPACT_GROUP);
+    {
+        /* about one CTA per SM when they fit at once, else one per group */
+        const int nct = hl_compact_persist_ctas(ntiles, h->sms);
+        if (nct > 0) {
+            CK(hl_launch_compact_persist(&ca, nct, s));
+            h->ticket_base += (unsigned)nct;
+        } else {
+            CK(hl_launch_compact(&ca, s));
+            h->ticket_base += (unsigned)((ntiles + HL_COMPACT_GROUP - 1) / HL_COMPACT_GROUP);
+        }
+    }
     h->last_launches = 1;
     return HL_NO_ERROR;
 }

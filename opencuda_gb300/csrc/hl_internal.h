@@ -219,6 +219,11 @@ typedef struct hl_final_args {
 cudaError_t hl_launch_trig(float *cosv, float *sinv, int T, int Tp,
                            double detheta, cudaStream_t s);
 cudaError_t hl_launch_compact(const hl_compact_args *a, cudaStream_t s);
+/* one image (a->imgs == NULL) with hl_compact_persist_ctas(ntiles, sms) CTAs
+ * in a cooperative launch (0: too many to be resident at once), each adding
+ * one to the ticket word */
+int hl_compact_persist_ctas(int ntiles, int sms);
+cudaError_t hl_launch_compact_persist(const hl_compact_args *a, int nct, cudaStream_t s);
 /* Tile masks of every image of a vote launch (nimg images: a->imgs, or
  * a->img0 when it is NULL); the vote kernel reads them. */
 cudaError_t hl_launch_tile_masks(const hl_vote_args *a, int nimg,

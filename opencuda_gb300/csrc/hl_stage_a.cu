@@ -14,6 +14,8 @@
  * HBM-bound: each image byte is read once (w*h bytes) and each edge point is
  * written once (4 bytes).
  */
+#include <algorithm>
+
 #include "hl_internal.h"
 
 #define FULL 0xffffffffu
@@ -48,6 +50,16 @@ __device__ __forceinline__ uint32_t eq255x4(uint32_t w)
 {
     uint32_t m = __vcmpeq4(w, 0xffffffffu) & 0x80808080u;
     return (m * 0x00204081u) >> 28;
+}
+
+/* The same mask by exact SWAR arithmetic: a byte of ~w is zero exactly when
+ * the byte of w is 0xFF; (b & 0x7F) + 0x7F sets the high bit of every
+ * nonzero low part with no carry between bytes, OR b keeps the rest. */
+__device__ __forceinline__ uint32_t ff_nibble(uint32_t w)
+{
+    const uint32_t t = ~w;
+    const uint32_t nz = (((t & 0x7f7f7f7fu) + 0x7f7f7f7fu) | t) & 0x80808080u;
+    return ((~nz & 0x80808080u) * 0x00204081u) >> 28;
 }
 
 /* Look-back state word: epoch (30 bits) | flag (2 bits) | value (32 bits).
@@ -155,6 +167,7 @@ __device__ int lookback(unsigned long long *state, int tile, int total,
  * trip; here a group waits just for its slowest predecessor to publish, and
  * 256 threads read up to 1024 predecessors in one round trip.  Waits are
  * bounded as in lookback(). */
+template <int NT>
 __device__ int prefix_all(const unsigned long long *state, int g, unsigned epoch,
                           int *status, int *s_red)
 {
@@ -163,16 +176,16 @@ __device__ int prefix_all(const unsigned long long *state, int g, unsigned epoch
     while (true) {
         int sum = 0;
         bool bad = false;
-        for (int j0 = 0; j0 < g; j0 += 4 * HL_COMPACT_THREADS) {
+        for (int j0 = 0; j0 < g; j0 += 4 * NT) {
             unsigned long long st[4];
 #pragma unroll
             for (int u = 0; u < 4; u++) {
-                const int j = j0 + u * HL_COMPACT_THREADS + tid;
+                const int j = j0 + u * NT + tid;
                 st[u] = (j < g) ? lb_load(&state[j]) : 0ull;
             }
 #pragma unroll
             for (int u = 0; u < 4; u++) {
-                const int j = j0 + u * HL_COMPACT_THREADS + tid;
+                const int j = j0 + u * NT + tid;
                 if (j < g) {
                     if ((unsigned)(st[u] >> 34) != epoch || ((st[u] >> 32) & 3u) == 0u)
                         bad = true;
@@ -189,7 +202,7 @@ __device__ int prefix_all(const unsigned long long *state, int g, unsigned epoch
                 s_red[tid >> 5] = sum;
             __syncthreads();
             int t = 0;
-            for (int w = 0; w < HL_COMPACT_THREADS / 32; w++)
+            for (int w = 0; w < NT / 32; w++)
                 t += s_red[w];
             __syncthreads();
             return t;
@@ -333,8 +346,8 @@ hl_compact_kernel(hl_compact_args a)
     }
     __syncthreads();
     if (s_im.ngroups <= LB_FULL_MAX) {
-        const int excl = prefix_all(a.tile_state + s_im.group_base, grp, a.epoch,
-                                    a.status, s_red);
+        const int excl = prefix_all<HL_COMPACT_THREADS>(a.tile_state + s_im.group_base, grp,
+                                                        a.epoch, a.status, s_red);
         if (tid == 0)
             s_excl = excl;
         __syncthreads();
@@ -384,6 +397,268 @@ hl_compact_kernel(hl_compact_args a)
      * 1e30 * cos(theta_k), and cosf of a float angle is never 0 */
     if (a.pts_f2 && tid < CT_GROUP && (s_tcnt[tid] & 1))
         a.pts_f2[s_im.pts_base + s_tbase[tid] + s_tcnt[tid]] = make_float2(1.0e30f, 0.0f);
+}
+
+/* Single-image compaction with few, large CTAs: CTA c of nct takes tiles [ntiles c / nct, ntiles (c + 1) / nct) -- at most CP_MAXT --
+ * with every one of its 16-byte loads in flight at once, in row order across
+ * its tiles; turns them into 16-bit masks of 255-pixels in tile-major order
+ * (chunk u = tile * 256 + row * 8 + column chunk, via shared memory), ranks
+ * them with one block scan (a thread owns one 128-pixel row of a tile),
+ * publishes one count, meets the other CTAs at one grid barrier (a
+ * cooperative launch: all CTAs resident) and sums its predecessors' counts
+ * in one read -- no polling of every predecessor, whose traffic grows with
+ * the square of the CTA count -- then scatters one 16-pixel chunk per
+ * thread.  Output as hl_compact_kernel:
+ * tile-major, raster order inside a tile, odd float2 tiles padded. */
+#define CP_THREADS 1024
+#define CP_MAXT 32
+#define CP_K (CP_MAXT * 256 / CP_THREADS)
+
+/* tile range of CTA c of nct and the divisor of its row-order load index */
+struct CpRange {
+    int t0, nt, nu;
+    unsigned rowlen, magic;
+};
+__device__ __forceinline__ CpRange cp_range(const hl_compact_args &a, int c, int nct)
+{
+    CpRange r;
+    r.t0 = (int)((long long)a.ntiles * c / nct);
+    r.nt = (int)((long long)a.ntiles * (c + 1) / nct) - r.t0;
+    r.nu = r.nt * 256;
+    r.rowlen = 8u * (unsigned)r.nt;
+    r.magic = 0xffffffffu / r.rowlen + 1u;
+    return r;
+}
+
+__global__ void __launch_bounds__(CP_THREADS, 1)
+hl_compact_persist_kernel(hl_compact_args a, int nct)
+{
+    __shared__ int s_wsum[CP_THREADS / 32];
+    __shared__ int s_tstart[CP_MAXT + 1];   /* point rank at each tile start */
+    __shared__ int s_tbase[CP_MAXT];        /* tile offsets within the CTA */
+    __shared__ int s_x0[CP_MAXT], s_y0[CP_MAXT];
+    __shared__ int s_total, s_excl;
+    __shared__ int s_red[CP_THREADS / 32];
+    __shared__ __align__(16) unsigned short s_mask[CP_MAXT * 256];
+    __shared__ unsigned short s_rowrel[CP_MAXT * 32];   /* row start in its tile */
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    /* a cooperative launch: every CTA is resident, so the CTA index orders
+     * the prefix and the grid barrier below always completes */
+    const int c = blockIdx.x;
+    const CpRange R = cp_range(a, c, nct);
+    const int nt = R.nt, nu = R.nu;
+    if (tid < nt) {
+        s_x0[tid] = ((R.t0 + tid) % a.tiles_x) * HL_TILE_W;
+        s_y0[tid] = ((R.t0 + tid) / a.tiles_x) * HL_TILE_H;
+    }
+    __syncthreads();
+
+    /* loads in row order across the CTA's tiles (load index L = r * 8 nt +
+     * tile * 8 + column chunk: a warp reads 512 contiguous bytes of a row),
+     * all in flight before any is used; r = L / (8 nt) by a multiply-high,
+     * exact for L * 8 nt < 2^32 */
+    uint4 v[CP_K];
+#pragma unroll
+    for (int k = 0; k < CP_K; k++) {
+        v[k] = make_uint4(0, 0, 0, 0);
+        const int L = tid + k * CP_THREADS;
+        if (L < nu) {
+            const int r = (int)__umulhi((unsigned)L, R.magic);
+            const int rem = L - r * (int)R.rowlen;
+            const int x = s_x0[rem >> 3] + (rem & 7) * 16;
+            const int y = s_y0[rem >> 3] + r;
+            const uint8_t *p = a.roi.base + (size_t)y * (size_t)a.roi.pitch + x;
+            if (y < a.roi.h && x + 16 <= a.roi.w && (((uintptr_t)p) & 15u) == 0)
+                v[k] = __ldcs((const uint4 *)p);
+        }
+    }
+    /* 16-bit masks of 255-pixels, handed to the tile-major order through
+     * shared memory (chunk u = tile * 256 + r * 8 + column chunk) */
+#pragma unroll
+    for (int k = 0; k < CP_K; k++) {
+        const int L = tid + k * CP_THREADS;
+        if (L < nu) {
+            const int r = (int)__umulhi((unsigned)L, R.magic);
+            const int rem = L - r * (int)R.rowlen;
+            const int tl = rem >> 3, ch = rem & 7;
+            const int x = s_x0[tl] + ch * 16;
+            const int y = s_y0[tl] + r;
+            uint32_t mm = 0;
+            if (y < a.roi.h && x < a.roi.w) {
+                const uint8_t *p = a.roi.base + (size_t)y * (size_t)a.roi.pitch + x;
+                if (x + 16 <= a.roi.w && (((uintptr_t)p) & 15u) == 0) {
+                    mm = ff_nibble(v[k].x) | (ff_nibble(v[k].y) << 4) |
+                         (ff_nibble(v[k].z) << 8) | (ff_nibble(v[k].w) << 12);
+                } else {
+                    const int lim = min(16, a.roi.w - x);
+                    for (int i = 0; i < lim; i++)
+                        mm |= (uint32_t)(p[i] == 255) << i;
+                }
+            }
+            s_mask[tl * 256 + r * 8 + ch] = (unsigned short)mm;
+        }
+    }
+    __syncthreads();
+    /* ranks in tile-major order: thread tid owns row tid % 32 of tile
+     * tid / 32 (chunks 8 tid .. 8 tid + 7, one 16-byte shared load); one
+     * block scan of the rows' counts */
+    const bool owner = tid * 8 < nu;
+    int cnt = 0;
+    if (owner) {
+        const uint4 q = reinterpret_cast<const uint4 *>(s_mask)[tid];
+        cnt = __popc(q.x) + __popc(q.y) + __popc(q.z) + __popc(q.w);
+    }
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o)
+            incl += t;
+    }
+    if (lane == 31)
+        s_wsum[warp] = incl;
+    __syncthreads();
+    {
+        const int ws = s_wsum[lane];
+        int wi = ws;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(FULL, wi, o);
+            if (lane >= o)
+                wi += t;
+        }
+        incl += __shfl_sync(FULL, wi - ws, warp);   /* block-inclusive */
+        if (tid == CP_THREADS - 1)
+            s_tstart[nt] = incl;
+    }
+    const int base = incl - cnt;   /* rank of this row's first point */
+    if (owner && (tid & 31) == 0)
+        s_tstart[tid >> 5] = base;
+    __syncthreads();
+    if (owner)
+        s_rowrel[tid] = (unsigned short)(base - s_tstart[tid >> 5]);
+    /* tile offsets within the CTA (float2 output pads odd tiles); the CTA's
+     * count is published, then one grid barrier (an arrival counter on the
+     * ticket word, bounded spin) and one read of the predecessors' counts */
+    const int pad = a.pts_f2 ? 1 : 0;
+    if (warp == 0) {
+        int cq = 0;
+        if (lane < nt)
+            cq = s_tstart[lane + 1] - s_tstart[lane];
+        const int pq = cq + (cq & pad);
+        int ti = pq;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(FULL, ti, o);
+            if (lane >= o)
+                ti += t;
+        }
+        if (lane < nt)
+            s_tbase[lane] = ti - pq;
+        const int total = __shfl_sync(FULL, ti, 31);
+        if (lane == 0) {
+            s_total = total;
+            lb_store(&a.tile_state[c], lb_pack(a.epoch, LB_AGG, (unsigned)total));
+            __threadfence();
+            atomicAdd(a.ticket, 1u);
+            const unsigned target = a.ticket_base + (unsigned)nct;
+            int spins = 0;
+            while ((int)(*(volatile unsigned *)a.ticket - target) < 0) {
+                if (++spins > LB_SPIN_LIMIT) {
+                    atomicOr(a.status, HL_ST_LOOKBACK_TIMEOUT);
+                    break;
+                }
+                __nanosleep(32);
+            }
+            __threadfence();
+        }
+    }
+    __syncthreads();
+    {
+        int sum = 0;
+        for (int j = tid; j < c; j += CP_THREADS)
+            sum += (int)(unsigned)(lb_load(&a.tile_state[j]) & 0xffffffffu);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            sum += __shfl_xor_sync(FULL, sum, o);
+        if (lane == 0)
+            s_red[warp] = sum;
+        __syncthreads();
+        if (tid == 0) {
+            int t = 0;
+            for (int w = 0; w < CP_THREADS / 32; w++)
+                t += s_red[w];
+            s_excl = t;
+        }
+        __syncthreads();
+    }
+    const int excl = s_excl;
+    if (tid < nt)
+        a.tile_off[R.t0 + tid] = excl + s_tbase[tid];
+    if (c == nct - 1 && tid == 0) {
+        a.tile_off[a.ntiles] = excl + s_total;
+        *a.count = excl + s_total;
+    }
+    /* scatter, one 16-pixel chunk per thread and round (chunk u = tid +
+     * 1024 k): its rank is its row's start plus the points of the row's
+     * chunks before it */
+#pragma unroll
+    for (int k = 0; k < CP_K; k++) {
+        const int u = tid + k * CP_THREADS;
+        if (u >= nu)
+            break;
+        uint32_t mm = s_mask[u];
+        if (!mm)
+            continue;
+        const int row = u >> 3, ch = u & 7, tl = u >> 8;
+        const uint4 q = reinterpret_cast<const uint4 *>(s_mask)[row];
+        const unsigned long long lo = (unsigned long long)q.x | ((unsigned long long)q.y << 32);
+        const unsigned long long hi = (unsigned long long)q.z | ((unsigned long long)q.w << 32);
+        const int nb = 16 * ch;
+        const int before = nb >= 64 ? __popcll(lo) + __popcll(hi & ((1ull << (nb - 64)) - 1ull))
+                                    : __popcll(lo & ((1ull << nb) - 1ull));
+        int pos = excl + s_tbase[tl] + s_rowrel[row] + before;
+        const int x = s_x0[tl] + 16 * ch;
+        const int y = s_y0[tl] + (row & 31);
+        while (mm) {
+            const int bb = __ffs(mm) - 1;
+            mm &= mm - 1;
+            if (a.pts_f2)
+                a.pts_f2[pos] = make_float2((float)(x + bb), (float)y);
+            else
+                a.pts[pos] = (uint32_t)(x + bb) | ((uint32_t)y << 16);
+            pos++;
+        }
+    }
+    /* the sentinel (1e30, 0) of an odd float2 tile never votes inside an
+     * accumulator (see hl_compact_kernel) */
+    if (pad && tid < nt) {
+        const int cq = s_tstart[tid + 1] - s_tstart[tid];
+        if (cq & 1)
+            a.pts_f2[excl + s_tbase[tid] + cq] = make_float2(1.0e30f, 0.0f);
+    }
+}
+
+/* CTAs of the single-image compaction: about one per SM, at most CP_MAXT
+ * tiles each; 0 when that needs more CTAs than can be resident at once
+ * (callers then use hl_launch_compact) */
+int hl_compact_persist_ctas(int ntiles, int sms)
+{
+    const int need = (ntiles + CP_MAXT - 1) / CP_MAXT;
+    const int nct = std::max(1, std::min(ntiles, std::max(sms, need)));
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hl_compact_persist_kernel,
+                                                      CP_THREADS, 0) != cudaSuccess)
+        return 0;
+    return nct <= per_sm * sms ? nct : 0;
+}
+
+cudaError_t hl_launch_compact_persist(const hl_compact_args *a, int nct, cudaStream_t s)
+{
+    hl_compact_args args = *a;
+    void *params[] = {&args, &nct};
+    return cudaLaunchCooperativeKernel((const void *)hl_compact_persist_kernel, dim3(nct),
+                                       dim3(CP_THREADS), params, 0, s);
 }
 
 cudaError_t hl_launch_compact(const hl_compact_args *a, cudaStream_t s)

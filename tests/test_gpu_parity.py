@@ -152,6 +152,30 @@ def test_compaction_points_and_order(hl_mod):
     assert o[0] == 0 and o[-1] == n and np.all(np.diff(o) >= 0)
 
 
+@pytest.mark.parametrize("w,h", [(4096, 4096), (8192, 2560), (1000, 37)])
+def test_compaction_large_and_fallback(hl_mod, w, h):
+    """About one CTA per SM (a cooperative launch) up to the tiles that many
+    CTAs can hold, one CTA per 4-tile group beyond (8192 x 2560 has 5120
+    tiles): the same points, order and tile offsets either way."""
+    HoughLine, Image = hl_mod
+    img = cases.synth_custom(w, h, 30, 100, 4000, 25000, 77)
+    hl = HoughLine()
+    for _ in range(2):
+        pts, offs, cnt = hl.compact(Image.from_host(img))
+        n = int(cnt.item())
+        assert n == int((img == 255).sum())
+        p = pts[:n].cpu().numpy().astype(np.uint32)
+        xs, ys = (p & 0xFFFF).astype(np.int64), (p >> 16).astype(np.int64)
+        assert np.all(img[ys, xs] == 255)
+        tiles_x = (w + 127) // 128
+        key = ((ys // 32) * tiles_x + xs // 128) * 4096 + (ys % 32) * 128 + xs % 128
+        assert np.all(np.diff(key) > 0)
+        o = offs.cpu().numpy()
+        tile = (ys // 32) * tiles_x + xs // 128
+        want = np.searchsorted(tile, np.arange(len(o) - 1))
+        assert np.array_equal(o[:-1], want) and o[-1] == n
+
+
 def test_compaction_unaligned_and_repeat(hl_mod):
     """Misaligned ROI origins take the scalar path; repeated calls reuse the
     epoch-tagged look-back state without clearing it."""
