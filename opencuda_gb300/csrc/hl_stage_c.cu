@@ -29,28 +29,6 @@
 #define FIN_CHUNK 1024
 #define FIN_SCACHE 1024
 
-/* append one peak key (warp-aggregated: one global atomic per warp) */
-__device__ __forceinline__ void push_key(bool is, unsigned long long key,
-                                         const hl_peak_img &im, int *status)
-{
-    const int lane = threadIdx.x & 31;
-    const unsigned b = __ballot_sync(FULL, is);
-    if (!b)
-        return;
-    const int leader = __ffs(b) - 1;
-    int base = 0;
-    if (lane == leader)
-        base = atomicAdd(im.ncand, __popc(b));
-    base = __shfl_sync(FULL, base, leader);
-    if (is) {
-        const int pos = base + __popc(b & ((1u << lane) - 1u));
-        if (pos < im.cap)
-            im.keys[pos] = key;
-        else
-            atomicOr(status, HL_ST_CAND_OVERFLOW);
-    }
-}
-
 /* Chunks of HL_PEAK_ROWS accumulator rows of one image each, taken
  * grid-stride; one thread per 4 consecutive bins of a row (one 16-byte
  * streaming load).  The neighbours are read only for bins above the
@@ -86,31 +64,87 @@ __global__ void __launch_bounds__(256) hl_peaks_kernel(hl_peak_args a)
             }
             if (!__any_sync(FULL, cand != 0u))
                 continue;
-#pragma unroll 1
-            for (int i = 0; i < 16; i++) {
-                const int u = i >> 2, q = i & 3;
-                const int e = e0 + u * blockDim.x + threadIdx.x;
-                bool is = false;
-                unsigned long long key = 0;
-                if ((cand >> i) & 1u) {
-                    const int row = row0 + e / q4;
-                    const int k = (e % q4) * 4 + q;
-                    if (k < a.T) {
-                        const int32_t *p = im.acc + (size_t)row * a.Tp + k;
-                        const int x = p[0];
-                        const int W = (k > 0) ? p[-1] : 0;
-                        const int E = (k + 1 < a.T) ? p[1] : 0;
-                        const int N = (row > 0) ? p[-a.Tp] : 0;
-                        const int S = (row + 1 < im.R) ? p[a.Tp] : 0;
-                        /* okano_3_0/HoughLine.cu:195-199 */
-                        if (x > W && x >= E && x > N && x >= S) {
-                            is = true;
-                            const unsigned idx = (unsigned)row * (unsigned)a.T + (unsigned)k;
-                            key = ((unsigned long long)(unsigned)x << 32) | (unsigned)(~idx);
+            /* rare path: the neighbours of every candidate -- the int4 rows
+             * above and below and the two edge bins -- loaded two groups at
+             * a time, the peak rule (okano_3_0/HoughLine.cu:195-199) from
+             * registers, then one aggregated append for the warp */
+            unsigned peak = 0u;
+#pragma unroll
+            for (int h = 0; h < 4; h += 2) {
+                int4 up[2], dn[2];
+                int wv[2], ev[2];
+#pragma unroll
+                for (int g = 0; g < 2; g++) {
+                    const int u = h + g;
+                    const int e = e0 + u * blockDim.x + threadIdx.x;
+                    const int rl = e / q4, row = row0 + rl, kq = (e - rl * q4) * 4;
+                    const bool any = ((cand >> (4 * u)) & 15u) != 0u;
+                    const int32_t *p = im.acc + (size_t)row * a.Tp + kq;
+                    up[g] = (any && row > 0) ? *reinterpret_cast<const int4 *>(p - a.Tp)
+                                             : make_int4(0, 0, 0, 0);
+                    dn[g] = (any && row + 1 < im.R) ? *reinterpret_cast<const int4 *>(p + a.Tp)
+                                                   : make_int4(0, 0, 0, 0);
+                    wv[g] = (any && kq > 0) ? p[-1] : 0;
+                    ev[g] = (any && kq + 4 < a.T) ? p[4] : 0;
+                }
+#pragma unroll
+                for (int g = 0; g < 2; g++) {
+                    const int u = h + g;
+                    const int e = e0 + u * blockDim.x + threadIdx.x;
+                    const int rl = e / q4, kq = (e - rl * q4) * 4;
+                    const int xv[4] = {v4[u].x, v4[u].y, v4[u].z, v4[u].w};
+                    const int nv[4] = {up[g].x, up[g].y, up[g].z, up[g].w};
+                    const int sv[4] = {dn[g].x, dn[g].y, dn[g].z, dn[g].w};
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const int k = kq + q;
+                        if (((cand >> (4 * u + q)) & 1u) && k < a.T) {
+                            const int x = xv[q];
+                            const int W = k > 0 ? (q > 0 ? xv[q - 1] : wv[g]) : 0;
+                            const int E = k + 1 < a.T ? (q < 3 ? xv[q + 1] : ev[g]) : 0;
+                            if (x > W && x >= E && x > nv[q] && x >= sv[q])
+                                peak |= 1u << (4 * u + q);
                         }
                     }
                 }
-                push_key(is, key, im, a.status);
+            }
+            /* append: one atomic per warp, each lane writes its keys */
+            const int lane = threadIdx.x & 31;
+            const int cnt = __popc(peak);
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o)
+                    incl += t;
+            }
+            const int wtot = __shfl_sync(FULL, incl, 31);
+            if (wtot == 0)
+                continue;
+            int base = 0;
+            if (lane == 31)
+                base = atomicAdd(im.ncand, wtot);
+            base = __shfl_sync(FULL, base, 31) + incl - cnt;
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                if (!((peak >> (4 * u)) & 15u))
+                    continue;
+                const int e = e0 + u * blockDim.x + threadIdx.x;
+                const int rl = e / q4;
+                const int row = row0 + rl, kq = (e - rl * q4) * 4;
+                const int xv[4] = {v4[u].x, v4[u].y, v4[u].z, v4[u].w};
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    if ((peak >> (4 * u + q)) & 1u) {
+                        const unsigned idx = (unsigned)row * (unsigned)a.T + (unsigned)(kq + q);
+                        if (base < im.cap)
+                            im.keys[base] = ((unsigned long long)(unsigned)xv[q] << 32) |
+                                            (unsigned)(~idx);
+                        else
+                            atomicOr(a.status, HL_ST_CAND_OVERFLOW);
+                        base++;
+                    }
+                }
             }
         }
     }
