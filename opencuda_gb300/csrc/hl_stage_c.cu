@@ -24,6 +24,9 @@
 
 #include <algorithm>
 
+#include <cooperative_groups.h>
+namespace cg = cooperative_groups;
+
 #define FULL 0xffffffffu
 #define FIN_THREADS 1024
 #define FIN_CHUNK 1024
@@ -236,13 +239,238 @@ __device__ __forceinline__ void decode(unsigned long long key, int T,
     *votes = (int)(key >> 32);
 }
 
-__global__ void __launch_bounds__(FIN_THREADS)
-hl_finalize_kernel(hl_final_args a, float scale)
+/* Predecessor bitmask of a sorted, decoded chunk of m candidates: bit j of
+ * pred[i][j / 32] <=> j < i and similar(j, i).  Only the words holding some
+ * j < i are built: entry (i, wd) for 32 wd < i, enumerated word by word.
+ * Four adjacent threads share an entry (8 tests each, OR-ed by shuffles);
+ * the threads of a warp mostly share wd and read the word's candidates with
+ * broadcast loads.  Threads t0, t0 + step, ... (step a multiple of 32) take
+ * the entries; pred may be another CTA's shared memory of the cluster. */
+__device__ __forceinline__ void build_pred(const FinSmem &sm, int m, const hl_final_args &a,
+                                           int t0, int step,
+                                           unsigned (*pred)[FIN_CHUNK / 32 + 1])
 {
-    extern __shared__ __align__(16) unsigned char fin_raw[];
-    FinSmem &sm = *reinterpret_cast<FinSmem *>(fin_raw);
+    const int W = (m + 31) >> 5;
+    int nent = 0;
+    for (int wd = 0; wd < W; wd++)
+        nent += max(0, m - 32 * wd - 1);
+    const int span = (4 * nent + 31) & ~31;
+    for (int e = t0; e < span; e += step) {
+        const int q = e & 3, en = e >> 2;
+        unsigned bits = 0u;
+        int i = 0, wd = 0, jn = 0;
+        if (en < nent) {
+            int rem = en;
+            while (rem >= m - 32 * wd - 1) {
+                rem -= m - 32 * wd - 1;
+                wd++;
+            }
+            i = 32 * wd + 1 + rem;
+            jn = min(32, i - (wd << 5));
+        }
+        {
+            /* every lane runs the same 8 tests (invalid ones masked
+             * afterwards), so the rare exact wrap-around test is a
+             * warp-uniform branch */
+            const int j0 = wd << 5;
+            const float ai = sm.ang[i];
+            const int di = sm.dist[i];
+#pragma unroll
+            for (int b = 8 * q; b < 8 * q + 8; b++) {
+                const int j = min(j0 + b, m - 1);
+                const float aj = sm.ang[j];
+                const int dj = sm.dist[j];
+                const bool same = (abs(dj - di) < a.thresdis) &
+                                  (fabsf(__fsub_rn(aj, ai)) < a.thresang);
+                const bool near = abs(dj + di) < a.thresdis;
+                const float est = fabsf(__fsub_rn(__fsub_rn(3.14159265f, aj), ai));
+                const bool lo = est < a.thresang - 1e-6f;
+                const bool hi = est > a.thresang + 1e-6f;
+                bool wrap = near & lo;
+                const bool amb = near & !lo & !hi & (b < jn);
+                if (__any_sync(FULL, amb)) {
+                    if (amb)
+                        wrap = wrap_exact(aj, ai, a.thresang);
+                }
+                bits |= (unsigned)((same | wrap) & (b < jn)) << b;
+            }
+        }
+        bits |= __shfl_xor_sync(FULL, bits, 1);
+        bits |= __shfl_xor_sync(FULL, bits, 2);
+        if (en < nent && q == 0)
+            pred[i][wd] = bits;
+    }
+}
+
+/* Rank sort of keys[0, m) into sorted[] (descending): keys are unique (the
+ * bin index is part of every key), so a key's rank is the number of larger
+ * keys.  tpk consecutive threads (a power of two, as many as the threads
+ * allow) rank one key, each against every tpk-th key, then sum by shuffles.
+ * Keys [k_lo, k_hi) are ranked by threads [0, nthr); out[d] receives them
+ * for d < ndst (several CTAs' arrays of a cluster). */
+__device__ __forceinline__ void rank_keys(const unsigned long long *keys, int m, int k_lo,
+                                          int k_hi, int nthr,
+                                          unsigned long long *const *out, int ndst)
+{
     const int tid = threadIdx.x;
-    const hl_final_img im = a.imgs ? a.imgs[blockIdx.x] : a.img0;  /* CTA = image */
+    const int mk = k_hi - k_lo;
+    if (mk <= 0)
+        return;
+    int tpk = 1;
+    while (tpk < 32 && 2 * tpk * mk <= nthr)
+        tpk <<= 1;
+    const int per = nthr / tpk;
+    const int part = tid & (tpk - 1);
+    for (int i0 = 0; i0 < mk; i0 += per) {
+        const int i = k_lo + i0 + tid / tpk;
+        const bool have = i < k_hi;
+        const unsigned long long ki = have ? keys[i] : 0ull;
+        int rank = 0;
+        if (have) {
+            int j = part;
+            for (; j + 3 * tpk < m; j += 4 * tpk)
+                rank += (keys[j] > ki) + (keys[j + tpk] > ki) + (keys[j + 2 * tpk] > ki) +
+                        (keys[j + 3 * tpk] > ki);
+            for (; j < m; j += tpk)
+                rank += keys[j] > ki;
+        }
+        for (int o = tpk >> 1; o > 0; o >>= 1)
+            rank += __shfl_xor_sync(FULL, rank, o);
+        if (have && part == 0)
+            for (int d = 0; d < ndst; d++)
+                out[d][rank] = ki;
+    }
+}
+
+/* The greedy pass and the output of one sorted, decoded chunk whose
+ * predecessor bitmask and `removed` words are built; S lines are already
+ * written.  Returns the number of lines this chunk adds. */
+__device__ int greedy_chunk(FinSmem &sm, const hl_final_img &im, int m, int K, int S)
+{
+    const int tid = threadIdx.x;
+    const int W = (m + 31) >> 5;
+    /* The greedy pass of okano_3_0/HoughLine.cu:900-927 keeps candidate i
+     * iff it was not removed by an earlier chunk and no earlier kept
+     * candidate is similar to it.  Resolved in rounds: an undecided
+     * candidate with a kept predecessor is dropped, one whose
+     * predecessors are all decided (none kept) is kept.  Each round
+     * decides at least the first undecided candidate; in practice a few
+     * rounds decide them all. */
+    if (tid < 32) {
+        unsigned d = (tid < W) ? sm.removed[tid] : 0xffffffffu;
+        if (tid == W - 1 && (m & 31))
+            d |= ~((1u << (m & 31)) - 1u);
+        sm.dec[tid] = d;
+        sm.alive[tid] = 0u;
+        sm.ndec[tid] = 0u;
+        sm.nalive[tid] = 0u;
+    }
+    __syncthreads();
+    for (int round = 0; round < m; round++) {
+        for (int i = tid; i < m; i += blockDim.x) {
+            const int iw = i >> 5;
+            const unsigned ib = 1u << (i & 31);
+            if (sm.dec[iw] & ib)
+                continue;
+            bool all = true, kill = false;
+            for (int w = 0; w < ((i + 31) >> 5); w++) {
+                const unsigned pw = sm.pred[i][w];
+                all = all && !(pw & ~sm.dec[w]);
+                kill = kill || (pw & sm.alive[w]);
+            }
+            if (kill) {
+                atomicOr(&sm.ndec[iw], ib);
+            } else if (all) {
+                atomicOr(&sm.ndec[iw], ib);
+                atomicOr(&sm.nalive[iw], ib);
+            }
+        }
+        __syncthreads();
+        if (tid < 32) {
+            const unsigned d = sm.dec[tid] | sm.ndec[tid];
+            sm.dec[tid] = d;
+            sm.alive[tid] |= sm.nalive[tid];
+            sm.ndec[tid] = 0u;
+            sm.nalive[tid] = 0u;
+            const bool done = __all_sync(FULL, d == 0xffffffffu);
+            if (tid == 0)
+                sm.misc[4] = done;
+        }
+        __syncthreads();
+        if (sm.misc[4])
+            break;
+    }
+    /* survivors in rank order, at most room of them */
+    {
+        const int room = K - S;
+        for (int i = tid; i < m; i += blockDim.x) {
+            const int iw = i >> 5;
+            const unsigned al = sm.alive[iw];
+            if ((al >> (i & 31)) & 1u) {
+                int q = __popc(al & ((1u << (i & 31)) - 1u));
+                for (int w = 0; w < iw; w++)
+                    q += __popc(sm.alive[w]);
+                if (q < room)
+                    sm.surv[q] = i;
+            }
+        }
+        if (tid < 32) {
+            int c = __popc(sm.alive[tid]);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                c += __shfl_xor_sync(FULL, c, o);
+            if (tid == 0)
+                sm.misc[3] = min(c, room);
+        }
+    }
+    __syncthreads();
+    const int ns = sm.misc[3];
+    for (int q = tid; q < ns; q += blockDim.x) {
+        const int i = sm.surv[q];
+        const int o = S + q;
+        hl_line L;
+        L.angle = sm.ang[i];
+        L.distance = sm.dist[i];
+        L.votes = sm.votes[i];
+        im.lines[o] = L;
+        if (o < FIN_SCACHE) {
+            sm.sang[o] = L.angle;
+            sm.sdist[o] = L.distance;
+        }
+    }
+    __syncthreads();
+    return ns;
+}
+
+/* thread 0 after the last chunk: the line count, the candidate counter
+ * cleared for the next call, overflow and status reporting */
+__device__ void finalize_report(const hl_final_args &a, const hl_final_img &im, int S,
+                                int ncand_raw)
+{
+    const int K = a.linesmax;
+    const int cnt = (K > 0) ? S : K;
+    if (im.count_out)
+        *im.count_out = cnt;
+    *im.ncand = 0;
+    if (ncand_raw > im.cap)
+        atomicOr(a.status, HL_ST_CAND_OVERFLOW);
+    if (a.hdr) {   /* one image: report and clear the status word */
+        int st = *a.status;
+        if (ncand_raw > im.cap)
+            st |= HL_ST_CAND_OVERFLOW;
+        a.hdr->count = cnt;
+        a.hdr->status = st;
+        a.hdr->ncand = ncand_raw;
+        *a.status = 0;
+    }
+}
+
+/* One CTA, one image: the whole tail (okano_3_0/HoughLine.cu:837-948) in
+ * chunks of FIN_CHUNK keys. */
+__device__ void finalize_cta(const hl_final_args &a, const hl_final_img &im, float scale,
+                             FinSmem &sm)
+{
+    const int tid = threadIdx.x;
     const int ncand_raw = *im.ncand;
     const int n = min(ncand_raw, im.cap);
     const int K = a.linesmax;
@@ -301,43 +529,16 @@ hl_finalize_kernel(hl_final_args a, float scale)
             }
             __syncthreads();
         }
-        /* descending order by rank: keys are unique (the bin index is part of
-         * every key), so a key's rank is the number of larger keys.  tpk
-         * consecutive threads (a power of two, as many as the block allows)
-         * rank one key, each against every tpk-th key, then sum by shuffles */
         __syncthreads();
         {
-            int tpk = 1;
-            while (tpk < 32 && 2 * tpk * m <= (int)blockDim.x)
-                tpk <<= 1;
-            const int per = blockDim.x / tpk;
-            const int part = tid & (tpk - 1);
-            for (int i0 = 0; i0 < m; i0 += per) {
-                const int i = i0 + tid / tpk;
-                const bool have = i < m;
-                const unsigned long long ki = have ? sm.keys[i] : 0ull;
-                int rank = 0;
-                if (have) {
-                    int j = part;
-                    for (; j + 3 * tpk < m; j += 4 * tpk)
-                        rank += (sm.keys[j] > ki) + (sm.keys[j + tpk] > ki) +
-                                (sm.keys[j + 2 * tpk] > ki) +
-                                (sm.keys[j + 3 * tpk] > ki);
-                    for (; j < m; j += tpk)
-                        rank += sm.keys[j] > ki;
-                }
-                for (int o = tpk >> 1; o > 0; o >>= 1)
-                    rank += __shfl_xor_sync(FULL, rank, o);
-                if (have && part == 0)
-                    sm.sorted[rank] = ki;
-            }
+            unsigned long long *dst = sm.sorted;
+            rank_keys(sm.keys, m, 0, m, blockDim.x, &dst, 1);
         }
         __syncthreads();
         taken += m;
         upper = sm.sorted[m - 1];
 
         /* decode; drop candidates similar to a survivor of an earlier chunk */
-        const int W = (m + 31) >> 5;
         for (int i = tid; i < 32; i += blockDim.x)
             sm.removed[i] = 0u;
         __syncthreads();
@@ -366,183 +567,104 @@ hl_finalize_kernel(hl_final_args a, float scale)
                 atomicOr(&sm.removed[i >> 5], 1u << (i & 31));
         }
         __syncthreads();
-        /* predecessor bitmask: bit j of pred[i] <=> j < i and similar(j, i).
-         * Only the words holding some j < i are built: entry (i, wd) for
-         * 32 wd < i, enumerated word by word.  Four adjacent threads share
-         * an entry (8 tests each, OR-ed by shuffles); the threads of a warp
-         * mostly share wd and read the word's candidates with broadcast
-         * loads. */
-        {
-            int nent = 0;
-            for (int wd = 0; wd < W; wd++)
-                nent += max(0, m - 32 * wd - 1);
-            const int span = (4 * nent + 31) & ~31;
-            for (int e = tid; e < span; e += blockDim.x) {
-                const int q = e & 3, en = e >> 2;
-                unsigned bits = 0u;
-                int i = 0, wd = 0, jn = 0;
-                if (en < nent) {
-                    int rem = en;
-                    while (rem >= m - 32 * wd - 1) {
-                        rem -= m - 32 * wd - 1;
-                        wd++;
-                    }
-                    i = 32 * wd + 1 + rem;
-                    jn = min(32, i - (wd << 5));
-                }
-                {
-                    /* every lane runs the same 8 tests (invalid ones masked
-                     * afterwards), so the rare exact wrap-around test is a
-                     * warp-uniform branch */
-                    const int j0 = wd << 5;
-                    const float ai = sm.ang[i];
-                    const int di = sm.dist[i];
-#pragma unroll
-                    for (int b = 8 * q; b < 8 * q + 8; b++) {
-                        const int j = min(j0 + b, m - 1);
-                        const float aj = sm.ang[j];
-                        const int dj = sm.dist[j];
-                        const bool same = (abs(dj - di) < a.thresdis) &
-                                          (fabsf(__fsub_rn(aj, ai)) < a.thresang);
-                        const bool near = abs(dj + di) < a.thresdis;
-                        const float est = fabsf(__fsub_rn(__fsub_rn(3.14159265f, aj), ai));
-                        const bool lo = est < a.thresang - 1e-6f;
-                        const bool hi = est > a.thresang + 1e-6f;
-                        bool wrap = near & lo;
-                        const bool amb = near & !lo & !hi & (b < jn);
-                        if (__any_sync(FULL, amb)) {
-                            if (amb)
-                                wrap = wrap_exact(aj, ai, a.thresang);
-                        }
-                        bits |= (unsigned)((same | wrap) & (b < jn)) << b;
-                    }
-                }
-                bits |= __shfl_xor_sync(FULL, bits, 1);
-                bits |= __shfl_xor_sync(FULL, bits, 2);
-                if (en < nent && q == 0)
-                    sm.pred[i][wd] = bits;
-            }
-        }
-        /* The greedy pass of okano_3_0/HoughLine.cu:900-927 keeps candidate i
-         * iff it was not removed by an earlier chunk and no earlier kept
-         * candidate is similar to it.  Resolved in rounds: an undecided
-         * candidate with a kept predecessor is dropped, one whose
-         * predecessors are all decided (none kept) is kept.  Each round
-         * decides at least the first undecided candidate; in practice a few
-         * rounds decide them all. */
-        if (tid < 32) {
-            unsigned d = (tid < W) ? sm.removed[tid] : 0xffffffffu;
-            if (tid == W - 1 && (m & 31))
-                d |= ~((1u << (m & 31)) - 1u);
-            sm.dec[tid] = d;
-            sm.alive[tid] = 0u;
-            sm.ndec[tid] = 0u;
-            sm.nalive[tid] = 0u;
-        }
+        build_pred(sm, m, a, tid, blockDim.x, sm.pred);
         __syncthreads();
-        for (int round = 0; round < m; round++) {
-            for (int i = tid; i < m; i += blockDim.x) {
-                const int iw = i >> 5;
-                const unsigned ib = 1u << (i & 31);
-                if (sm.dec[iw] & ib)
-                    continue;
-                bool all = true, kill = false;
-                for (int w = 0; w < ((i + 31) >> 5); w++) {
-                    const unsigned pw = sm.pred[i][w];
-                    all = all && !(pw & ~sm.dec[w]);
-                    kill = kill || (pw & sm.alive[w]);
-                }
-                if (kill) {
-                    atomicOr(&sm.ndec[iw], ib);
-                } else if (all) {
-                    atomicOr(&sm.ndec[iw], ib);
-                    atomicOr(&sm.nalive[iw], ib);
-                }
-            }
-            __syncthreads();
-            if (tid < 32) {
-                const unsigned d = sm.dec[tid] | sm.ndec[tid];
-                sm.dec[tid] = d;
-                sm.alive[tid] |= sm.nalive[tid];
-                sm.ndec[tid] = 0u;
-                sm.nalive[tid] = 0u;
-                const bool done = __all_sync(FULL, d == 0xffffffffu);
-                if (tid == 0)
-                    sm.misc[4] = done;
-            }
-            __syncthreads();
-            if (sm.misc[4])
-                break;
-        }
-        /* survivors in rank order, at most room of them */
-        {
-            const int room = K - S;
-            for (int i = tid; i < m; i += blockDim.x) {
-                const int iw = i >> 5;
-                const unsigned al = sm.alive[iw];
-                if ((al >> (i & 31)) & 1u) {
-                    int q = __popc(al & ((1u << (i & 31)) - 1u));
-                    for (int w = 0; w < iw; w++)
-                        q += __popc(sm.alive[w]);
-                    if (q < room)
-                        sm.surv[q] = i;
-                }
-            }
-            if (tid < 32) {
-                int c = __popc(sm.alive[tid]);
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1)
-                    c += __shfl_xor_sync(FULL, c, o);
-                if (tid == 0)
-                    sm.misc[3] = min(c, room);
-            }
-        }
-        __syncthreads();
-        const int ns = sm.misc[3];
-        for (int q = tid; q < ns; q += blockDim.x) {
-            const int i = sm.surv[q];
-            const int o = S + q;
-            hl_line L;
-            L.angle = sm.ang[i];
-            L.distance = sm.dist[i];
-            L.votes = sm.votes[i];
-            im.lines[o] = L;
-            if (o < FIN_SCACHE) {
-                sm.sang[o] = L.angle;
-                sm.sdist[o] = L.distance;
-            }
-        }
-        S += ns;
-        __syncthreads();
+        S += greedy_chunk(sm, im, m, K, S);
     }
-    if (tid == 0) {
-        const int cnt = (K > 0) ? S : K;
-        if (im.count_out)
-            *im.count_out = cnt;
-        *im.ncand = 0;
-        if (ncand_raw > im.cap)
-            atomicOr(a.status, HL_ST_CAND_OVERFLOW);
-        if (a.hdr) {   /* one image: report and clear the status word */
-            int st = *a.status;
-            if (ncand_raw > im.cap)
-                st |= HL_ST_CAND_OVERFLOW;
-            a.hdr->count = cnt;
-            a.hdr->status = st;
-            a.hdr->ncand = ncand_raw;
-            *a.status = 0;
-        }
+    if (tid == 0)
+        finalize_report(a, im, S, ncand_raw);
+}
+
+__global__ void __launch_bounds__(FIN_THREADS)
+hl_finalize_kernel(hl_final_args a, float scale)
+{
+    extern __shared__ __align__(16) unsigned char fin_raw[];
+    FinSmem &sm = *reinterpret_cast<FinSmem *>(fin_raw);
+    const hl_final_img im = a.imgs ? a.imgs[blockIdx.x] : a.img0;  /* CTA = image */
+    finalize_cta(a, im, scale, sm);
+}
+
+#define FIN_CLUSTER 8
+
+/* One image on a cluster of FIN_CLUSTER CTAs (one per SM) when its peaks
+ * fit one chunk: every CTA loads the keys, ranks an eighth of them into
+ * every CTA's sorted[] (distributed shared memory), decodes all of them and
+ * builds an eighth of the predecessor words into CTA 0's bitmask; after the
+ * cluster barrier CTA 0 alone runs the greedy pass.  With more peaks than a
+ * chunk CTA 0 runs finalize_cta and the others leave at once (no shared
+ * memory of another CTA is touched in that case). */
+__global__ void __cluster_dims__(FIN_CLUSTER, 1, 1) __launch_bounds__(FIN_THREADS)
+hl_finalize_cluster_kernel(hl_final_args a, float scale)
+{
+    extern __shared__ __align__(16) unsigned char fin_raw[];
+    FinSmem &sm = *reinterpret_cast<FinSmem *>(fin_raw);
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    const int tid = threadIdx.x;
+    const hl_final_img im = a.img0;
+    const int ncand_raw = *im.ncand;
+    const int n = min(ncand_raw, im.cap);
+    const int K = a.linesmax;
+    if (n > FIN_CHUNK || n == 0 || K <= 0) {
+        if (rank == 0)
+            finalize_cta(a, im, scale, sm);
+        return;
     }
+    const int m = n;
+    for (int i = tid; i < m; i += blockDim.x)
+        sm.keys[i] = im.keys[i];
+    __syncthreads();
+    {
+        unsigned long long *dst[FIN_CLUSTER];
+#pragma unroll
+        for (int d = 0; d < FIN_CLUSTER; d++)
+            dst[d] = cl.map_shared_rank(sm.sorted, d);
+        rank_keys(sm.keys, m, m * rank / FIN_CLUSTER, m * (rank + 1) / FIN_CLUSTER,
+                  blockDim.x, dst, FIN_CLUSTER);
+    }
+    cl.sync();
+    const int off = (im.ref_numrho - 1) / 2;
+    for (int i = tid; i < m; i += blockDim.x) {
+        float ang;
+        int dist, vts;
+        decode(sm.sorted[i], a.T, im.rho_min, off, scale, a.detheta, &ang, &dist, &vts);
+        sm.ang[i] = ang;
+        sm.dist[i] = dist;
+        sm.votes[i] = vts;
+    }
+    if (rank == 0)
+        for (int i = tid; i < 32; i += blockDim.x)
+            sm.removed[i] = 0u;
+    __syncthreads();
+    build_pred(sm, m, a, rank * (int)blockDim.x + tid, FIN_CLUSTER * (int)blockDim.x,
+               reinterpret_cast<unsigned (*)[FIN_CHUNK / 32 + 1]>(
+                   cl.map_shared_rank(&sm.pred[0][0], 0)));
+    cl.sync();
+    if (rank != 0)
+        return;
+    const int S = greedy_chunk(sm, im, m, K, 0);
+    if (tid == 0)
+        finalize_report(a, im, S, ncand_raw);
 }
 
 cudaError_t hl_launch_finalize(const hl_final_args *a, int nimg, cudaStream_t s)
 {
     const size_t smem = sizeof(FinSmem);
-    cudaError_t e = cudaFuncSetAttribute(
-        hl_finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-        (int)smem);
+    const float scale = (float)(1.0 / (a->T + 2));   /* :882-883 */
+    cudaError_t e;
+    if (nimg == 1 && !a->imgs) {
+        /* one image: a cluster spreads the sort and the bitmask */
+        e = cudaFuncSetAttribute(hl_finalize_cluster_kernel,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess)
+            return e;
+        hl_finalize_cluster_kernel<<<FIN_CLUSTER, FIN_THREADS, smem, s>>>(*a, scale);
+        return cudaGetLastError();
+    }
+    e = cudaFuncSetAttribute(hl_finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
     if (e != cudaSuccess)
         return e;
-    const float scale = (float)(1.0 / (a->T + 2));   /* :882-883 */
     hl_finalize_kernel<<<nimg, FIN_THREADS, smem, s>>>(*a, scale);
     return cudaGetLastError();
 }
