@@ -10,6 +10,8 @@
 
 #include "houghline_gb300.h"
 
+#include <utility>
+
 /* Compaction tiles: 128 x 32 pixels; one CTA of 256 threads reads one tile,
  * 16 pixels (one 16-byte vector) per thread. */
 #define HL_TILE_W 128
@@ -218,6 +220,40 @@ typedef struct hl_final_args {
 /* launchers (return cudaGetLastError() after the launch) */
 cudaError_t hl_launch_trig(float *cosv, float *sinv, int T, int Tp,
                            double detheta, cudaStream_t s);
+#ifdef __CUDACC__
+/* Programmatic dependent launch: the pipeline's kernels are launched with
+ * programmatic stream serialization, so a kernel's grid can be set up while
+ * its predecessor drains.  Each kernel waits for its predecessor's completion
+ * (and memory) before it touches global memory, then lets its own successor
+ * launch.  Both are no-ops for a kernel launched the ordinary way. */
+__device__ __forceinline__ void hl_pdl_begin()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+/* launch `kernel` with programmatic stream serialization (and, if coop, as a
+ * cooperative launch) */
+template <typename... Params, typename... Args>
+static inline cudaError_t hl_launch_pdl(void (*kernel)(Params...), dim3 grid, dim3 block,
+                                        size_t smem, cudaStream_t s, bool coop,
+                                        Args &&...args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[2];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    at[1].id = cudaLaunchAttributeCooperative;
+    at[1].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = coop ? 2 : 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+#endif
 cudaError_t hl_launch_compact(const hl_compact_args *a, cudaStream_t s);
 /* one image (a->imgs == NULL) with hl_compact_persist_ctas(ntiles, sms) CTAs
  * in a cooperative launch (0: too many to be resident at once), each adding

@@ -236,6 +236,7 @@ hl_compact_kernel(hl_compact_args a)
     __shared__ int s_red[HL_COMPACT_THREADS / 32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int ngroups = a.imgs ? a.ngroups : (a.ntiles + CT_GROUP - 1) / CT_GROUP;
+    hl_pdl_begin();
 
     /* Groups are taken in ticket order, so every predecessor of a group is
      * already resident when the group looks back: the waits always end. */
@@ -442,6 +443,7 @@ hl_compact_persist_kernel(hl_compact_args a, int nct)
     __shared__ __align__(16) unsigned short s_mask[CP_MAXT * 256];
     __shared__ unsigned short s_rowrel[CP_MAXT * 32];   /* row start in its tile */
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    hl_pdl_begin();
     /* a cooperative launch: every CTA is resident, so the CTA index orders
      * the prefix and the grid barrier below always completes */
     const int c = blockIdx.x;
@@ -655,17 +657,15 @@ int hl_compact_persist_ctas(int ntiles, int sms)
 
 cudaError_t hl_launch_compact_persist(const hl_compact_args *a, int nct, cudaStream_t s)
 {
-    hl_compact_args args = *a;
-    void *params[] = {&args, &nct};
-    return cudaLaunchCooperativeKernel((const void *)hl_compact_persist_kernel, dim3(nct),
-                                       dim3(CP_THREADS), params, 0, s);
+    return hl_launch_pdl(hl_compact_persist_kernel, dim3(nct), dim3(CP_THREADS), 0, s, true,
+                         *a, nct);
 }
 
 cudaError_t hl_launch_compact(const hl_compact_args *a, cudaStream_t s)
 {
     const int ngroups = a->imgs ? a->ngroups : (a->ntiles + CT_GROUP - 1) / CT_GROUP;
-    hl_compact_kernel<<<ngroups, HL_COMPACT_THREADS, 0, s>>>(*a);
-    return cudaGetLastError();
+    return hl_launch_pdl(hl_compact_kernel, dim3(ngroups), dim3(HL_COMPACT_THREADS), 0, s,
+                         false, *a);
 }
 
 /* Bounding box of an interleaved (x, y) list: bbox = {xmin, ymin, xmax, ymax}

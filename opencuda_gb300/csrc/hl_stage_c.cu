@@ -40,6 +40,7 @@ namespace cg = cooperative_groups;
 __global__ void __launch_bounds__(256) hl_peaks_kernel(hl_peak_args a)
 {
     const int q4 = a.Tp >> 2;
+    hl_pdl_begin();
     for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
         const int2 ch = a.chunks ? a.chunks[c] : make_int2(0, c * HL_PEAK_ROWS);
         const hl_peak_img im = a.imgs ? a.imgs[ch.x] : a.img0;
@@ -159,8 +160,7 @@ cudaError_t hl_launch_peaks(const hl_peak_args *a, cudaStream_t s)
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int blocks = std::max(1, std::min(a->nchunks, sms * 8));
-    hl_peaks_kernel<<<blocks, 256, 0, s>>>(*a);
-    return cudaGetLastError();
+    return hl_launch_pdl(hl_peaks_kernel, dim3(blocks), dim3(256), 0, s, false, *a);
 }
 
 /* ------------------------------------------------------------------ */
@@ -580,6 +580,7 @@ hl_finalize_kernel(hl_final_args a, float scale)
 {
     extern __shared__ __align__(16) unsigned char fin_raw[];
     FinSmem &sm = *reinterpret_cast<FinSmem *>(fin_raw);
+    hl_pdl_begin();
     const hl_final_img im = a.imgs ? a.imgs[blockIdx.x] : a.img0;  /* CTA = image */
     finalize_cta(a, im, scale, sm);
 }
@@ -601,6 +602,7 @@ hl_finalize_cluster_kernel(hl_final_args a, float scale)
     cg::cluster_group cl = cg::this_cluster();
     const int rank = (int)cl.block_rank();
     const int tid = threadIdx.x;
+    hl_pdl_begin();
     const hl_final_img im = a.img0;
     const int ncand_raw = *im.ncand;
     const int n = min(ncand_raw, im.cap);
@@ -658,15 +660,15 @@ cudaError_t hl_launch_finalize(const hl_final_args *a, int nimg, cudaStream_t s)
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess)
             return e;
-        hl_finalize_cluster_kernel<<<FIN_CLUSTER, FIN_THREADS, smem, s>>>(*a, scale);
-        return cudaGetLastError();
+        return hl_launch_pdl(hl_finalize_cluster_kernel, dim3(FIN_CLUSTER), dim3(FIN_THREADS),
+                             smem, s, false, *a, scale);
     }
     e = cudaFuncSetAttribute(hl_finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
     if (e != cudaSuccess)
         return e;
-    hl_finalize_kernel<<<nimg, FIN_THREADS, smem, s>>>(*a, scale);
-    return cudaGetLastError();
+    return hl_launch_pdl(hl_finalize_kernel, dim3(nimg), dim3(FIN_THREADS), smem, s, false, *a,
+                         scale);
 }
 
 /* acc[R][Tp] -> acc[R][T] */

@@ -578,6 +578,7 @@ hl_vote_kernel(hl_vote_args a)
     const int batch = 64 * ncons;
     const int nslices = a.Tp / HL_SLICE;
 
+    hl_pdl_begin();
     /* the block and its dump row start at zero; after each item the
      * consumers clear what it used */
     {
@@ -723,6 +724,7 @@ hl_vote_kernel(hl_vote_args a)
 __global__ void __launch_bounds__(256)
 hl_merge_kernel(hl_merge_args a)
 {
+    hl_pdl_begin();
     const hl_merge_region r = a.regs[blockIdx.y];
     const int i = blockIdx.x * 256 + threadIdx.x;
     if (i >= r.rows * (HL_SLICE / 4))
@@ -763,8 +765,8 @@ cudaError_t hl_launch_merge(const hl_merge_args *a, int max_rows, cudaStream_t s
     if (a->nreg <= 0)
         return cudaSuccess;
     const unsigned gx = (unsigned)((max_rows * (HL_SLICE / 4) + 255) / 256);
-    hl_merge_kernel<<<dim3(gx, (unsigned)a->nreg), 256, 0, s>>>(*a);
-    return cudaGetLastError();
+    return hl_launch_pdl(hl_merge_kernel, dim3(gx, (unsigned)a->nreg), dim3(256), 0, s, false,
+                         *a);
 }
 
 cudaError_t hl_launch_tile_masks(const hl_vote_args *a, int nimg, size_t max_words,
@@ -790,16 +792,17 @@ cudaError_t hl_launch_vote(const hl_vote_args *a, int threads, int grid,
                                  (int)smem);
         if (e != cudaSuccess)
             return e;
-        hl_vote_kernel<true><<<grid, threads, smem, s>>>(*a);
+        return hl_launch_pdl(hl_vote_kernel<true>, dim3(grid), dim3(threads), smem, s, false,
+                             *a);
     } else {
         e = cudaFuncSetAttribute(hl_vote_kernel<false>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem);
         if (e != cudaSuccess)
             return e;
-        hl_vote_kernel<false><<<grid, threads, smem, s>>>(*a);
+        return hl_launch_pdl(hl_vote_kernel<false>, dim3(grid), dim3(threads), smem, s, false,
+                             *a);
     }
-    return cudaGetLastError();
 }
 
 size_t hl_vote_points_smem_bytes(int win_rows)
