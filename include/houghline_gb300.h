@@ -136,6 +136,18 @@ int hl_batch_async(hl_handle *h, const hl_image_desc *imgs, int nimg,
                    int *counts_dev, void *stream);
 int hl_set_batch_graph(hl_handle *h, int enable);
 
+/* The tiled caller of okano_3_0/HoughRec.cu:716-760 as one hl_batch call:
+ * img (its data, pitch and size; its own ROI is ignored, as the reference
+ * overwrites it) in piecenum x piecenum cells of cell_x = width / piecenum by
+ * cell_y = height / piecenum pixels, cell (x, y) with ROI [x cell_x,
+ * x cell_x + cell_x - 1) x [y cell_y, y cell_y + cell_y - 1) (the
+ * reference's exclusive end drops the cell's last column and row).  lines /
+ * counts: HOST arrays of piecenum^2 * linesmax records and piecenum^2 counts,
+ * cell y * piecenum + x first; line parameters are in the cell's local
+ * coordinates, as the reference's per-cell houghLine calls return them. */
+int hl_tiles(hl_handle *h, const hl_image_desc *img, int piecenum, int linesmax,
+             hl_line *lines, int *counts, void *stream);
+
 /* Autotuner (no reference counterpart): times hl_batch_async on the given
  * images for every candidate vote-kernel shape (rho-window rows x threads
  * per CTA), keeps the fastest with hl_set_vote_shape and reports it.

@@ -99,6 +99,7 @@ SIGNATURES = {
     "hl_batch": (I, [H, C.POINTER(hl_image_desc), I, PI, I, P, PI, P]),
     "hl_batch_async": (I, [H, C.POINTER(hl_image_desc), I, PI, I, P, P, P]),
     "hl_set_batch_graph": (I, [H, I]),
+    "hl_tiles": (I, [H, C.POINTER(hl_image_desc), I, I, P, PI, P]),
     "hl_autotune": (I, [H, C.POINTER(hl_image_desc), I, PI, I, C.POINTER(hl_tune_entry),
                         C.POINTER(hl_tune_entry), I, PI, P]),
     "hl_plain_points": (I, [H, P, I, PI, P, P]),

@@ -1908,6 +1908,29 @@ extern "C" int hl_batch_async(hl_handle *h, const hl_image_desc *imgs, int nimg,
                      reinterpret_cast<cudaStream_t>(stream));
 }
 
+extern "C" int hl_tiles(hl_handle *h, const hl_image_desc *img, int piecenum, int linesmax,
+                        hl_line *lines, int *counts, void *stream)
+{
+    if (!h || !img || !counts)
+        return HL_NULL_POINTER;
+    if (piecenum <= 0 || piecenum > 1024)
+        return HL_INVALID_DATA;
+    const int cx = img->width / piecenum, cy = img->height / piecenum;
+    if (cx < 2 || cy < 2)
+        return HL_INVALID_DATA;
+    std::vector<hl_image_desc> cells((size_t)piecenum * piecenum, *img);
+    for (int y = 0; y < piecenum; y++)
+        for (int x = 0; x < piecenum; x++) {
+            hl_image_desc &d = cells[(size_t)y * piecenum + x];
+            d.roi_x1 = x * cx;
+            d.roi_x2 = x * cx + cx - 1;   /* okano_3_0/HoughRec.cu:745-748 */
+            d.roi_y1 = y * cy;
+            d.roi_y2 = y * cy + cy - 1;
+        }
+    return hl_batch(h, cells.data(), (int)cells.size(), nullptr, linesmax, lines, counts,
+                    stream);
+}
+
 extern "C" int hl_batch(hl_handle *h, const hl_image_desc *imgs, int nimg,
                         const int *thresholds, int linesmax, hl_line *lines,
                         int *counts, void *stream)

@@ -229,6 +229,27 @@ class HoughLine:
                         for j in range(max(counts[i], 0))])
         return rc, res
 
+    def houghLineTiles(self, inimg: Image, piecenum: int, linesmax: int = 16,
+                       stream=None):
+        """The tiled caller of okano_3_0/HoughRec.cu:716-760 as one batched
+        launch (hl_tiles): piecenum x piecenum cells of (w / piecenum,
+        h / piecenum) pixels, cell (x, y) with ROI x1 = x * cell_x,
+        x2 = x1 + cell_x - 1 (the reference's exclusive end drops the cell's
+        last column and row).  Returns (rc, lines) with lines[y * piecenum + x]
+        in the cell's local coordinates, as the reference's per-cell
+        houghLine calls give them."""
+        n = max(piecenum, 0) ** 2
+        K = max(linesmax, 0)
+        out = (_lib.hl_line * max(K * n, 1))()
+        counts = (C.c_int * max(n, 1))()
+        d = inimg.desc()
+        rc = self._L.hl_tiles(self._h, C.byref(d), piecenum, linesmax, out, counts,
+                              self._stream(stream))
+        if rc != _lib.NO_ERROR:
+            return rc, []
+        return rc, [[LineParam(*out[i * K + j].as_tuple()) for j in range(max(counts[i], 0))]
+                    for i in range(n)]
+
     def set_batch_graph(self, enable: bool) -> int:
         return self._L.hl_set_batch_graph(self._h, 1 if enable else 0)
 

@@ -63,6 +63,7 @@ def test_batch_entry_points_reject_null_without_gpu():
     lib = _lib.load()
     assert lib.hl_batch(None, None, 0, None, 0, None, None, None) == _lib.NULL_POINTER
     assert lib.hl_batch_async(None, None, 0, None, 0, None, None, None) == _lib.NULL_POINTER
+    assert lib.hl_tiles(None, None, 4, 16, None, None, None) == _lib.NULL_POINTER
     assert lib.hl_set_batch_graph(None, 1) == _lib.NULL_POINTER
     assert lib.hl_autotune(None, None, 0, None, 0, None, None, 0, None, None) == \
         _lib.NULL_POINTER

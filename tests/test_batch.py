@@ -127,3 +127,29 @@ def test_batch_errors(hl_mod):
     d.roiX2 = d.width + 1   # ROI outside the image
     rc, _ = hl.houghLineBatch([d], 16)
     assert rc == -1
+
+
+def test_tiled_cells_one_launch(hl_mod):
+    """The HoughRec tiling (okano_3_0/HoughRec.cu:716-760): every cell of a
+    piecenum x piecenum grid, ROIs [x c, x c + c - 1), in one batched launch
+    equals the per-cell plain call and the oracle on the cell."""
+    HoughLine, Image = hl_mod
+    img = cases.synth_custom(1600, 1200, 40, 60, 900, 15000, 321)
+    hl = HoughLine(detheta=math.pi / 180, threshold=40, thresang=float(np.float32(math.pi / 30)),
+                   thresdis=15)
+    dimg = Image.from_host(img)
+    rc, per_cell = hl.houghLineTiles(dimg, 4, 24)
+    assert rc == 0 and len(per_cell) == 16
+    cx, cy = 1600 // 4, 1200 // 4
+    for y in range(4):
+        for x in range(4):
+            roi = (x * cx, y * cy, x * cx + cx - 1, y * cy + cy - 1)
+            rc1, plain = hl.houghLine(Image(dimg.data, roi), None, 24)
+            assert rc1 == 0
+            got = [l.astuple() for l in per_cell[y * 4 + x]]
+            assert got == [l.astuple() for l in plain]
+            c, s = hl.trig_table()
+            x1, y1, x2, y2 = roi
+            want, _, _ = O.houghline(img[y1:y2, x1:x2], c, s, math.pi / 180, 1.0, 40,
+                                     hl.getThresAng(), hl.getThresDis(), 24)
+            assert got == want
