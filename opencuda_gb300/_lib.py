@@ -39,6 +39,19 @@ class hl_line(C.Structure):
         return (self.angle, self.distance, self.votes)
 
 
+class hl_circle(C.Structure):
+    """CircleParam, okano_3_0/HoughCircle.h:37-44"""
+    _fields_ = [("a", C.c_int), ("b", C.c_int), ("radius", C.c_int), ("votes", C.c_int)]
+
+    def as_tuple(self):
+        return (self.a, self.b, self.radius, self.votes)
+
+
+class hl_circle_params(C.Structure):
+    _fields_ = [("radius_min", C.c_int), ("radius_max", C.c_int),
+                ("dist_thres", C.c_float), ("r_thres", C.c_int), ("threshold", C.c_int)]
+
+
 class hl_image_desc(C.Structure):
     _fields_ = [("data", C.c_void_p), ("pitch", C.c_size_t),
                 ("width", C.c_int), ("height", C.c_int),
@@ -100,6 +113,9 @@ SIGNATURES = {
     "hl_batch_async": (I, [H, C.POINTER(hl_image_desc), I, PI, I, P, P, P]),
     "hl_set_batch_graph": (I, [H, I]),
     "hl_tiles": (I, [H, C.POINTER(hl_image_desc), I, I, P, PI, P]),
+    "hl_circles": (I, [H, C.POINTER(hl_image_desc), C.POINTER(hl_circle_params), PI, P, P]),
+    "hl_circle_accumulator": (I, [H, C.POINTER(hl_image_desc), C.POINTER(hl_circle_params),
+                                  P, P]),
     "hl_autotune": (I, [H, C.POINTER(hl_image_desc), I, PI, I, C.POINTER(hl_tune_entry),
                         C.POINTER(hl_tune_entry), I, PI, P]),
     "hl_plain_points": (I, [H, P, I, PI, P, P]),

@@ -43,7 +43,7 @@ def _run(cmd: list[str]) -> None:
 
 
 CU_SOURCES = ["hl_stage_a.cu", "hl_vote.cu", "hl_stage_c.cu", "hl_stage_f.cu",
-              "hl_noalloc.cu", "hl_cnn.cu", "hl_synth.cu", "hl_window.cu"]
+              "hl_noalloc.cu", "hl_cnn.cu", "hl_synth.cu", "hl_window.cu", "hl_circle.cu"]
 CXX_SOURCES = ["hl_api.cpp", "HoughLine.cpp", "Image.cpp", "hl_proposal.cpp"]
 C_SOURCES = ["synth.c"]
 
@@ -99,14 +99,16 @@ def build_oracle(force: bool = False) -> Path:
     outdir = ORACLE / "_build"
     outdir.mkdir(parents=True, exist_ok=True)
     out = outdir / "libhough_oracle.so"
-    srcs = [ORACLE / "hough_oracle.c", ORACLE / "hough_oracle.h"]
+    srcs = [ORACLE / "hough_oracle.c", ORACLE / "hough_oracle.h",
+            ORACLE / "circle_oracle.c", ORACLE / "circle_oracle.h"]
     if not force and _newer(out, srcs):
         return out
     tmp = outdir / "libhough_oracle.so.tmp"
     # -ffp-contract=off: every float product and sum is rounded as written
     # (aarch64 gcc would otherwise fuse them into fmadd).
     _run(["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
-          "-std=gnu11", str(ORACLE / "hough_oracle.c"), "-o", str(tmp), "-lm"])
+          "-std=gnu11", str(ORACLE / "hough_oracle.c"), str(ORACLE / "circle_oracle.c"),
+          "-o", str(tmp), "-lm"])
     os.replace(tmp, out)
     return out
 

@@ -72,6 +72,17 @@ struct hl_handle {
     size_t cap_merge;
     int4 *d_scratch;
     size_t cap_scratch;
+    /* HoughCircle: accumulator, midpoint-step table (cached per radius
+     * range), candidate keys, [ncand, status] counters, results */
+    int32_t *d_cacc;
+    size_t cap_cacc;
+    int2 *d_ctab;
+    size_t cap_ctab;
+    int ctab_rmin, ctab_rmax, ctab_n;
+    unsigned long long *d_ckeys;
+    int *d_ccnt;
+    unsigned char *d_cres;
+    unsigned char *h_cres;
     /* admitted-tile masks of the cached geometry (see hl_tile_mask_kernel) */
     unsigned *d_tmask;
     size_t cap_tmask;
@@ -240,12 +251,15 @@ extern "C" int hl_destroy(hl_handle *h)
     void *ptrs[] = {h->d_cos, h->d_sin, h->d_pts, h->d_tile_state,
                     h->d_tile_off, h->d_acc, h->d_keys, h->d_aux,
                     h->d_result, h->d_counters, h->order_dev,
-                    h->d_merge, h->d_scratch, h->d_tmask};
+                    h->d_merge, h->d_scratch, h->d_tmask, h->d_cacc, h->d_ctab,
+                    h->d_ckeys, h->d_ccnt, h->d_cres};
     for (void *q : ptrs)
         if (q)
             cudaFree(q);
     if (h->h_result)
         cudaFreeHost(h->h_result);
+    if (h->h_cres)
+        cudaFreeHost(h->h_cres);
     if (h->prof_ev) {
         for (int i = 0; i < HL_PROF_MAX * (HL_NSTAGE + 1); i++)
             cudaEventDestroy(h->prof_ev[i]);
@@ -675,6 +689,43 @@ static int roi_of(const hl_image_desc *img, hl_roi *roi)
 }
 
 /* stages (a) + (b) into h->d_acc ([R][Tp]) */
+/* Stage (a) of one image's ROI into h->d_pts (float2, tile-major, odd tiles
+ * padded), h->d_tile_off and the point count h->d_counters[2]: about one
+ * CTA per SM when they fit at once, else one CTA per 4-tile group. */
+static int launch_compaction(hl_handle *h, const hl_roi &roi, const hl_geom &g,
+                             cudaStream_t s)
+{
+    const int ntiles = g.tiles_x * g.tiles_y;
+    hl_compact_args ca;
+    memset(&ca, 0, sizeof(ca));
+    ca.roi = roi;
+    ca.tiles_x = g.tiles_x;
+    ca.ntiles = ntiles;
+    ca.tile_state = h->d_tile_state;
+    ca.ticket = reinterpret_cast<unsigned *>(h->d_counters + 3);
+    ca.ticket_base = h->ticket_base;
+    if (++h->epoch >= (1u << 30)) {
+        CK(cudaMemsetAsync(h->d_tile_state, 0,
+                           sizeof(unsigned long long) * h->cap_tiles, s));
+        h->epoch = 1;
+    }
+    ca.epoch = h->epoch;
+    ca.pts = nullptr;
+    ca.pts_f2 = reinterpret_cast<float2 *>(h->d_pts);
+    ca.tile_off = h->d_tile_off;
+    ca.count = h->d_counters + 2;
+    ca.status = h->d_counters + 1;
+    const int nct = hl_compact_persist_ctas(ntiles, h->sms);
+    if (nct > 0) {
+        CK(hl_launch_compact_persist(&ca, nct, s));
+        h->ticket_base += (unsigned)nct;
+    } else {
+        CK(hl_launch_compact(&ca, s));
+        h->ticket_base += (unsigned)((ntiles + HL_COMPACT_GROUP - 1) / HL_COMPACT_GROUP);
+    }
+    return HL_NO_ERROR;
+}
+
 static int run_ab(hl_handle *h, const hl_roi &roi, const hl_geom &g,
                   cudaStream_t s, int *launches)
 {
@@ -727,41 +778,10 @@ static int run_ab(hl_handle *h, const hl_roi &roi, const hl_geom &g,
         h->masks_dirty = 0;
     }
 
-    hl_compact_args ca;
-    memset(&ca, 0, sizeof(ca));
-    ca.roi = roi;
-    ca.tiles_x = g.tiles_x;
-    ca.ntiles = ntiles;
-    ca.imgs = nullptr;
-    ca.group_img = nullptr;
-    ca.nimg = 0;
-    ca.ngroups = 0;
-    ca.tile_state = h->d_tile_state;
-    ca.ticket = reinterpret_cast<unsigned *>(h->d_counters + 3);
-    ca.ticket_base = h->ticket_base;
-    if (++h->epoch >= (1u << 30)) {
-        CK(cudaMemsetAsync(h->d_tile_state, 0,
-                           sizeof(unsigned long long) * h->cap_tiles, s));
-        h->epoch = 1;
-    }
-    ca.epoch = h->epoch;
-    ca.pts = nullptr;
-    ca.pts_f2 = reinterpret_cast<float2 *>(h->d_pts);
-    ca.tile_off = h->d_tile_off;
-    ca.count = h->d_counters + 2;
-    ca.status = h->d_counters + 1;
     prof_mark(h, 0, s);
-    {
-        /* about one CTA per SM when they fit at once, else one per group */
-        const int nct = hl_compact_persist_ctas(ntiles, h->sms);
-        if (nct > 0) {
-            CK(hl_launch_compact_persist(&ca, nct, s));
-            h->ticket_base += (unsigned)nct;
-        } else {
-            CK(hl_launch_compact(&ca, s));
-            h->ticket_base += (unsigned)((ntiles + HL_COMPACT_GROUP - 1) / HL_COMPACT_GROUP);
-        }
-    }
+    rc = launch_compaction(h, roi, g, s);
+    if (rc != HL_NO_ERROR)
+        return rc;
     (*launches)++;
     prof_mark(h, 1, s);
 
@@ -2369,5 +2389,176 @@ extern "C" int hl_proposal_batch(hl_handle *h, hl_net *net,
         memcpy(&v, &st_host[2], sizeof(v));
         stats->votes = (long long)v;
     }
+    return HL_NO_ERROR;
+}
+
+/* ---- HoughCircle (include/hl_circle.h) ---------------------------------- */
+
+/* the midpoint steps of every radius (okano_3_0/HoughCircle.cu:214-243):
+ * {radius - rmin, x | y << 16} for x = 0, y = r, d = 3 - 2r while x < y;
+ * at most what one CTA's shared memory holds */
+#define HL_CIRCLE_MAXTAB (200 * 1024 / 8)
+
+static int circle_prepare(hl_handle *h, const hl_image_desc *img, const hl_circle_params *p,
+                          hl_roi *roi, hl_geom *g, cudaStream_t s)
+{
+    if (!h || !img || !p)
+        return HL_NULL_POINTER;
+    if (p->radius_min < 0 || p->radius_max < p->radius_min || p->radius_max >= 65536 ||
+        p->threshold < 0 || !(p->dist_thres == p->dist_thres))
+        return HL_INVALID_DATA;
+    int rc = roi_of(img, roi);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    if ((rc = hl_geometry(h, roi->w, roi->h, g)) != HL_NO_ERROR)
+        return rc;
+    if ((rc = ensure_image(h, *g, roi->w, roi->h)) != HL_NO_ERROR)
+        return rc;
+    if (!h->d_ctab || h->ctab_rmin != p->radius_min || h->ctab_rmax != p->radius_max) {
+        std::vector<int2> tab;
+        for (int r = p->radius_min; r <= p->radius_max; r++) {
+            int x = 0, y = r, d = 3 - 2 * r;
+            while (x < y) {
+                tab.push_back(make_int2(r - p->radius_min, x | (y << 16)));
+                if ((int)tab.size() > HL_CIRCLE_MAXTAB)
+                    return HL_INVALID_DATA;   /* radius range too wide */
+                if (d < y)
+                    d += 4 * x + 6;
+                else {
+                    d += 4 * (x - y) + 10;
+                    y--;
+                }
+                x++;
+            }
+        }
+        if ((rc = grow((void **)&h->d_ctab, &h->cap_ctab,
+                       sizeof(int2) * std::max(tab.size(), (size_t)1))) != HL_NO_ERROR)
+            return rc;
+        if (!tab.empty())
+            CK(cudaMemcpy(h->d_ctab, tab.data(), sizeof(int2) * tab.size(),
+                          cudaMemcpyHostToDevice));
+        h->ctab_rmin = p->radius_min;
+        h->ctab_rmax = p->radius_max;
+        h->ctab_n = (int)tab.size();
+    }
+    (void)s;
+    return HL_NO_ERROR;
+}
+
+/* compaction and the vote into acc ([nr][h][w], cleared here) */
+static int circle_vote(hl_handle *h, const hl_roi &roi, const hl_geom &g,
+                       const hl_circle_params *p, int32_t *acc, cudaStream_t s)
+{
+    const int nr = p->radius_max - p->radius_min + 1;
+    CK(cudaMemsetAsync(acc, 0, sizeof(int32_t) * (size_t)nr * roi.w * roi.h, s));
+    int rc = launch_compaction(h, roi, g, s);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    if (h->ctab_n == 0)
+        return HL_NO_ERROR;   /* radius 0 only: no votes */
+    hl_circle_vote_args va;
+    va.pts = reinterpret_cast<const float2 *>(h->d_pts);
+    va.count = h->d_counters + 2;
+    va.tab = h->d_ctab;
+    va.ntab = h->ctab_n;
+    va.w = roi.w;
+    va.h = roi.h;
+    va.acc = acc;
+    CK(hl_launch_circle_vote(&va, std::max(h->sms, 1), s));
+    return HL_NO_ERROR;
+}
+
+extern "C" int hl_circle_accumulator(hl_handle *h, const hl_image_desc *img,
+                                     const hl_circle_params *p, int32_t *acc_dev,
+                                     void *stream)
+{
+    if (!acc_dev)
+        return HL_NULL_POINTER;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    hl_roi roi;
+    hl_geom g;
+    int rc = circle_prepare(h, img, p, &roi, &g, s);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    return circle_vote(h, roi, g, p, acc_dev, s);
+}
+
+extern "C" int hl_circles(hl_handle *h, const hl_image_desc *img, const hl_circle_params *p,
+                          int *circlemax, hl_circle *out, void *stream)
+{
+    if (!circlemax)
+        return HL_NULL_POINTER;
+    if (*circlemax > 0 && !out)
+        return HL_NULL_POINTER;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    hl_roi roi;
+    hl_geom g;
+    int rc = circle_prepare(h, img, p, &roi, &g, s);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    const int nr = p->radius_max - p->radius_min + 1;
+    const size_t cells = (size_t)nr * roi.w * roi.h;
+    if (cells >= (size_t)0xffffffffu)
+        return HL_OP_OVERFLOW;   /* the candidate key holds a 32-bit index */
+    const int cm = std::max(*circlemax, 0);
+    const size_t rbytes = sizeof(hl_result_hdr) + sizeof(hl_circle) * (size_t)std::max(cm, 1);
+    if ((rc = grow((void **)&h->d_cacc, &h->cap_cacc, sizeof(int32_t) * cells)) != HL_NO_ERROR)
+        return rc;
+    if (!h->d_ckeys) {
+        CK(cudaMalloc(&h->d_ckeys, sizeof(unsigned long long) * HL_CIRCLE_MAXCAND));
+        CK(cudaMalloc(&h->d_ccnt, 2 * sizeof(int)));
+        CK(cudaMemset(h->d_ccnt, 0, 2 * sizeof(int)));
+    }
+    /* results: header + room for circlemax circles, pinned mirror */
+    static const size_t kResCap = sizeof(hl_result_hdr) + sizeof(hl_circle) * 4096;
+    if (rbytes > kResCap)
+        return HL_INVALID_DATA;
+    if (!h->d_cres) {
+        CK(cudaMalloc(&h->d_cres, kResCap));
+        CK(cudaMallocHost(&h->h_cres, kResCap + sizeof(int)));
+    }
+    if ((rc = circle_vote(h, roi, g, p, h->d_cacc, s)) != HL_NO_ERROR)
+        return rc;
+    hl_circle_peak_args pa;
+    pa.acc = h->d_cacc;
+    pa.nr = nr;
+    pa.w = roi.w;
+    pa.h = roi.h;
+    pa.threshold = p->threshold;
+    pa.keys = h->d_ckeys;
+    pa.ncand = h->d_ccnt;
+    pa.cap = HL_CIRCLE_MAXCAND;
+    pa.status = h->d_ccnt + 1;
+    CK(hl_launch_circle_peaks(&pa, std::max(h->sms, 1), s));
+    hl_circle_final_args fa;
+    fa.keys = h->d_ckeys;
+    fa.ncand = h->d_ccnt;
+    fa.w = roi.w;
+    fa.h = roi.h;
+    fa.rmin = p->radius_min;
+    fa.dist_thres = p->dist_thres;
+    fa.r_thres = p->r_thres;
+    fa.circlemax = cm;
+    fa.roi_x = img->roi_x1;
+    fa.roi_y = img->roi_y1;
+    fa.out = reinterpret_cast<hl_circle *>(h->d_cres + sizeof(hl_result_hdr));
+    fa.hdr = reinterpret_cast<hl_result_hdr *>(h->d_cres);
+    fa.status = h->d_ccnt + 1;
+    CK(hl_launch_circle_final(&fa, s));
+    /* the results and the compaction's status word */
+    int *cstat = reinterpret_cast<int *>(h->h_cres + kResCap);
+    CK(cudaMemcpyAsync(h->h_cres, h->d_cres, rbytes, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(cstat, h->d_counters + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const hl_result_hdr *hdr = reinterpret_cast<const hl_result_hdr *>(h->h_cres);
+    if (*cstat != 0) {
+        reset_counters(h, s);
+        return HL_CUDA_ERROR;
+    }
+    if (hdr->status != 0)
+        return (hdr->status & HL_ST_CAND_OVERFLOW) ? HL_OP_OVERFLOW : HL_CUDA_ERROR;
+    if (hdr->count > 0)
+        memcpy(out, h->h_cres + sizeof(hl_result_hdr), sizeof(hl_circle) * (size_t)hdr->count);
+    *circlemax = hdr->count;
     return HL_NO_ERROR;
 }

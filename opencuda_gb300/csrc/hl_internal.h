@@ -9,6 +9,7 @@
 #include <stdint.h>
 
 #include "houghline_gb300.h"
+#include "hl_circle.h"
 
 #include <utility>
 
@@ -254,6 +255,41 @@ static inline cudaError_t hl_launch_pdl(void (*kernel)(Params...), dim3 grid, di
     return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 #endif
+/* HoughCircle (hl_circle.cu) */
+#define HL_CIRCLE_MAXCAND 4096
+typedef struct hl_circle_vote_args {
+    const float2 *pts;        /* the compaction's points (odd tiles padded) */
+    const int *count;         /* entries of pts */
+    const int2 *tab;          /* {radius - rmin, x | y << 16} midpoint steps */
+    int ntab;
+    int w, h;                 /* ROI */
+    int32_t *acc;             /* [nr][h][w] */
+} hl_circle_vote_args;
+typedef struct hl_circle_peak_args {
+    const int32_t *acc;
+    int nr, w, h;
+    int threshold;
+    unsigned long long *keys; /* votes << 32 | ~index */
+    int *ncand;
+    int cap;
+    int *status;
+} hl_circle_peak_args;
+typedef struct hl_circle_final_args {
+    const unsigned long long *keys;
+    int *ncand;
+    int w, h, rmin;
+    float dist_thres;
+    int r_thres;
+    int circlemax;
+    int roi_x, roi_y;         /* added to the centres */
+    hl_circle *out;
+    hl_result_hdr *hdr;
+    int *status;
+} hl_circle_final_args;
+cudaError_t hl_launch_circle_vote(const hl_circle_vote_args *a, int sms, cudaStream_t s);
+cudaError_t hl_launch_circle_peaks(const hl_circle_peak_args *a, int sms, cudaStream_t s);
+cudaError_t hl_launch_circle_final(const hl_circle_final_args *a, cudaStream_t s);
+
 cudaError_t hl_launch_compact(const hl_compact_args *a, cudaStream_t s);
 /* one image (a->imgs == NULL) with hl_compact_persist_ctas(ntiles, sms) CTAs
  * in a cooperative launch (0: too many to be resident at once), each adding

@@ -68,6 +68,13 @@ def lib() -> C.CDLL:
         L.ho_real_line.argtypes = [P, C.c_long, C.c_int, C.c_int, C.c_int, C.c_int,
                                    C.c_int, C.c_int, C.c_float, C.c_float, P]
         L.ho_real_line.restype = C.c_int
+        L.hc_vote.argtypes = [P, C.c_long, C.c_int, C.c_int, C.c_int, C.c_int, P]
+        L.hc_vote.restype = C.c_longlong
+        L.hc_peaks.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_long]
+        L.hc_peaks.restype = C.c_long
+        L.hc_circles.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                 C.c_float, C.c_int, C.POINTER(C.c_int), P]
+        L.hc_circles.restype = C.c_long
         _lib = L
     return _lib
 
@@ -213,3 +220,38 @@ def max_threads() -> int:
 def default_thresang() -> float:
     """okano_3_0/HoughLine.h:123  thresang = M_PI/180*5.0f (float member)."""
     return float(np.float32(math.pi / 180 * 5.0))
+
+
+# ---- HoughCircle (oracle/circle_oracle.c) -------------------------------
+
+def circle_vote(roi: np.ndarray, rmin: int, rmax: int) -> np.ndarray:
+    """acc[z, y, x] of okano_3_0/HoughCircle.cu:187-245 for radii rmin..rmax
+    over the ROI array roi (uint8, 255 = edge)."""
+    roi = np.ascontiguousarray(roi, dtype=np.uint8)
+    h, w = roi.shape
+    acc = np.zeros((rmax - rmin + 1, h, w), np.int32)
+    lib().hc_vote(_p(roi), w, w, h, rmin, rmax, _p(acc))
+    return acc
+
+
+def circle_peaks(acc: np.ndarray, threshold: int) -> np.ndarray:
+    nr, h, w = acc.shape
+    acc = np.ascontiguousarray(acc, dtype=np.int32)
+    n = lib().hc_peaks(_p(acc), nr, w, h, threshold, None, 0)
+    idx = np.zeros(max(n, 1), np.int64)
+    lib().hc_peaks(_p(acc), nr, w, h, threshold, _p(idx), n)
+    return idx[:n]
+
+
+def houghcircle(roi: np.ndarray, rmin: int, rmax: int, threshold: int, dist_thres: float,
+                r_thres: int, circlemax: int):
+    """The image path of HoughCircle::houghcircle (okano_3_0/HoughCircle.cu:
+    1165-1214) on an ROI array: [(a, b, radius, votes)] in ROI-local
+    coordinates, and the candidate count."""
+    acc = circle_vote(roi, rmin, rmax)
+    nr, h, w = acc.shape
+    out = np.zeros((max(circlemax, 1), 4), np.int32)
+    cm = C.c_int(circlemax)
+    n = lib().hc_circles(_p(acc), nr, w, h, rmin, threshold, C.c_float(dist_thres),
+                         r_thres, C.byref(cm), _p(out))
+    return [tuple(int(v) for v in out[i]) for i in range(max(cm.value, 0))], int(n)

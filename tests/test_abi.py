@@ -10,7 +10,7 @@ from opencuda_gb300 import _lib
 ROOT = Path(__file__).resolve().parent.parent
 
 
-C_HEADERS = ["houghline_gb300.h", "hl_proposal.h"]
+C_HEADERS = ["houghline_gb300.h", "hl_proposal.h", "hl_circle.h"]
 
 
 def declared_symbols():
@@ -37,6 +37,9 @@ def test_struct_layouts():
     assert C.sizeof(_lib.hl_line) == 12
     assert _lib.hl_line.distance.offset == 4
     assert C.sizeof(_lib.hl_params) == 32
+    # CircleParam: int a, b, radius, votes (okano_3_0/HoughCircle.h:37-44)
+    assert C.sizeof(_lib.hl_circle) == 16
+    assert C.sizeof(_lib.hl_circle_params) == 20
 
 
 def test_error_codes_match_reference():
@@ -64,6 +67,8 @@ def test_batch_entry_points_reject_null_without_gpu():
     assert lib.hl_batch(None, None, 0, None, 0, None, None, None) == _lib.NULL_POINTER
     assert lib.hl_batch_async(None, None, 0, None, 0, None, None, None) == _lib.NULL_POINTER
     assert lib.hl_tiles(None, None, 4, 16, None, None, None) == _lib.NULL_POINTER
+    assert lib.hl_circles(None, None, None, None, None, None) == _lib.NULL_POINTER
+    assert lib.hl_circle_accumulator(None, None, None, None, None) == _lib.NULL_POINTER
     assert lib.hl_set_batch_graph(None, 1) == _lib.NULL_POINTER
     assert lib.hl_autotune(None, None, 0, None, 0, None, None, 0, None, None) == \
         _lib.NULL_POINTER

@@ -1,0 +1,124 @@
+"""HoughCircle on the GPU engine (include/hl_circle.h) against the CPU
+oracle (oracle/circle_oracle.c): the (radius, row, column) accumulator bit
+for bit, and the ranked, merged circles."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def ring_image(w, h, circles, noise=0.0, seed=0):
+    """255 on the pixels within half a pixel of each circle, plus salt."""
+    yy, xx = np.mgrid[0:h, 0:w]
+    img = np.zeros((h, w), np.uint8)
+    for a, b, r in circles:
+        img[np.abs(np.hypot(xx - a, yy - b) - r) < 0.5] = 255
+    if noise:
+        rng = np.random.default_rng(seed)
+        img[rng.random((h, w)) < noise] = 255
+    return img
+
+
+CASES = [
+    # (w, h, circles, noise, roi, rmin, rmax, threshold, dist, rthres, cmax)
+    (160, 120, [(50, 60, 20), (110, 40, 12)], 0.0, None, 5, 30, 30, 10.0, 5, 8),
+    (300, 200, [(80, 90, 35), (200, 100, 22), (150, 40, 9)], 0.01, (17, 11, 283, 190),
+     5, 50, 40, 50.0, 20, 16),
+    (256, 256, [(128, 128, 60), (60, 60, 18)], 0.02, None, 40, 64, 60, 20.0, 8, 12),
+    (97, 53, [(40, 26, 10)], 0.0, (3, 2, 95, 51), 0, 12, 10, 5.0, 3, 4),
+]
+
+
+@pytest.fixture(scope="module")
+def hc_mod(cuda):
+    from opencuda_gb300.houghcircle import HoughCircle, points_image
+    from opencuda_gb300.houghline import Image
+    return HoughCircle, Image, points_image
+
+
+def _roi_arr(img, roi):
+    if roi is None:
+        return img
+    x1, y1, x2, y2 = roi
+    return img[y1:y2, x1:x2]
+
+
+@pytest.mark.parametrize("case", CASES, ids=[f"{c[0]}x{c[1]}r{c[5]}-{c[6]}" for c in CASES])
+def test_circle_accumulator_bit_exact(hc_mod, case):
+    HoughCircle, Image, _ = hc_mod
+    w, h, circles, noise, roi, rmin, rmax, thr, dist, rth, cmax = case
+    img = ring_image(w, h, circles, noise, seed=w)
+    hc = HoughCircle(rmin, rmax, dist, rth, thr)
+    acc = hc.accumulator(Image.from_host(img, roi)).cpu().numpy()
+    want = O.circle_vote(_roi_arr(img, roi), rmin, rmax)
+    assert acc.shape == want.shape
+    assert np.array_equal(acc, want)
+
+
+@pytest.mark.parametrize("case", CASES, ids=[f"{c[0]}x{c[1]}r{c[5]}-{c[6]}" for c in CASES])
+def test_circles_match_oracle(hc_mod, case):
+    HoughCircle, Image, _ = hc_mod
+    w, h, circles, noise, roi, rmin, rmax, thr, dist, rth, cmax = case
+    img = ring_image(w, h, circles, noise, seed=w)
+    hc = HoughCircle(rmin, rmax, dist, rth, thr)
+    rc, got = hc.houghcircle(Image.from_host(img, roi), None, cmax)
+    assert rc == 0
+    want, n = O.houghcircle(_roi_arr(img, roi), rmin, rmax, thr, dist, rth, cmax)
+    ox, oy = (roi[0], roi[1]) if roi else (0, 0)
+    assert [c.astuple() for c in got] == [(a + ox, b + oy, r, v) for a, b, r, v in want]
+    assert len(got) > 0
+
+
+def test_circles_found_where_drawn(hc_mod):
+    HoughCircle, Image, _ = hc_mod
+    img = ring_image(200, 160, [(70, 80, 25), (150, 60, 15)])
+    hc = HoughCircle(5, 40, 15.0, 6, 40)
+    rc, got = hc.houghcircle(Image.from_host(img), None, 4)
+    assert rc == 0
+    found = {(c.a, c.b, c.radius) for c in got}
+    for a, b, r in [(70, 80, 25), (150, 60, 15)]:
+        assert any(abs(fa - a) <= 1 and abs(fb - b) <= 1 and abs(fr - r) <= 1
+                   for fa, fb, fr in found), (a, b, r, found)
+
+
+def test_circle_edge_cases(hc_mod):
+    from opencuda_gb300 import _lib
+    HoughCircle, Image, _ = hc_mod
+    empty = Image.from_host(np.zeros((64, 64), np.uint8))
+    hc = HoughCircle(5, 20, 10.0, 5, 10)
+    assert hc.houghcircle(empty, None, 8) == (0, [])
+    # nothing above the threshold
+    img = ring_image(100, 100, [(50, 50, 15)])
+    assert HoughCircle(5, 20, 10.0, 5, 100000).houghcircle(Image.from_host(img), None, 8) == (0, [])
+    # room for no circle
+    rc, got = HoughCircle(5, 20, 10.0, 5, 20).houghcircle(Image.from_host(img), None, 0)
+    assert rc == 0 and got == []
+    # radius_max < radius_min
+    bad = HoughCircle(5, 20, 10.0, 5, 20)
+    bad.radiusMax = 3
+    assert bad.houghcircle(Image.from_host(img), None, 8)[0] == _lib.INVALID_DATA
+    # more local maxima above the threshold than the tail ranks: an error,
+    # never a silently shortened list
+    noisy = ring_image(400, 400, [], noise=0.3, seed=7)
+    rc, _ = HoughCircle(5, 8, 10.0, 5, 0).houghcircle(Image.from_host(noisy), None, 8)
+    assert rc == _lib.OP_OVERFLOW
+
+
+def test_circle_guidingset(hc_mod):
+    """The coordinate-set path (okano_3_0/HoughCircle.cu:1175-1193): the points
+    drawn into a (max x + 2) x (max y + 2) image, then the image path."""
+    HoughCircle, Image, points_image = hc_mod
+    img = ring_image(150, 130, [(60, 70, 22)])
+    ys, xs = np.nonzero(img)
+    xy = np.stack([xs, ys], 1)
+    hc = HoughCircle(10, 30, 10.0, 5, 40)
+    rc, got = hc.houghcircle(None, xy, 4)
+    assert rc == 0
+    pim = np.zeros((int(ys.max()) + 2, int(xs.max()) + 2), np.uint8)
+    pim[ys, xs] = 255
+    want, _ = O.houghcircle(pim, 10, 30, 40, 10.0, 5, 4)
+    assert [c.astuple() for c in got] == list(want) and got
