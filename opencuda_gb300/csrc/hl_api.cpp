@@ -72,13 +72,7 @@ struct hl_handle {
     size_t cap_merge;
     int4 *d_scratch;
     size_t cap_scratch;
-    /* HoughCircle: accumulator, midpoint-step table (cached per radius
-     * range), candidate keys, [ncand, status] counters, results */
-    int32_t *d_cacc;
-    size_t cap_cacc;
-    int2 *d_ctab;
-    size_t cap_ctab;
-    int ctab_rmin, ctab_rmax, ctab_n;
+    /* HoughCircle: candidate keys, [ncand, status] counters, results */
     unsigned long long *d_ckeys;
     int *d_ccnt;
     unsigned char *d_cres;
@@ -251,7 +245,7 @@ extern "C" int hl_destroy(hl_handle *h)
     void *ptrs[] = {h->d_cos, h->d_sin, h->d_pts, h->d_tile_state,
                     h->d_tile_off, h->d_acc, h->d_keys, h->d_aux,
                     h->d_result, h->d_counters, h->order_dev,
-                    h->d_merge, h->d_scratch, h->d_tmask, h->d_cacc, h->d_ctab,
+                    h->d_merge, h->d_scratch, h->d_tmask,
                     h->d_ckeys, h->d_ccnt, h->d_cres};
     for (void *q : ptrs)
         if (q)
@@ -2394,13 +2388,8 @@ extern "C" int hl_proposal_batch(hl_handle *h, hl_net *net,
 
 /* ---- HoughCircle (include/hl_circle.h) ---------------------------------- */
 
-/* the midpoint steps of every radius (okano_3_0/HoughCircle.cu:214-243):
- * {radius - rmin, x | y << 16} for x = 0, y = r, d = 3 - 2r while x < y;
- * at most what one CTA's shared memory holds */
-#define HL_CIRCLE_MAXTAB (200 * 1024 / 8)
-
 static int circle_prepare(hl_handle *h, const hl_image_desc *img, const hl_circle_params *p,
-                          hl_roi *roi, hl_geom *g, cudaStream_t s)
+                          hl_roi *roi, hl_geom *g)
 {
     if (!h || !img || !p)
         return HL_NULL_POINTER;
@@ -2412,59 +2401,42 @@ static int circle_prepare(hl_handle *h, const hl_image_desc *img, const hl_circl
         return rc;
     if ((rc = hl_geometry(h, roi->w, roi->h, g)) != HL_NO_ERROR)
         return rc;
-    if ((rc = ensure_image(h, *g, roi->w, roi->h)) != HL_NO_ERROR)
-        return rc;
-    if (!h->d_ctab || h->ctab_rmin != p->radius_min || h->ctab_rmax != p->radius_max) {
-        std::vector<int2> tab;
-        for (int r = p->radius_min; r <= p->radius_max; r++) {
-            int x = 0, y = r, d = 3 - 2 * r;
-            while (x < y) {
-                tab.push_back(make_int2(r - p->radius_min, x | (y << 16)));
-                if ((int)tab.size() > HL_CIRCLE_MAXTAB)
-                    return HL_INVALID_DATA;   /* radius range too wide */
-                if (d < y)
-                    d += 4 * x + 6;
-                else {
-                    d += 4 * (x - y) + 10;
-                    y--;
-                }
-                x++;
-            }
-        }
-        if ((rc = grow((void **)&h->d_ctab, &h->cap_ctab,
-                       sizeof(int2) * std::max(tab.size(), (size_t)1))) != HL_NO_ERROR)
-            return rc;
-        if (!tab.empty())
-            CK(cudaMemcpy(h->d_ctab, tab.data(), sizeof(int2) * tab.size(),
-                          cudaMemcpyHostToDevice));
-        h->ctab_rmin = p->radius_min;
-        h->ctab_rmax = p->radius_max;
-        h->ctab_n = (int)tab.size();
-    }
-    (void)s;
-    return HL_NO_ERROR;
+    return ensure_image(h, *g, roi->w, roi->h);
 }
 
-/* compaction and the vote into acc ([nr][h][w], cleared here) */
-static int circle_vote(hl_handle *h, const hl_roi &roi, const hl_geom &g,
-                       const hl_circle_params *p, int32_t *acc, cudaStream_t s)
+/* the compaction, then one tile-kernel launch: the accumulator written to acc
+ * ([nr][h][w]) when it is given, the local maxima appended to the handle's
+ * candidate keys when peaks is set */
+static int circle_run(hl_handle *h, const hl_roi &roi, const hl_geom &g,
+                      const hl_circle_params *p, int32_t *acc, bool peaks, cudaStream_t s)
 {
     const int nr = p->radius_max - p->radius_min + 1;
-    CK(cudaMemsetAsync(acc, 0, sizeof(int32_t) * (size_t)nr * roi.w * roi.h, s));
+    hl_circle_tile_args ta;
+    memset(&ta, 0, sizeof(ta));
+    ta.ntx = (roi.w + HL_CIRCLE_TW - 1) / HL_CIRCLE_TW;
+    ta.nty = (roi.h + HL_CIRCLE_TH - 1) / HL_CIRCLE_TH;
+    if ((long long)ta.ntx * ta.nty * nr > 0x7fffffffLL)
+        return HL_OP_OVERFLOW;   /* more CTAs than one launch takes */
     int rc = launch_compaction(h, roi, g, s);
     if (rc != HL_NO_ERROR)
         return rc;
-    if (h->ctab_n == 0)
-        return HL_NO_ERROR;   /* radius 0 only: no votes */
-    hl_circle_vote_args va;
-    va.pts = reinterpret_cast<const float2 *>(h->d_pts);
-    va.count = h->d_counters + 2;
-    va.tab = h->d_ctab;
-    va.ntab = h->ctab_n;
-    va.w = roi.w;
-    va.h = roi.h;
-    va.acc = acc;
-    CK(hl_launch_circle_vote(&va, std::max(h->sms, 1), s));
+    ta.pts = reinterpret_cast<const float2 *>(h->d_pts);
+    ta.tile_off = h->d_tile_off;
+    ta.ctiles_x = g.tiles_x;
+    ta.ctiles_y = g.tiles_y;
+    ta.w = roi.w;
+    ta.h = roi.h;
+    ta.rmin = p->radius_min;
+    ta.nr = nr;
+    ta.acc = acc;
+    ta.threshold = p->threshold;
+    if (peaks) {
+        ta.keys = h->d_ckeys;
+        ta.ncand = h->d_ccnt;
+        ta.cap = HL_CIRCLE_MAXCAND;
+        ta.status = h->d_ccnt + 1;
+    }
+    CK(hl_launch_circle_tiles(&ta, s));
     return HL_NO_ERROR;
 }
 
@@ -2477,10 +2449,10 @@ extern "C" int hl_circle_accumulator(hl_handle *h, const hl_image_desc *img,
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     hl_roi roi;
     hl_geom g;
-    int rc = circle_prepare(h, img, p, &roi, &g, s);
+    int rc = circle_prepare(h, img, p, &roi, &g);
     if (rc != HL_NO_ERROR)
         return rc;
-    return circle_vote(h, roi, g, p, acc_dev, s);
+    return circle_run(h, roi, g, p, acc_dev, false, s);
 }
 
 extern "C" int hl_circles(hl_handle *h, const hl_image_desc *img, const hl_circle_params *p,
@@ -2493,7 +2465,7 @@ extern "C" int hl_circles(hl_handle *h, const hl_image_desc *img, const hl_circl
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     hl_roi roi;
     hl_geom g;
-    int rc = circle_prepare(h, img, p, &roi, &g, s);
+    int rc = circle_prepare(h, img, p, &roi, &g);
     if (rc != HL_NO_ERROR)
         return rc;
     const int nr = p->radius_max - p->radius_min + 1;
@@ -2502,8 +2474,6 @@ extern "C" int hl_circles(hl_handle *h, const hl_image_desc *img, const hl_circl
         return HL_OP_OVERFLOW;   /* the candidate key holds a 32-bit index */
     const int cm = std::max(*circlemax, 0);
     const size_t rbytes = sizeof(hl_result_hdr) + sizeof(hl_circle) * (size_t)std::max(cm, 1);
-    if ((rc = grow((void **)&h->d_cacc, &h->cap_cacc, sizeof(int32_t) * cells)) != HL_NO_ERROR)
-        return rc;
     if (!h->d_ckeys) {
         CK(cudaMalloc(&h->d_ckeys, sizeof(unsigned long long) * HL_CIRCLE_MAXCAND));
         CK(cudaMalloc(&h->d_ccnt, 2 * sizeof(int)));
@@ -2517,19 +2487,8 @@ extern "C" int hl_circles(hl_handle *h, const hl_image_desc *img, const hl_circl
         CK(cudaMalloc(&h->d_cres, kResCap));
         CK(cudaMallocHost(&h->h_cres, kResCap + sizeof(int)));
     }
-    if ((rc = circle_vote(h, roi, g, p, h->d_cacc, s)) != HL_NO_ERROR)
+    if ((rc = circle_run(h, roi, g, p, nullptr, true, s)) != HL_NO_ERROR)
         return rc;
-    hl_circle_peak_args pa;
-    pa.acc = h->d_cacc;
-    pa.nr = nr;
-    pa.w = roi.w;
-    pa.h = roi.h;
-    pa.threshold = p->threshold;
-    pa.keys = h->d_ckeys;
-    pa.ncand = h->d_ccnt;
-    pa.cap = HL_CIRCLE_MAXCAND;
-    pa.status = h->d_ccnt + 1;
-    CK(hl_launch_circle_peaks(&pa, std::max(h->sms, 1), s));
     hl_circle_final_args fa;
     fa.keys = h->d_ckeys;
     fa.ncand = h->d_ccnt;

@@ -1,20 +1,26 @@
 /*
  * hl_circle.cu -- HoughCircle on the HoughLine engine (the image path of
  * HoughCircle::houghcircle, okano_3_0/HoughCircle.cu:927-1165): the edge
- * pixels come from the same compaction, votes go into a (radius, row,
- * column) accumulator, then a local-maximum pass and a one-CTA tail.
+ * pixels come from the same compaction, votes are counted in (radius, row,
+ * column) accumulator tiles in shared memory, the local maxima taken in the
+ * same pass, then a one-CTA tail.
  *
- *   hl_circle_vote_kernel  -- every edge point votes, for every radius, the
- *       eight octant points of the reference's midpoint circle
+ *   hl_circle_tile_kernel -- one CTA per (accumulator tile, radius), largest
+ *       radius first.  The CTA counts its tile and a one-cell apron: every
+ *       edge point within the radius of them (read from the compaction tiles
+ *       that overlap that halo) walks the reference's midpoint circle
  *       (okano_3_0/HoughCircle.cu:187-245: x = 0, y = r, d = 3 - 2r; while
- *       x < y ...; points on the axes twice).  The (radius, x, y) steps of
- *       every radius are tabulated once on the host; a CTA takes a point at a
- *       time and its threads the table entries, so a point's votes issue in
- *       parallel; each lands with red.global in the L2-resident accumulator.
- *   hl_circle_peaks_kernel -- okano_3_0/HoughCircle.cu:321-370: v above the
- *       threshold, above the left and upper neighbours and at least the right
- *       and lower ones (zero outside the ROI), per radius; the keys
- *       (votes << 32 | ~index) appended with one atomic per warp.
+ *       x < y ...; eight octant points a step, the points on the axes twice)
+ *       and adds shared-memory atomics for the points inside the counted
+ *       cells; votes outside the ROI are dropped, as the reference drops
+ *       them.  The whole sum of a cell is then in shared memory, so the
+ *       interior is written out (the accumulator entry point) and/or its
+ *       local maxima taken (okano_3_0/HoughCircle.cu:321-370: v above the
+ *       threshold, above the left and upper neighbours and at least the
+ *       right and lower ones, zero outside the ROI) with the apron as the
+ *       neighbours; the keys (votes << 32 | ~index) are appended with one
+ *       atomic per warp.  The accumulator never goes to HBM on the circle
+ *       path.
  *   hl_circle_final_kernel -- one CTA: rank sort (votes descending, index
  *       ascending: the deviation from the reference's shear sort is only the
  *       order of equal votes), decode (:632-657), the greedy merge of
@@ -24,80 +30,156 @@
 
 #define FULL 0xffffffffu
 
-/* ---- vote ---------------------------------------------------------------- */
+/* ---- vote + local maxima ------------------------------------------------- */
 
-/* tab[e] = {z, x | y << 16}: step (x, y) of radius rmin + z */
-__global__ void __launch_bounds__(256)
-hl_circle_vote_kernel(hl_circle_vote_args a)
+#define CT_AW (HL_CIRCLE_TW + 2)
+#define CT_AH (HL_CIRCLE_TH + 2)
+#define CT_THREADS 512
+#define CT_ROWS 256   /* compaction-tile rows of the halo taken per pass */
+
+struct CircleTileSmem {
+    int cnt[CT_AH * CT_AW];   /* the tile and its apron, row-major */
+    int pre[CT_ROWS + 1];     /* points of the halo rows before each row */
+    int start[CT_ROWS];       /* first point of each halo row */
+    int red[CT_THREADS / 32];
+};
+
+/* one vote at local cell (x, y) when it lies in [xlo, xhi) x [ylo, yhi) */
+__device__ __forceinline__ void ct_vote(int *cnt, int x, int y, int xlo, int xw, int ylo,
+                                        int yh)
 {
-    extern __shared__ int2 s_tab[];
-    hl_pdl_begin();
-    for (int e = threadIdx.x; e < a.ntab; e += blockDim.x)
-        s_tab[e] = a.tab[e];
-    __syncthreads();
-    const int n = *a.count;
-    const size_t plane = (size_t)a.w * a.h;
-    for (int p = blockIdx.x; p < n; p += gridDim.x) {
-        const float2 pt = a.pts[p];
-        if (!(pt.x < 1.0e29f))
-            continue;   /* the compaction's sentinel of an odd tile */
-        const int x0 = (int)pt.x, y0 = (int)pt.y;
-        for (int e = threadIdx.x; e < a.ntab; e += blockDim.x) {
-            const int2 t = s_tab[e];
-            const int ox = t.y & 0xffff, oy = t.y >> 16;
-            int32_t *acc = a.acc + (size_t)t.x * plane;
-            const int xs[8] = {x0 + ox, x0 + ox, x0 - ox, x0 - ox,
-                               x0 + oy, x0 + oy, x0 - oy, x0 - oy};
-            const int ys[8] = {y0 + oy, y0 - oy, y0 + oy, y0 - oy,
-                               y0 + ox, y0 - ox, y0 + ox, y0 - ox};
-#pragma unroll
-            for (int q = 0; q < 8; q++)
-                if (xs[q] >= 0 && xs[q] < a.w && ys[q] >= 0 && ys[q] < a.h)
-                    atomicAdd(acc + (size_t)ys[q] * a.w + xs[q], 1);
-        }
-    }
+    if ((unsigned)(x - xlo) < (unsigned)xw && (unsigned)(y - ylo) < (unsigned)yh)
+        atomicAdd(cnt + y * CT_AW + x, 1);
 }
 
-/* ---- peaks --------------------------------------------------------------- */
-
-__global__ void __launch_bounds__(256)
-hl_circle_peaks_kernel(hl_circle_peak_args a)
+__global__ void __launch_bounds__(CT_THREADS, 2)
+hl_circle_tile_kernel(hl_circle_tile_args a)
 {
+    extern __shared__ __align__(16) unsigned char ct_raw[];
+    CircleTileSmem &sm = *reinterpret_cast<CircleTileSmem *>(ct_raw);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int ntile = a.ntx * a.nty;
+    const int z = a.nr - 1 - (int)(blockIdx.x / (unsigned)ntile);
+    const int tile = (int)(blockIdx.x % (unsigned)ntile);
+    const int r = a.rmin + z;
+    const int tx0 = (tile % a.ntx) * HL_CIRCLE_TW, ty0 = (tile / a.ntx) * HL_CIRCLE_TH;
+    /* counted cells, image coordinates: the tile and its apron within the ROI;
+     * local cell (x, y) is image cell (x + tx0 - 1, y + ty0 - 1) */
+    const int cx0 = max(tx0 - 1, 0), cy0 = max(ty0 - 1, 0);
+    const int cx1 = min(tx0 + HL_CIRCLE_TW + 1, a.w), cy1 = min(ty0 + HL_CIRCLE_TH + 1, a.h);
+    {
+        int4 *c4 = reinterpret_cast<int4 *>(sm.cnt);
+        for (int i = tid; i < CT_AH * CT_AW / 4; i += CT_THREADS)
+            c4[i] = make_int4(0, 0, 0, 0);
+    }
     hl_pdl_begin();
-    const long long total = (long long)a.nr * a.h * a.w;
-    const int lane = threadIdx.x & 31;
-    for (long long base = (long long)blockIdx.x * blockDim.x; base < total;
-         base += (long long)gridDim.x * blockDim.x) {
-        const long long i = base + threadIdx.x;
-        bool is = false;
-        int v = 0;
-        if (i < total) {
-            const int x = (int)(i % a.w);
-            const long long zy = i / a.w;
-            const int y = (int)(zy % a.h);
-            const int32_t *p = a.acc + i;
-            v = p[0];
-            if (v > a.threshold) {
-                const int L = x > 0 ? p[-1] : 0;
-                const int R = x + 1 < a.w ? p[1] : 0;
-                const int U = y > 0 ? p[-a.w] : 0;
-                const int D = y + 1 < a.h ? p[a.w] : 0;
-                is = v > L && v >= R && v > U && v >= D;
+    __syncthreads();
+    if (r > 0) {
+        const int xlo = cx0 - (tx0 - 1), xw = cx1 - cx0;
+        const int ylo = cy0 - (ty0 - 1), yh = cy1 - cy0;
+        /* the halo: points within r of the counted cells */
+        const int hx0 = max(cx0 - r, 0), hx1 = min(cx1 - 1 + r, a.w - 1);
+        const int hy0 = max(cy0 - r, 0), hy1 = min(cy1 - 1 + r, a.h - 1);
+        const int ctx0 = hx0 / HL_TILE_W, ctx1 = hx1 / HL_TILE_W;
+        const int cty0 = hy0 / HL_TILE_H, cty1 = hy1 / HL_TILE_H;
+        for (int row0 = cty0; row0 <= cty1; row0 += CT_ROWS) {
+            const int nrow = min(CT_ROWS, cty1 - row0 + 1);
+            /* the halo's compaction tiles of one row are consecutive, and so
+             * are their points */
+            int len = 0;
+            if (tid < nrow) {
+                const int t = (row0 + tid) * a.ctiles_x;
+                const int s0 = a.tile_off[t + ctx0];
+                len = a.tile_off[t + ctx1 + 1] - s0;
+                sm.start[tid] = s0;
             }
+            int v = len;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(FULL, v, o);
+                if (lane >= o)
+                    v += t;
+            }
+            if (lane == 31 && warp < CT_ROWS / 32)
+                sm.red[warp] = v;
+            __syncthreads();
+            if (tid < CT_ROWS) {
+                int off = 0;
+                for (int k = 0; k < warp; k++)
+                    off += sm.red[k];
+                sm.pre[tid + 1] = off + v;
+            }
+            if (tid == 0)
+                sm.pre[0] = 0;
+            __syncthreads();
+            const int total = sm.pre[nrow];
+            for (int i = tid; i < total; i += CT_THREADS) {
+                int lo = 0, hi = nrow - 1;   /* the row k with pre[k] <= i < pre[k + 1] */
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (sm.pre[mid] <= i)
+                        lo = mid;
+                    else
+                        hi = mid - 1;
+                }
+                const float2 pt = a.pts[sm.start[lo] + (i - sm.pre[lo])];
+                if (!(pt.x < 1.0e29f))
+                    continue;   /* the compaction's sentinel of an odd tile */
+                const int px = (int)pt.x, py = (int)pt.y;
+                if (px < hx0 || px > hx1 || py < hy0 || py > hy1)
+                    continue;
+                const int x0 = px - (tx0 - 1), y0 = py - (ty0 - 1);
+                int x = 0, y = r, d = 3 - 2 * r;
+                while (x < y) {
+                    ct_vote(sm.cnt, x0 + x, y0 + y, xlo, xw, ylo, yh);
+                    ct_vote(sm.cnt, x0 + x, y0 - y, xlo, xw, ylo, yh);
+                    ct_vote(sm.cnt, x0 - x, y0 + y, xlo, xw, ylo, yh);
+                    ct_vote(sm.cnt, x0 - x, y0 - y, xlo, xw, ylo, yh);
+                    ct_vote(sm.cnt, x0 + y, y0 + x, xlo, xw, ylo, yh);
+                    ct_vote(sm.cnt, x0 + y, y0 - x, xlo, xw, ylo, yh);
+                    ct_vote(sm.cnt, x0 - y, y0 + x, xlo, xw, ylo, yh);
+                    ct_vote(sm.cnt, x0 - y, y0 - x, xlo, xw, ylo, yh);
+                    if (d < y)
+                        d += 4 * x + 6;
+                    else {
+                        d += 4 * (x - y) + 10;
+                        y--;
+                    }
+                    x++;
+                }
+            }
+            __syncthreads();   /* before the next pass rewrites pre / start */
         }
-        const unsigned b = __ballot_sync(FULL, is);
-        if (!b)
-            continue;
-        int pos = 0;
-        if (lane == 0)
-            pos = atomicAdd(a.ncand, __popc(b));
-        pos = __shfl_sync(FULL, pos, 0) + __popc(b & ((1u << lane) - 1u));
-        if (is) {
-            if (pos < a.cap)
-                a.keys[pos] = ((unsigned long long)(unsigned)v << 32) |
-                              (unsigned)(~(unsigned)i);
-            else
-                atomicOr(a.status, HL_ST_CAND_OVERFLOW);
+    }
+    /* the interior: written out and/or its local maxima taken (cells
+     * outside the ROI were never counted: their zeros are the reference's
+     * border) */
+    const int iw = min(HL_CIRCLE_TW, a.w - tx0), ih = min(HL_CIRCLE_TH, a.h - ty0);
+    const size_t zrow = (size_t)z * a.h;
+    for (int c = tid; c < HL_CIRCLE_TW * HL_CIRCLE_TH; c += CT_THREADS) {
+        const int row = c / HL_CIRCLE_TW, col = c - row * HL_CIRCLE_TW;
+        const bool in = col < iw && row < ih;
+        const int *p = sm.cnt + (row + 1) * CT_AW + (col + 1);
+        const int v = in ? p[0] : 0;
+        if (a.acc && in)
+            a.acc[(zrow + ty0 + row) * a.w + tx0 + col] = v;
+        if (a.keys) {
+            const bool is = in && v > a.threshold && v > p[-1] && v >= p[1] &&
+                            v > p[-CT_AW] && v >= p[CT_AW];
+            const unsigned b = __ballot_sync(FULL, is);
+            if (!b)
+                continue;
+            int pos = 0;
+            if (lane == 0)
+                pos = atomicAdd(a.ncand, __popc(b));
+            pos = __shfl_sync(FULL, pos, 0) + __popc(b & ((1u << lane) - 1u));
+            if (is) {
+                const unsigned idx = (unsigned)((zrow + ty0 + row) * a.w + tx0 + col);
+                if (pos < a.cap)
+                    a.keys[pos] = ((unsigned long long)(unsigned)v << 32) | (unsigned)(~idx);
+                else
+                    atomicOr(a.status, HL_ST_CAND_OVERFLOW);
+            }
         }
     }
 }
@@ -218,23 +300,17 @@ hl_circle_final_kernel(hl_circle_final_args a)
 
 /* ---- launchers ----------------------------------------------------------- */
 
-cudaError_t hl_launch_circle_vote(const hl_circle_vote_args *a, int sms, cudaStream_t s)
+cudaError_t hl_launch_circle_tiles(const hl_circle_tile_args *a, cudaStream_t s)
 {
-    const size_t smem = sizeof(int2) * (size_t)a->ntab;
-    cudaError_t e = cudaFuncSetAttribute(hl_circle_vote_kernel,
+    const size_t smem = sizeof(CircleTileSmem);
+    cudaError_t e = cudaFuncSetAttribute(hl_circle_tile_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return e;
-    return hl_launch_pdl(hl_circle_vote_kernel, dim3(sms * 8), dim3(256), smem, s, false, *a);
-}
-
-cudaError_t hl_launch_circle_peaks(const hl_circle_peak_args *a, int sms, cudaStream_t s)
-{
-    const long long total = (long long)a->nr * a->h * a->w;
-    long long blocks = (total + 255) / 256;
-    if (blocks > (long long)sms * 16)
-        blocks = (long long)sms * 16;
-    return hl_launch_pdl(hl_circle_peaks_kernel, dim3((unsigned)blocks), dim3(256), 0, s,
+    const long long grid = (long long)a->ntx * a->nty * a->nr;
+    if (grid <= 0 || grid > 0x7fffffffLL)
+        return cudaErrorInvalidConfiguration;
+    return hl_launch_pdl(hl_circle_tile_kernel, dim3((unsigned)grid), dim3(CT_THREADS), smem, s,
                          false, *a);
 }
 

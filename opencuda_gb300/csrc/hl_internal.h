@@ -257,23 +257,26 @@ static inline cudaError_t hl_launch_pdl(void (*kernel)(Params...), dim3 grid, di
 #endif
 /* HoughCircle (hl_circle.cu) */
 #define HL_CIRCLE_MAXCAND 4096
-typedef struct hl_circle_vote_args {
+/* One CTA per (accumulator tile, radius): the tile and a one-cell apron are
+ * counted in shared memory from the points of the halo (the compaction tiles
+ * within the radius of the tile); then the interior is written to acc and/or
+ * its local maxima appended to keys. */
+#define HL_CIRCLE_TW 192
+#define HL_CIRCLE_TH 128
+typedef struct hl_circle_tile_args {
     const float2 *pts;        /* the compaction's points (odd tiles padded) */
-    const int *count;         /* entries of pts */
-    const int2 *tab;          /* {radius - rmin, x | y << 16} midpoint steps */
-    int ntab;
+    const int *tile_off;      /* [ctiles_x * ctiles_y + 1] */
+    int ctiles_x, ctiles_y;   /* compaction tiles (HL_TILE_W x HL_TILE_H) */
     int w, h;                 /* ROI */
-    int32_t *acc;             /* [nr][h][w] */
-} hl_circle_vote_args;
-typedef struct hl_circle_peak_args {
-    const int32_t *acc;
-    int nr, w, h;
+    int rmin, nr;
+    int ntx, nty;             /* accumulator tiles */
+    int32_t *acc;             /* [nr][h][w], or NULL */
     int threshold;
-    unsigned long long *keys; /* votes << 32 | ~index */
+    unsigned long long *keys; /* votes << 32 | ~index, or NULL */
     int *ncand;
     int cap;
     int *status;
-} hl_circle_peak_args;
+} hl_circle_tile_args;
 typedef struct hl_circle_final_args {
     const unsigned long long *keys;
     int *ncand;
@@ -286,8 +289,7 @@ typedef struct hl_circle_final_args {
     hl_result_hdr *hdr;
     int *status;
 } hl_circle_final_args;
-cudaError_t hl_launch_circle_vote(const hl_circle_vote_args *a, int sms, cudaStream_t s);
-cudaError_t hl_launch_circle_peaks(const hl_circle_peak_args *a, int sms, cudaStream_t s);
+cudaError_t hl_launch_circle_tiles(const hl_circle_tile_args *a, cudaStream_t s);
 cudaError_t hl_launch_circle_final(const hl_circle_final_args *a, cudaStream_t s);
 
 cudaError_t hl_launch_compact(const hl_compact_args *a, cudaStream_t s);

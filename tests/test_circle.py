@@ -30,6 +30,9 @@ CASES = [
      5, 50, 40, 50.0, 20, 16),
     (256, 256, [(128, 128, 60), (60, 60, 18)], 0.02, None, 40, 64, 60, 20.0, 8, 12),
     (97, 53, [(40, 26, 10)], 0.0, (3, 2, 95, 51), 0, 12, 10, 5.0, 3, 4),
+    # radii near the accumulator tile's size, an ROI over 4 x 3 tiles
+    (700, 330, [(100, 100, 80), (400, 200, 95), (600, 150, 70)], 0.005, (5, 7, 690, 325),
+     60, 100, 80, 30.0, 10, 8),
 ]
 
 
