@@ -20,6 +20,10 @@ top-256 lines: compaction -> vote -> peak NMS -> rank/merge, all on the GPU.
           beside it
   cpu_baseline : the C transcription of the reference's vote loop + host
           tail (oracle/hough_oracle.c) on this host's cores
+  circle : HoughCircle (include/hl_circle.h) at the reference's default
+          parameters on a 1024 x 1024 ring scene: device and e2e images/s,
+          votes against the shared-memory atomic ceiling, the C restatement
+          (oracle/circle_oracle.c) on one core beside it
 
 --impl reference times that CPU transcription alone (the reference's path
 has no CPU implementation of its own; its GPU kernels are the K40-era code
@@ -348,6 +352,76 @@ def proposal_workload(L, HoughLine, Image, dev, sp, kind: int, n: int, reps: int
             "network": "6 conv3x3 (tcgen05), 32 ch, trained on 64K GPU-generated scenes"}
 
 
+def circle_workload(L, Image, dev, sp, atom_peak: float, reps: int, cpu: bool):
+    """HoughCircle::houghcircle at the reference's default parameters (radii
+    5-50, distThres 50, rThres 20, cirThreshold 100), circleMax 32, on a
+    1024 x 1024 scene of 24 rings (radii 8-50) and 1% salt.  Device: CUDA
+    events around the synchronous hl_circles call (compaction, tile vote +
+    local maxima, tail, result copy) with the image resident and L2 flushed
+    between calls.  e2e: host wall time from the host image (pinned) through
+    the upload, hl_circles and the circles on the host.  The votes are the
+    accumulator's sum (the in-ROI midpoint votes), counted once untimed."""
+    import torch
+    import cases
+    from opencuda_gb300.houghcircle import HoughCircle
+    from oracle import oracle as O
+    host = cases.circle_scene(1024, 1024, 24, 8, 50, 10000, 77)
+    h, w = host.shape
+    img = Image.from_host(host, device=dev)
+    pinned = torch.from_numpy(host).pin_memory()
+    hc = HoughCircle()
+    cm = 32
+    votes = int(hc.accumulator(img, stream=sp).sum().item())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(3):
+        rc, got = hc.houghcircle(img, None, cm, stream=sp)
+    if rc != 0:
+        raise RuntimeError(f"hl_circles returned {rc}")
+    torch.cuda.synchronize(dev)
+    ms = []
+    for _ in range(reps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        hc.houghcircle(img, None, cm, stream=sp)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms.append(e0.elapsed_time(e1))
+    t = statistics.median(ms)
+    dst = img.data
+    e2e = []
+    for _ in range(reps):
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        dst.copy_(pinned, non_blocking=True)
+        rc, got = hc.houghcircle(img, None, cm, stream=sp)
+        e2e.append((time.perf_counter() - t0) * 1e3)
+    te = statistics.median(e2e)
+    out = {"workload": "HoughCircle 1024x1024, 24 rings r 8-50 + 1% salt, radii 5-50, "
+                       "distThres 50, rThres 20, cirThreshold 100, circleMax 32",
+           "value": 1e3 / t, "unit": "images/s", "ms_per_image": t,
+           "e2e": {"value": 1e3 / te, "unit": "images/s", "ms_per_image": te,
+                   "h2d_bytes_per_step": int(host.nbytes),
+                   "d2h_bytes_per_step": 16 * (cm + 1)},
+           "edge_pixels": int((host == 255).sum()), "votes": votes, "circles": len(got),
+           "roofline": {"bound": "smem_atomic", "achieved": votes / (t / 1e3) / 1e12,
+                        "peak": atom_peak / 1e12, "unit": "T atomics/s",
+                        "frac": votes / (t / 1e3) / atom_peak,
+                        "note": "whole call (all launches and the result copy) as the time"},
+           "reps": reps, "l2": "flushed between calls"}
+    if cpu:
+        t0 = time.perf_counter()
+        want, _ = O.houghcircle(host, 5, 50, 100, 50.0, 20, cm)
+        tc = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 1 / tc, "unit": "images/s", "cores": 1, "kind": "port",
+                               "sample": "1 image through the C restatement (vote, local "
+                                         "maxima, sort, merge), one thread"}
+        out["matches_oracle"] = [c.astuple() for c in got] == list(want)
+    return out
+
+
 def _lib_mod():
     from opencuda_gb300 import _lib
     return _lib
@@ -566,6 +640,10 @@ def run_gb300(args):
     if not args.no_batch and not args.no_proposal:
         line["proposal"] = [proposal_workload(L, HoughLine, Image, dev, sp, 4, 128, 5),
                             proposal_workload(L, HoughLine, Image, dev, sp, 5, 1024, 3)]
+    if not args.no_circle:
+        line["circle"] = circle_workload(L, Image, dev, sp, atom.value,
+                                         min(max(args.steps, 5), 50),
+                                         ws == 1 and not args.no_cpu_baseline)
     if ws == 1 and not args.no_cpu_baseline:
         n, el, v, cores = cpu_reference_images(imgs_host, args.cpu_budget)
         line["cpu_baseline"] = {"value": n / el, "unit": "images/s", "cores": cores,
@@ -591,6 +669,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the batched (256 uneven images) measurement")
+    ap.add_argument("--no-circle", action="store_true",
+                    help="skip the HoughCircle measurement")
     ap.add_argument("--no-proposal", action="store_true",
                     help="skip the proposal-guided measurements")
     args = ap.parse_args()

@@ -16,6 +16,7 @@ HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "libhough_oracle.so"
 REF_RUNNER = HERE / "_build" / "libref_runner.so"
 REF_FATBIN = HERE / "_ref" / "houghline_ref.fatbin"
+REF_CIRCLE_FATBIN = HERE / "_ref" / "houghcircle_ref.fatbin"
 
 RANK_CANONICAL = 0
 RANK_REF_SHELL = 1

@@ -1,14 +1,15 @@
 /*
  * ref_runner.c -- runs the REFERENCE's own vote and draw kernels
  * (okano_3_0/HoughLine.cu:86-130 _houghlineImgKer, :133-165
- * _houghlineCorKer, :216-249 _houghoutKer) from the fatbin that
- * oracle/build_ref.sh compiles out of the reference sources, through the CUDA
- * driver API.  TEST INFRASTRUCTURE ONLY: it produces golden accumulators that
+ * _houghlineCorKer, :216-249 _houghoutKer; okano_3_0/HoughCircle.cu:187-245
+ * _houghcirImgKer) from the fatbins that oracle/build_ref.sh compiles out of
+ * the reference sources, through the CUDA driver API.  TEST INFRASTRUCTURE ONLY: it produces golden accumulators that
  * pin the CPU oracle (tests/golden/make_golden.py).
  *
- * The reference's peak kernel _findlocalMaxKer is deliberately never run: its
- * grid is rounded up and it has no bounds check (:791-798, :174-206), so it
- * writes outside its buffer.
+ * The reference's peak kernels are deliberately never run: their grids are
+ * rounded up and they have no bounds check, so they write outside their
+ * buffers (_findlocalMaxKer, okano_3_0/HoughLine.cu:791-798, :174-206;
+ * _findpartmaxKer, okano_3_0/HoughCircle.cu:321-370, launched at :993).
  *
  * Kernel argument structs restate the layouts of Image / ImageCuda
  * (okano_3_0/Image.h:44-78) and Template (okano_3_0/Template.h:14-20).
@@ -42,8 +43,8 @@ typedef struct {
     int votes;
 } ref_LineParam;
 
-static CUmodule g_mod;
-static CUfunction g_img, g_cor, g_out;
+static CUmodule g_mod, g_cmod;
+static CUfunction g_img, g_cor, g_out, g_cvote;
 static char g_err[512];
 
 const char *rr_error(void) { return g_err; }
@@ -61,14 +62,14 @@ const char *rr_error(void) { return g_err; }
     } while (0)
 
 /* Find a kernel by a fragment of its name among the module's functions. */
-static int find_fn(const char *frag, CUfunction *out)
+static int find_fn(CUmodule mod, const char *frag, CUfunction *out)
 {
     unsigned n = 0;
-    DCK(cuModuleGetFunctionCount(&n, g_mod));
+    DCK(cuModuleGetFunctionCount(&n, mod));
     CUfunction *fs = (CUfunction *)calloc(n ? n : 1, sizeof(CUfunction));
     if (!fs)
         return -6;
-    CUresult r = cuModuleEnumerateFunctions(fs, n, g_mod);
+    CUresult r = cuModuleEnumerateFunctions(fs, n, mod);
     if (r != CUDA_SUCCESS) {
         free(fs);
         snprintf(g_err, sizeof(g_err), "cuModuleEnumerateFunctions failed");
@@ -103,12 +104,79 @@ int rr_init(const char *fatbin_path)
     DCK(cuDevicePrimaryCtxRetain(&ctx, dev));
     DCK(cuCtxSetCurrent(ctx));
     DCK(cuModuleLoad(&g_mod, fatbin_path));
-    if (find_fn("_houghlineImgKer", &g_img))
+    if (find_fn(g_mod, "_houghlineImgKer", &g_img))
         return -7;
-    if (find_fn("_houghlineCorKer", &g_cor))
+    if (find_fn(g_mod, "_houghlineCorKer", &g_cor))
         return -7;
-    if (find_fn("_houghoutKer", &g_out))
+    if (find_fn(g_mod, "_houghoutKer", &g_out))
         return -7;
+    return 0;
+}
+
+/* Load the HoughCircle fatbin into the same context (after rr_init). */
+int rr_init_circle(const char *fatbin_path)
+{
+    if (g_cmod)
+        return 0;
+    if (!g_mod) {
+        snprintf(g_err, sizeof(g_err), "rr_init has not run");
+        return -7;
+    }
+    DCK(cuModuleLoad(&g_cmod, fatbin_path));
+    if (find_fn(g_cmod, "_houghcirImgKer", &g_cvote))
+        return -7;
+    return 0;
+}
+
+/* Vote an ROI of a host image with the reference's _houghcirImgKer, launched
+ * as okano_3_0/HoughCircle.cu:964-977 does (32 x 8 blocks over the ROI, one
+ * grid layer per radius, the ROI sub-image of :956).  acc receives the
+ * reference's zero-bordered buffer, (rmax - rmin + 1) planes of
+ * (roi_h + 2) x (roi_w + 2) ints. */
+int rr_circle_vote(const uint8_t *img, int width, int height, long pitch,
+                   int x1, int y1, int x2, int y2, int rmin, int rmax, int32_t *acc)
+{
+    int bw = x2 - x1, bh = y2 - y1;
+    const int nr = rmax - rmin + 1;
+    if (!g_cvote || bw <= 0 || bh <= 0 || rmin < 0 || nr <= 0 || nr > 65535) {
+        snprintf(g_err, sizeof(g_err), "bad circle vote arguments");
+        return -1;
+    }
+    size_t dpitch = ((size_t)width + 511) / 512 * 512;
+    size_t accn = (size_t)nr * (size_t)(bw + 2) * (size_t)(bh + 2);
+    CUdeviceptr dimg = 0, dacc = 0;
+    DCK(cuMemAlloc(&dimg, dpitch * (size_t)height));
+    DCK(cuMemAlloc(&dacc, accn * 4));
+    DCK(cuMemsetD32(dacc, 0, accn));
+    CUDA_MEMCPY2D cp;
+    memset(&cp, 0, sizeof(cp));
+    cp.srcMemoryType = CU_MEMORYTYPE_HOST;
+    cp.srcHost = img;
+    cp.srcPitch = (size_t)pitch;
+    cp.dstMemoryType = CU_MEMORYTYPE_DEVICE;
+    cp.dstDevice = dimg;
+    cp.dstPitch = dpitch;
+    cp.WidthInBytes = (size_t)width;
+    cp.Height = (size_t)height;
+    DCK(cuMemcpy2D(&cp));
+    ref_ImageCuda sub;
+    memset(&sub, 0, sizeof(sub));
+    sub.imgMeta.width = (size_t)bw;
+    sub.imgMeta.height = (size_t)bh;
+    sub.imgMeta.roiX1 = x1;
+    sub.imgMeta.roiY1 = y1;
+    sub.imgMeta.roiX2 = x2;
+    sub.imgMeta.roiY2 = y2;
+    sub.imgMeta.imgData = (unsigned char *)(uintptr_t)(dimg + (size_t)y1 * dpitch + (size_t)x1);
+    sub.pitchBytes = dpitch;
+    int radius_min = rmin;
+    void *args[] = {&sub, &dacc, &radius_min, &bw, &bh};
+    DCK(cuLaunchKernel(g_cvote, (unsigned)((bw + 31) / 32), (unsigned)((bh + 7) / 8),
+                       (unsigned)nr, 32, 8, 1, 0, 0, args, NULL));
+    DCK(cuCtxSynchronize());
+    DCK(cuMemcpyDtoH(acc, dacc, accn * 4));
+    cuMemFree(dimg);
+    cuMemFree(dacc);
     return 0;
 }
 

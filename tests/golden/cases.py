@@ -72,6 +72,59 @@ def synth_custom(w: int, h: int, nseg: int, lmin: int, lmax: int, ppm: int,
     return img
 
 
+def circle_scene(w: int, h: int, ncircles: int, rmin: int, rmax: int, ppm: int,
+                 seed: int) -> np.ndarray:
+    """Rings drawn with the integer Bresenham circle (d < 0 rule, so not the
+    vote's own step rule), radii in [rmin, rmax], centres anywhere in the
+    image, plus ppm salt pixels per million; integer-only."""
+    rng = _splitmix(seed)
+    img = np.zeros((h, w), np.uint8)
+    for _ in range(ncircles):
+        r = rmin + next(rng) % (rmax - rmin + 1)
+        a, b = next(rng) % w, next(rng) % h
+        x, y, d = 0, r, 3 - 2 * r
+        pts = []
+        while x <= y:
+            pts += [(a + x, b + y), (a + x, b - y), (a - x, b + y), (a - x, b - y),
+                    (a + y, b + x), (a + y, b - x), (a - y, b + x), (a - y, b - x)]
+            if d < 0:
+                d += 4 * x + 6
+            else:
+                d += 4 * (x - y) + 10
+                y -= 1
+            x += 1
+        for px, py in pts:
+            if 0 <= px < w and 0 <= py < h:
+                img[py, px] = 255
+    for _ in range(w * h * ppm // 1_000_000):
+        img[next(rng) % h, next(rng) % w] = 255
+    return img
+
+
+# HoughCircle parity cases: the ring scene's recipe, the ROI (None: the whole
+# image) and the voted radius range
+CIRCLE_CASES = {
+    "circ_160x120": dict(w=160, h=120, n=3, dr=(8, 40), ppm=5000, seed=5, roi=None,
+                         r=(5, 30)),
+    "circ_roi_300x200": dict(w=300, h=200, n=6, dr=(5, 60), ppm=10000, seed=6,
+                             roi=(17, 11, 283, 190), r=(5, 50)),
+    "circ_r0_97x53": dict(w=97, h=53, n=2, dr=(3, 20), ppm=20000, seed=7,
+                          roi=(3, 2, 95, 51), r=(0, 12)),
+    "circ_700x330": dict(w=700, h=330, n=5, dr=(60, 100), ppm=5000, seed=8,
+                         roi=(5, 7, 690, 325), r=(60, 100)),
+    "circ_1024": dict(w=1024, h=1024, n=24, dr=(8, 50), ppm=10000, seed=77, roi=None,
+                      r=(5, 50)),
+}
+
+
+def circle_case_image(c: dict) -> np.ndarray:
+    return circle_scene(c["w"], c["h"], c["n"], c["dr"][0], c["dr"][1], c["ppm"], c["seed"])
+
+
+def circle_case_roi(c: dict) -> tuple[int, int, int, int]:
+    return tuple(c["roi"]) if c["roi"] else (0, 0, c["w"], c["h"])
+
+
 def kat(name: str) -> np.ndarray:
     if name == "vertical":
         img = np.zeros((48, 64), np.uint8)

@@ -1,16 +1,19 @@
 """Generate the golden fixtures in this directory on a GB300.
 
 Runs the REFERENCE's own kernels -- _houghlineImgKer, _houghlineCorKer and
-_houghoutKer from okano_3_0/HoughLine.cu, compiled for sm_103a by
-oracle/build_ref.sh into oracle/_ref/houghline_ref.fatbin -- on every case of
-cases.py and records a hash of each result, plus the cos/sin tables the GPU
-evaluates (CUDA's cosf/sinf at theta_k = (float)(k * detheta)).
+_houghoutKer from okano_3_0/HoughLine.cu, and _houghcirImgKer from
+okano_3_0/HoughCircle.cu, compiled for sm_103a by oracle/build_ref.sh into
+oracle/_ref/ -- on every case of cases.py and records a hash of each result,
+plus the cos/sin tables the GPU evaluates (CUDA's cosf/sinf at
+theta_k = (float)(k * detheta)).
 
-    python tests/golden/make_golden.py OUT_DIR
+    python tests/golden/make_golden.py OUT_DIR [--circle-only]
 
 writes OUT_DIR/golden.json and OUT_DIR/trig_tables.npz; the committed copies
-in tests/golden/ came from such a run.  The reference's peak kernel
-_findlocalMaxKer is never run (it writes outside its buffer).
+in tests/golden/ came from such a run (--circle-only recomputes the circle
+records alone, keeping the rest of the committed golden.json).  The
+reference's peak kernels _findlocalMaxKer and _findpartmaxKer are never run
+(they write outside their buffers).
 """
 from __future__ import annotations
 
@@ -54,7 +57,39 @@ def table_for(tables: dict, detheta: float):
     return tables[f"cos_T{T}"], tables[f"sin_T{T}"]
 
 
-def main(out_dir: str) -> int:
+def circle_golden(rr) -> dict:
+    """The reference's circle vote on every circle case against the oracle's:
+    the reference's buffer has a one-cell zero border per radius plane
+    (okano_3_0/HoughCircle.cu:170-179); its interior is the oracle layout."""
+    rc = rr.rr_init_circle(str(O.REF_CIRCLE_FATBIN).encode())
+    if rc != 0:
+        raise RuntimeError("rr_init_circle failed: " + rr.rr_error().decode())
+    out = {}
+    for name, c in cases.CIRCLE_CASES.items():
+        img = cases.circle_case_image(c)
+        h, w = img.shape
+        x1, y1, x2, y2 = cases.circle_case_roi(c)
+        rmin, rmax = c["r"]
+        nr, rw, rh = rmax - rmin + 1, x2 - x1, y2 - y1
+        ref = np.zeros((nr, rh + 2, rw + 2), np.int32)
+        rc = rr.rr_circle_vote(C.c_void_p(img.ctypes.data), w, h, w, x1, y1, x2, y2,
+                               rmin, rmax, C.c_void_p(ref.ctypes.data))
+        if rc != 0:
+            raise RuntimeError(name + ": reference kernel failed: " + rr.rr_error().decode())
+        inner = np.ascontiguousarray(ref[:, 1:-1, 1:-1])
+        mine = O.circle_vote(np.ascontiguousarray(img[y1:y2, x1:x2]), rmin, rmax)
+        rec = {"w": w, "h": h, "roi": [x1, y1, x2, y2], "rmin": rmin, "rmax": rmax,
+               "fnv_image": O.fnv1a(img), "fnv_ref_acc": O.fnv1a(inner),
+               "sum": int(inner.sum(dtype=np.int64)), "max": int(inner.max()),
+               "border_zero": bool(int(ref.sum(dtype=np.int64)) == int(inner.sum(dtype=np.int64))),
+               "edge_points": int((img[y1:y2, x1:x2] == 255).sum()),
+               "oracle_equal": bool(np.array_equal(mine, inner))}
+        out[name] = rec
+        print(name, "oracle_equal" if rec["oracle_equal"] else "DIFFERS", rec["sum"])
+    return out
+
+
+def main(out_dir: str, circle_only: bool = False) -> int:
     out = Path(out_dir)
     out.mkdir(parents=True, exist_ok=True)
     build.build_library()
@@ -62,6 +97,8 @@ def main(out_dir: str) -> int:
     runner = build.build_ref_runner()
     rr = C.CDLL(str(runner))
     rr.rr_error.restype = C.c_char_p
+    rr.rr_circle_vote.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_long, C.c_int, C.c_int,
+                                  C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
     rr.rr_vote_image.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_long, C.c_int,
                                  C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                  C.c_void_p]
@@ -73,6 +110,12 @@ def main(out_dir: str) -> int:
     if rc != 0:
         print("rr_init failed:", rr.rr_error().decode())
         return 1
+    if circle_only:
+        golden = json.loads((HERE / "golden.json").read_text())
+        golden["circle"] = circle_golden(rr)
+        with open(out / "golden.json", "w") as f:
+            json.dump(golden, f, indent=1, sort_keys=True)
+        return 0 if all(r["oracle_equal"] for r in golden["circle"].values()) else 1
     tables = trig_tables()
     np.savez(out / "trig_tables.npz", **tables)
     golden = {"cases": {}, "tables": {}}
@@ -163,6 +206,7 @@ def main(out_dir: str) -> int:
     golden["draw"] = {"case": "cfg1_s1234", "lines": [[float(a), int(d)] for a, d in zip(ang, dist)],
                       "fnv_image": O.fnv1a(drawn), "lit": int((drawn == 255).sum())}
     np.save(out / "draw_cfg1.npy", drawn)
+    golden["circle"] = circle_golden(rr)
     with open(out / "golden.json", "w") as f:
         json.dump(golden, f, indent=1, sort_keys=True)
     bad = [n for n, r in golden["cases"].items() if not r["oracle_equal"]]
@@ -171,4 +215,6 @@ def main(out_dir: str) -> int:
 
 
 if __name__ == "__main__":
-    sys.exit(main(sys.argv[1] if len(sys.argv) > 1 else str(ROOT / "gpurun_out" / "golden")))
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    sys.exit(main(args[0] if args else str(ROOT / "gpurun_out" / "golden"),
+                  circle_only="--circle-only" in sys.argv))

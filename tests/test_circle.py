@@ -125,3 +125,22 @@ def test_circle_guidingset(hc_mod):
     pim[ys, xs] = 255
     want, _ = O.houghcircle(pim, 10, 30, 40, 10.0, 5, 4)
     assert [c.astuple() for c in got] == list(want) and got
+
+
+def test_accumulator_matches_reference_kernel(hc_mod):
+    """The GPU accumulator against the hash of the reference's own
+    _houghcirImgKer on the committed circle scenes."""
+    import json
+    import sys
+    from pathlib import Path
+    HoughCircle, Image, _ = hc_mod
+    here = Path(__file__).resolve().parent / "golden"
+    sys.path.insert(0, str(here))
+    import cases
+    gold = json.loads((here / "golden.json").read_text())["circle"]
+    for name, c in cases.CIRCLE_CASES.items():
+        img = cases.circle_case_image(c)
+        rmin, rmax = c["r"]
+        acc = HoughCircle(rmin, rmax).accumulator(
+            Image.from_host(img, cases.circle_case_roi(c))).cpu().numpy()
+        assert O.fnv1a(np.ascontiguousarray(acc)) == gold[name]["fnv_ref_acc"], name

@@ -47,3 +47,31 @@ def test_known_circles_found():
     for a, b, r in [(70, 80, 25), (150, 60, 15)]:
         assert any(abs(c[0] - a) <= 1 and abs(c[1] - b) <= 1 and abs(c[2] - r) <= 1
                    for c in got), (a, b, r, got)
+
+
+def _golden_circle():
+    import json
+    from pathlib import Path
+    g = json.loads((Path(__file__).resolve().parent / "golden" / "golden.json").read_text())
+    return g["circle"]
+
+
+def test_oracle_vote_matches_reference_kernel():
+    """The oracle's accumulator against the hash of the reference's own
+    _houghcirImgKer (okano_3_0/HoughCircle.cu:187-245) on the same scenes,
+    recorded on a GB300 by tests/golden/make_golden.py."""
+    import sys
+    from pathlib import Path
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    import cases
+    gold = _golden_circle()
+    assert set(gold) == set(cases.CIRCLE_CASES)
+    for name, c in cases.CIRCLE_CASES.items():
+        rec = gold[name]
+        assert rec["oracle_equal"] and rec["border_zero"], name
+        img = cases.circle_case_image(c)
+        assert O.fnv1a(img) == rec["fnv_image"], name
+        x1, y1, x2, y2 = cases.circle_case_roi(c)
+        acc = O.circle_vote(img[y1:y2, x1:x2], *c["r"])
+        assert int(acc.sum(dtype=np.int64)) == rec["sum"], name
+        assert O.fnv1a(acc) == rec["fnv_ref_acc"], name
