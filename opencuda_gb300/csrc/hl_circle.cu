@@ -32,25 +32,74 @@
 
 /* ---- vote + local maxima ------------------------------------------------- */
 
-#define CT_AW (HL_CIRCLE_TW + 2)
+/* local cell (x, y) is image cell (x + tx0 - CT_OX, y + ty0 - 1): the
+ * interior starts on a 16-byte boundary of every row, the apron is the column
+ * before and after it and the rows above and below */
+#define CT_OX 4
+#define CT_AW (HL_CIRCLE_TW + 8)
 #define CT_AH (HL_CIRCLE_TH + 2)
+#define CT_CELLS (CT_AH * CT_AW)
 #define CT_THREADS 512
+#define CT_WARPS (CT_THREADS / 32)
 #define CT_ROWS 256   /* compaction-tile rows of the halo taken per pass */
 
 struct CircleTileSmem {
-    int cnt[CT_AH * CT_AW];   /* the tile and its apron, row-major */
+    int cnt[CT_CELLS];        /* the tile and its apron, row-major */
     int pre[CT_ROWS + 1];     /* points of the halo rows before each row */
     int start[CT_ROWS];       /* first point of each halo row */
-    int red[CT_THREADS / 32];
+    int red[CT_WARPS];
+    unsigned char rank_lane[CT_WARPS][32];   /* lane of the k-th queued point */
 };
 
-/* one vote at local cell (x, y) when it lies in [xlo, xhi) x [ylo, yhi) */
-__device__ __forceinline__ void ct_vote(int *cnt, int x, int y, int xlo, int xw, int ylo,
-                                        int yh)
+/* one vote at the shared-memory word addr when p holds: a predicated
+ * red.shared, so a warp's eight octant votes of a step issue without a
+ * branch around each */
+__device__ __forceinline__ void ct_red(unsigned addr, bool p)
 {
-    if ((unsigned)(x - xlo) < (unsigned)xw && (unsigned)(y - ylo) < (unsigned)yh)
-        atomicAdd(cnt + y * CT_AW + x, 1);
+    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.b32 q, %1, 0;\n\t@q red.shared.add.u32 [%0], 1;\n\t}"
+                 :: "r"(addr), "r"((int)p) : "memory");
 }
+
+/* Each lane walks the midpoint circle of radius r around its point (x0, y0)
+ * (okano_3_0/HoughCircle.cu:214-243) and votes the octant points that fall in
+ * [0, xw) x [0, yh); pbase is the shared address of that region's origin.
+ * The warp's lanes share r, so the loop and its d < y branch are uniform. */
+__device__ __forceinline__ void ct_walk(int x0, int y0, int r, int xw, int yh, unsigned pbase)
+{
+    int x = 0, y = r, d = 3 - 2 * r;
+    while (x < y) {
+        const int xa = x0 + x, xb = x0 - x, xc = x0 + y, xd = x0 - y;
+        const int ya = y0 + y, yb = y0 - y, yc = y0 + x, yd = y0 - x;
+        const bool fxa = (unsigned)xa < (unsigned)xw, fxb = (unsigned)xb < (unsigned)xw;
+        const bool fxc = (unsigned)xc < (unsigned)xw, fxd = (unsigned)xd < (unsigned)xw;
+        const bool fya = (unsigned)ya < (unsigned)yh, fyb = (unsigned)yb < (unsigned)yh;
+        const bool fyc = (unsigned)yc < (unsigned)yh, fyd = (unsigned)yd < (unsigned)yh;
+        const unsigned ra = pbase + 4u * (unsigned)(ya * CT_AW);
+        const unsigned rb = pbase + 4u * (unsigned)(yb * CT_AW);
+        const unsigned rc = pbase + 4u * (unsigned)(yc * CT_AW);
+        const unsigned rd = pbase + 4u * (unsigned)(yd * CT_AW);
+        /* okano_3_0/HoughCircle.cu:227-234 */
+        ct_red(ra + 4u * (unsigned)xa, fxa && fya);
+        ct_red(rb + 4u * (unsigned)xa, fxa && fyb);
+        ct_red(ra + 4u * (unsigned)xb, fxb && fya);
+        ct_red(rb + 4u * (unsigned)xb, fxb && fyb);
+        ct_red(rc + 4u * (unsigned)xc, fxc && fyc);
+        ct_red(rd + 4u * (unsigned)xc, fxc && fyd);
+        ct_red(rc + 4u * (unsigned)xd, fxd && fyc);
+        ct_red(rd + 4u * (unsigned)xd, fxd && fyd);
+        if (d < y)
+            d += 4 * x + 6;
+        else {
+            d += 4 * (x - y) + 10;
+            y--;
+        }
+        x++;
+    }
+}
+
+/* a point no vote of which lands in the counted cells (an idle lane): every
+ * coordinate stays negative for radii below 65536, and y * CT_AW fits an int */
+#define CT_NOWHERE (-(1 << 20))
 
 __global__ void __launch_bounds__(CT_THREADS, 2)
 hl_circle_tile_kernel(hl_circle_tile_args a)
@@ -63,25 +112,27 @@ hl_circle_tile_kernel(hl_circle_tile_args a)
     const int tile = (int)(blockIdx.x % (unsigned)ntile);
     const int r = a.rmin + z;
     const int tx0 = (tile % a.ntx) * HL_CIRCLE_TW, ty0 = (tile / a.ntx) * HL_CIRCLE_TH;
-    /* counted cells, image coordinates: the tile and its apron within the ROI;
-     * local cell (x, y) is image cell (x + tx0 - 1, y + ty0 - 1) */
+    /* counted cells, image coordinates: the tile and its apron within the ROI */
     const int cx0 = max(tx0 - 1, 0), cy0 = max(ty0 - 1, 0);
     const int cx1 = min(tx0 + HL_CIRCLE_TW + 1, a.w), cy1 = min(ty0 + HL_CIRCLE_TH + 1, a.h);
     {
         int4 *c4 = reinterpret_cast<int4 *>(sm.cnt);
-        for (int i = tid; i < CT_AH * CT_AW / 4; i += CT_THREADS)
+        for (int i = tid; i < CT_CELLS / 4; i += CT_THREADS)
             c4[i] = make_int4(0, 0, 0, 0);
     }
     hl_pdl_begin();
     __syncthreads();
     if (r > 0) {
-        const int xlo = cx0 - (tx0 - 1), xw = cx1 - cx0;
-        const int ylo = cy0 - (ty0 - 1), yh = cy1 - cy0;
+        const int xlo = cx0 - tx0 + CT_OX, xw = cx1 - cx0;
+        const int ylo = cy0 - ty0 + 1, yh = cy1 - cy0;
+        const unsigned pbase = (unsigned)__cvta_generic_to_shared(sm.cnt) +
+                               4u * (unsigned)(ylo * CT_AW + xlo);
         /* the halo: points within r of the counted cells */
         const int hx0 = max(cx0 - r, 0), hx1 = min(cx1 - 1 + r, a.w - 1);
         const int hy0 = max(cy0 - r, 0), hy1 = min(cy1 - 1 + r, a.h - 1);
         const int ctx0 = hx0 / HL_TILE_W, ctx1 = hx1 / HL_TILE_W;
         const int cty0 = hy0 / HL_TILE_H, cty1 = hy1 / HL_TILE_H;
+        int qx = CT_NOWHERE, qy = CT_NOWHERE, qn = 0;   /* the warp's queue: lanes < qn */
         for (int row0 = cty0; row0 <= cty1; row0 += CT_ROWS) {
             const int nrow = min(CT_ROWS, cty1 - row0 + 1);
             /* the halo's compaction tiles of one row are consecutive, and so
@@ -113,72 +164,117 @@ hl_circle_tile_kernel(hl_circle_tile_args a)
                 sm.pre[0] = 0;
             __syncthreads();
             const int total = sm.pre[nrow];
-            for (int i = tid; i < total; i += CT_THREADS) {
-                int lo = 0, hi = nrow - 1;   /* the row k with pre[k] <= i < pre[k + 1] */
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (sm.pre[mid] <= i)
-                        lo = mid;
-                    else
-                        hi = mid - 1;
-                }
-                const float2 pt = a.pts[sm.start[lo] + (i - sm.pre[lo])];
-                if (!(pt.x < 1.0e29f))
-                    continue;   /* the compaction's sentinel of an odd tile */
-                const int px = (int)pt.x, py = (int)pt.y;
-                if (px < hx0 || px > hx1 || py < hy0 || py > hy1)
-                    continue;
-                const int x0 = px - (tx0 - 1), y0 = py - (ty0 - 1);
-                int x = 0, y = r, d = 3 - 2 * r;
-                while (x < y) {
-                    ct_vote(sm.cnt, x0 + x, y0 + y, xlo, xw, ylo, yh);
-                    ct_vote(sm.cnt, x0 + x, y0 - y, xlo, xw, ylo, yh);
-                    ct_vote(sm.cnt, x0 - x, y0 + y, xlo, xw, ylo, yh);
-                    ct_vote(sm.cnt, x0 - x, y0 - y, xlo, xw, ylo, yh);
-                    ct_vote(sm.cnt, x0 + y, y0 + x, xlo, xw, ylo, yh);
-                    ct_vote(sm.cnt, x0 + y, y0 - x, xlo, xw, ylo, yh);
-                    ct_vote(sm.cnt, x0 - y, y0 + x, xlo, xw, ylo, yh);
-                    ct_vote(sm.cnt, x0 - y, y0 - x, xlo, xw, ylo, yh);
-                    if (d < y)
-                        d += 4 * x + 6;
-                    else {
-                        d += 4 * (x - y) + 10;
-                        y--;
+            /* a warp takes 32 consecutive candidates at a time and queues
+             * those inside the halo, one per lane; a full queue walks its 32
+             * circles at once */
+            for (int ib = warp * 32; ib < total; ib += CT_THREADS) {
+                const int i = ib + lane;
+                int cx = CT_NOWHERE, cy = CT_NOWHERE;
+                bool ok = false;
+                if (i < total) {
+                    int lo = 0, hi = nrow - 1;   /* the row k with pre[k] <= i < pre[k + 1] */
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (sm.pre[mid] <= i)
+                            lo = mid;
+                        else
+                            hi = mid - 1;
                     }
-                    x++;
+                    const float2 pt = a.pts[sm.start[lo] + (i - sm.pre[lo])];
+                    /* the compaction's sentinel of an odd tile is 1e30 */
+                    if (pt.x < 1.0e29f) {
+                        const int px = (int)pt.x, py = (int)pt.y;
+                        ok = px >= hx0 && px <= hx1 && py >= hy0 && py <= hy1;
+                        cx = px - tx0 + CT_OX - xlo;
+                        cy = py - ty0 + 1 - ylo;
+                    }
                 }
+                const unsigned vm = __ballot_sync(FULL, ok);
+                const int nv = __popc(vm);
+                if (ok)
+                    sm.rank_lane[warp][__popc(vm & ((1u << lane) - 1u))] = (unsigned char)lane;
+                __syncwarp();
+                /* slots [qn, qn + take) take the first ranks */
+                const int take = min(32 - qn, nv);
+                const bool fill = lane >= qn && lane - qn < take;
+                int src = fill ? sm.rank_lane[warp][lane - qn] : lane;
+                int nx = __shfl_sync(FULL, cx, src), ny = __shfl_sync(FULL, cy, src);
+                if (fill) {
+                    qx = nx;
+                    qy = ny;
+                }
+                qn += take;
+                if (qn == 32) {
+                    ct_walk(qx, qy, r, xw, yh, pbase);
+                    /* the ranks left over start the next queue */
+                    const int rem = nv - take;
+                    const bool f2 = lane < rem;
+                    src = f2 ? sm.rank_lane[warp][take + lane] : lane;
+                    nx = __shfl_sync(FULL, cx, src);
+                    ny = __shfl_sync(FULL, cy, src);
+                    qx = f2 ? nx : CT_NOWHERE;
+                    qy = f2 ? ny : CT_NOWHERE;
+                    qn = rem;
+                }
+                __syncwarp();   /* rank_lane is rewritten by the next batch */
             }
             __syncthreads();   /* before the next pass rewrites pre / start */
         }
+        if (qn > 0)
+            ct_walk(qx, qy, r, xw, yh, pbase);
     }
+    __syncthreads();
     /* the interior: written out and/or its local maxima taken (cells
      * outside the ROI were never counted: their zeros are the reference's
-     * border) */
+     * border).  A warp takes whole rows, a lane four cells of one 16-byte
+     * load; the neighbour tests run only where one of the four is above the
+     * threshold. */
     const int iw = min(HL_CIRCLE_TW, a.w - tx0), ih = min(HL_CIRCLE_TH, a.h - ty0);
     const size_t zrow = (size_t)z * a.h;
-    for (int c = tid; c < HL_CIRCLE_TW * HL_CIRCLE_TH; c += CT_THREADS) {
-        const int row = c / HL_CIRCLE_TW, col = c - row * HL_CIRCLE_TW;
-        const bool in = col < iw && row < ih;
-        const int *p = sm.cnt + (row + 1) * CT_AW + (col + 1);
-        const int v = in ? p[0] : 0;
-        if (a.acc && in)
-            a.acc[(zrow + ty0 + row) * a.w + tx0 + col] = v;
-        if (a.keys) {
-            const bool is = in && v > a.threshold && v > p[-1] && v >= p[1] &&
-                            v > p[-CT_AW] && v >= p[CT_AW];
-            const unsigned b = __ballot_sync(FULL, is);
-            if (!b)
+    for (int row = warp; row < ih; row += CT_WARPS) {
+        const int *prow = sm.cnt + (row + 1) * CT_AW + CT_OX;
+        for (int c0 = 0; c0 < iw; c0 += 128) {
+            const int col = c0 + 4 * lane;
+            int4 q = make_int4(0, 0, 0, 0);
+            if (col < iw)
+                q = *reinterpret_cast<const int4 *>(prow + col);
+            if (a.acc) {
+                int32_t *g = a.acc + (zrow + ty0 + row) * a.w + tx0 + col;
+                const int vv[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+                for (int e = 0; e < 4; e++)
+                    if (col + e < iw)
+                        g[e] = vv[e];
+            }
+            if (!a.keys)
                 continue;
-            int pos = 0;
-            if (lane == 0)
-                pos = atomicAdd(a.ncand, __popc(b));
-            pos = __shfl_sync(FULL, pos, 0) + __popc(b & ((1u << lane) - 1u));
-            if (is) {
-                const unsigned idx = (unsigned)((zrow + ty0 + row) * a.w + tx0 + col);
-                if (pos < a.cap)
-                    a.keys[pos] = ((unsigned long long)(unsigned)v << 32) | (unsigned)(~idx);
-                else
-                    atomicOr(a.status, HL_ST_CAND_OVERFLOW);
+            const int m = max(max(q.x, q.y), max(q.z, q.w));
+            if (!__any_sync(FULL, m > a.threshold))
+                continue;
+            const int vv[4] = {q.x, q.y, q.z, q.w};
+            unsigned mine = 0;
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int *p = prow + col + e;
+                const int v = vv[e];
+                if (col + e < iw && v > a.threshold && v > p[-1] && v >= p[1] &&
+                    v > p[-CT_AW] && v >= p[CT_AW])
+                    mine |= 1u << e;
+            }
+            const int cnt = __popc(mine);
+            int pos = cnt ? atomicAdd(a.ncand, cnt) : 0;
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                if (mine & (1u << e)) {
+                    const unsigned idx =
+                        (unsigned)((zrow + ty0 + row) * a.w + tx0 + col + e);
+                    if (pos < a.cap)
+                        a.keys[pos] = ((unsigned long long)(unsigned)vv[e] << 32) |
+                                      (unsigned)(~idx);
+                    else
+                        atomicOr(a.status, HL_ST_CAND_OVERFLOW);
+                    pos++;
+                }
             }
         }
     }

@@ -144,3 +144,20 @@ def test_accumulator_matches_reference_kernel(hc_mod):
         acc = HoughCircle(rmin, rmax).accumulator(
             Image.from_host(img, cases.circle_case_roi(c))).cpu().numpy()
         assert O.fnv1a(np.ascontiguousarray(acc)) == gold[name]["fnv_ref_acc"], name
+
+
+def test_radii_across_the_table_limit(hc_mod):
+    """Radii 1452-1457: the tile kernel tabulates the midpoint circle up to
+    radius 1454 and walks it per point above that; both against the oracle."""
+    HoughCircle, Image, _ = hc_mod
+    rng = np.random.default_rng(5)
+    img = np.zeros((400, 2960), np.uint8)
+    img[rng.random(img.shape) < 3e-4] = 255
+    yy, xx = np.mgrid[0:400, 0:2960]
+    img[np.abs(np.hypot(xx - 1480, yy - 1655) - 1455) < 0.5] = 255
+    acc = HoughCircle(1452, 1457).accumulator(Image.from_host(img)).cpu().numpy()
+    want = O.circle_vote(img, 1452, 1457)
+    assert np.array_equal(acc, want)
+    rc, got = HoughCircle(1452, 1457, 20.0, 3, 3).houghcircle(Image.from_host(img), None, 16)
+    want_c, _ = O.houghcircle(img, 1452, 1457, 3, 20.0, 3, 16)
+    assert rc == 0 and [c.astuple() for c in got] == list(want_c)
