@@ -146,9 +146,10 @@ def test_accumulator_matches_reference_kernel(hc_mod):
         assert O.fnv1a(np.ascontiguousarray(acc)) == gold[name]["fnv_ref_acc"], name
 
 
-def test_radii_across_the_table_limit(hc_mod):
-    """Radii 1452-1457: the tile kernel tabulates the midpoint circle up to
-    radius 1454 and walks it per point above that; both against the oracle."""
+def test_radii_wider_than_the_tiles(hc_mod):
+    """Radii 1452-1457 over a 2960 x 400 ROI: every circle crosses many
+    accumulator tiles and most of its votes fall outside the ROI; the
+    accumulator and the circles against the oracle."""
     HoughCircle, Image, _ = hc_mod
     rng = np.random.default_rng(5)
     img = np.zeros((400, 2960), np.uint8)
