@@ -44,7 +44,7 @@ def _run(cmd: list[str]) -> None:
 
 CU_SOURCES = ["hl_stage_a.cu", "hl_vote.cu", "hl_stage_c.cu", "hl_stage_f.cu",
               "hl_noalloc.cu", "hl_cnn.cu", "hl_synth.cu", "hl_window.cu", "hl_circle.cu"]
-CXX_SOURCES = ["hl_api.cpp", "HoughLine.cpp", "Image.cpp", "hl_proposal.cpp"]
+CXX_SOURCES = ["hl_api.cpp", "HoughLine.cpp", "HoughCircle.cpp", "Image.cpp", "hl_proposal.cpp"]
 C_SOURCES = ["synth.c"]
 
 

@@ -18,11 +18,11 @@ BUILD = ROOT / "opencuda_gb300" / "_build"
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
 
-def compile_main() -> Path:
-    exe = BUILD / "houghline_class_main"
+def compile_main(name: str = "houghline_class_main") -> Path:
+    exe = BUILD / name
     cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off",
            "-I", str(ROOT / "include"), "-I", os.path.join(CUDA, "include"),
-           str(ROOT / "tests" / "cpp" / "houghline_class_main.cpp"),
+           str(ROOT / "tests" / "cpp" / (name + ".cpp")),
            "-L", str(BUILD), "-lhoughline_gb300",
            f"-Wl,-rpath,{BUILD}", "-o", str(exe)]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -32,6 +32,7 @@ def compile_main() -> Path:
 
 def test_caller_compiles_and_links():
     assert compile_main().exists()
+    assert compile_main("houghcircle_class_main").exists()
 
 
 def _parse(out: str):
@@ -111,3 +112,53 @@ def test_cpp_class_matches_oracle(cuda):
     assert res["points"] == (0, n)
     assert res["points_lines"] == [tuple(w) for w in wp]
     assert ["null=-2"] in res["misc"]      # NULL_POINTER, okano_3_0/HoughLine.cu:640
+
+
+@pytest.mark.gpu
+def test_cpp_circle_class_matches_oracle(cuda, tmp_path):
+    """include/HoughCircle.h: houghcircle on an image, on its ROI and on a
+    point set, and pieceCircle, against the oracle."""
+    exe = compile_main("houghcircle_class_main")
+    W, H = 400, 300
+    img = cases.circle_scene(W, H, 8, 8, 45, 3000, 21)
+    raw = tmp_path / "scene.raw"
+    raw.write_bytes(img.tobytes())
+    r = subprocess.run([str(exe), str(raw), str(W), str(H)], capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    got, rcn, misc = {}, {}, {}
+    for line in r.stdout.splitlines():
+        p = line.split()
+        if len(p) == 6 and p[1] == "circle":
+            got.setdefault(p[0], []).append(tuple(int(v) for v in p[2:]))
+        elif len(p) == 3 and p[1].startswith("rc="):
+            rcn[p[0]] = (int(p[1][3:]), int(p[2][2:]))
+        else:
+            misc[p[0]] = p[1:]
+    args = (5, 50, 60, 30.0, 10)
+
+    def oracle(a, cm, ox=0, oy=0):
+        want, _ = O.houghcircle(a, args[0], args[1], args[2], args[3], args[4], cm)
+        return [(x + ox, y + oy, rr, v) for x, y, rr, v in want]
+
+    full = oracle(img, 32)
+    assert rcn["full"] == (0, len(full)) and got.get("full", []) == full and full
+    roi = oracle(img[30:H - 10, 40:W - 20], 32, 40, 30)
+    assert rcn["roi"] == (0, len(roi)) and got.get("roi", []) == roi
+    cx, cy, pieces = W // 2, H // 2, []
+    for y in range(2):
+        for x in range(2):
+            x1, y1 = x * cx, y * cy
+            pieces += oracle(img[y1:y1 + cy - 1, x1:x1 + cx - 1], 10, x1, y1)
+    pieces = pieces[:64]
+    assert rcn["piece"] == (0, len(pieces)) and got.get("piece", []) == pieces
+    assert misc["lastroi"] == [str(cx), str(cy), str(2 * cx - 1), str(2 * cy - 1)]
+    ys, xs = np.nonzero(img == 255)
+    pim = np.zeros((ys.max() + 2, xs.max() + 2), np.uint8)
+    pim[ys, xs] = 255
+    pts = oracle(pim, 32)
+    assert rcn["points"] == (0, len(pts)) and got.get("points", []) == pts
+    assert misc["null=-2"] == [] or "null=-2" in r.stdout
+    assert misc["defaults"] == ["5", "50", "50", "20", "100"]
+    assert misc["setmin=-1"] == ["keep=5"] and misc["setthr=-1"] == ["keep=100"]
+
