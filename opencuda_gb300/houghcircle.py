@@ -113,6 +113,27 @@ class HoughCircle:
             return rc, []
         return rc, [CircleParam(*out[i].as_tuple()) for i in range(max(cm.value, 0))]
 
+    def pieceCircle(self, inimg: Image, piecenum: int, circleMax: int, stream=None):
+        """okano_3_0/HoughCircle.cu:1323-1400: piecenum x piecenum pieces of
+        (width // piecenum) x (height // piecenum), ROI [x*c, x*c + c - 1),
+        up to 10 circles each in image coordinates, concatenated in row-major
+        piece order up to circleMax; the last piece's ROI stays on inimg."""
+        if inimg is None:
+            return _lib.NULL_POINTER, []
+        if piecenum <= 0:
+            return _lib.INVALID_DATA, []
+        cx, cy = inimg.width // piecenum, inimg.height // piecenum
+        out = []
+        for y in range(piecenum):
+            for x in range(piecenum):
+                inimg.roiX1, inimg.roiX2 = x * cx, x * cx + cx - 1
+                inimg.roiY1, inimg.roiY2 = y * cy, y * cy + cy - 1
+                rc, got = self.houghcircle(inimg, None, 10, stream)
+                if rc != _lib.NO_ERROR:
+                    return rc, []
+                out += got[:max(circleMax - len(out), 0)]
+        return _lib.NO_ERROR, out
+
     def accumulator(self, inimg: Image, stream=None):
         """The vote accumulator [radius][row][col] of the ROI (CUDA tensor)."""
         import torch

@@ -162,3 +162,23 @@ def test_radii_wider_than_the_tiles(hc_mod):
     rc, got = HoughCircle(1452, 1457, 20.0, 3, 3).houghcircle(Image.from_host(img), None, 16)
     want_c, _ = O.houghcircle(img, 1452, 1457, 3, 20.0, 3, 16)
     assert rc == 0 and [c.astuple() for c in got] == list(want_c)
+
+
+def test_piece_circle(hc_mod):
+    """pieceCircle of the Python mirror: 3 x 3 pieces against the oracle on
+    each piece's ROI, concatenated in row-major order."""
+    HoughCircle, Image, _ = hc_mod
+    img = ring_image(330, 240, [(50, 40, 20), (170, 120, 30), (280, 200, 25), (90, 190, 15)],
+                     0.01, seed=3)
+    im = Image.from_host(img)
+    rc, got = HoughCircle(5, 30, 20.0, 5, 20).pieceCircle(im, 3, 12)
+    assert rc == 0
+    want = []
+    for y in range(3):
+        for x in range(3):
+            x1, y1 = x * 110, y * 80
+            w, _ = O.houghcircle(img[y1:y1 + 79, x1:x1 + 109], 5, 30, 20, 20.0, 5, 10)
+            want += [(a + x1, b + y1, r, v) for a, b, r, v in w]
+    assert [c.astuple() for c in got] == want[:12]
+    assert (im.roiX1, im.roiY1, im.roiX2, im.roiY2) == (220, 160, 329, 239)
+
