@@ -718,53 +718,106 @@ hl_vote_kernel(hl_vote_args a)
 }
 
 /* The blocks voted in parts: block region = sum of its parts' scratch
- * slots, row 0 of the padding columns (thetas >= T) stored as zero.  One
- * CTA per 256 int4 of a region (grid.y = region); every slot is read once,
- * from L2 where the vote launch just wrote it. */
+ * slots, row 0 of the padding columns (thetas >= T) stored as zero.  A
+ * thread takes 16 bytes of every part of its region (grid.y = region): two
+ * output int4 when the parts hold 16-bit counts, one otherwise; every slot
+ * is read once, from L2 where the vote launch just wrote it. */
 __global__ void __launch_bounds__(256)
 hl_merge_kernel(hl_merge_args a)
 {
     hl_pdl_begin();
     const hl_merge_region r = a.regs[blockIdx.y];
-    const int i = blockIdx.x * 256 + threadIdx.x;
-    if (i >= r.rows * (HL_SLICE / 4))
-        return;
-    int4 v = make_int4(0, 0, 0, 0);
+    const int n4 = r.rows * (HL_SLICE / 4);   /* output int4 of the region */
+    int4 v0 = make_int4(0, 0, 0, 0), v1 = make_int4(0, 0, 0, 0);
+    int o;   /* first output int4 of this thread */
     if (a.part16) {
-        const int2 *src = reinterpret_cast<const int2 *>(a.scratch + (size_t)r.slot0 * a.slot4) + i;
-        for (int p = 0; p < r.nparts; p++) {
-            const int2 o = __ldcg(src + (size_t)p * 2 * a.slot4);
-            v.x += o.x & 0xffff;
-            v.y += (unsigned)o.x >> 16;
-            v.z += o.y & 0xffff;
-            v.w += (unsigned)o.y >> 16;
+        /* one 16-byte load per part: eight 16-bit counts, output int4 o and
+         * o + 1 (a row holds 8, so both lie in one row); up to four parts'
+         * loads in flight at once */
+        const int j = blockIdx.x * 256 + threadIdx.x;
+        o = 2 * j;
+        if (o >= n4)
+            return;
+        const int4 *src = a.scratch + (size_t)r.slot0 * a.slot4 + j;
+        int p = 0;
+        for (; p + 4 <= r.nparts; p += 4) {
+            int4 q[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                q[u] = __ldcg(src + (size_t)(p + u) * a.slot4);
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                v0.x += q[u].x & 0xffff;
+                v0.y += (unsigned)q[u].x >> 16;
+                v0.z += q[u].y & 0xffff;
+                v0.w += (unsigned)q[u].y >> 16;
+                v1.x += q[u].z & 0xffff;
+                v1.y += (unsigned)q[u].z >> 16;
+                v1.z += q[u].w & 0xffff;
+                v1.w += (unsigned)q[u].w >> 16;
+            }
+        }
+        for (; p < r.nparts; p++) {
+            const int4 q = __ldcg(src + (size_t)p * a.slot4);
+            v0.x += q.x & 0xffff;
+            v0.y += (unsigned)q.x >> 16;
+            v0.z += q.y & 0xffff;
+            v0.w += (unsigned)q.y >> 16;
+            v1.x += q.z & 0xffff;
+            v1.y += (unsigned)q.z >> 16;
+            v1.z += q.w & 0xffff;
+            v1.w += (unsigned)q.w >> 16;
         }
     } else {
-        const int4 *src = a.scratch + (size_t)r.slot0 * a.slot4 + i;
-        for (int p = 0; p < r.nparts; p++) {
-            const int4 o = __ldcg(src + (size_t)p * a.slot4);
-            v.x += o.x;
-            v.y += o.y;
-            v.z += o.z;
-            v.w += o.w;
+        o = blockIdx.x * 256 + threadIdx.x;
+        if (o >= n4)
+            return;
+        const int4 *src = a.scratch + (size_t)r.slot0 * a.slot4 + o;
+        int p = 0;
+        for (; p + 4 <= r.nparts; p += 4) {
+            int4 q[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                q[u] = __ldcg(src + (size_t)(p + u) * a.slot4);
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                v0.x += q[u].x;
+                v0.y += q[u].y;
+                v0.z += q[u].z;
+                v0.w += q[u].w;
+            }
+        }
+        for (; p < r.nparts; p++) {
+            const int4 q = __ldcg(src + (size_t)p * a.slot4);
+            v0.x += q.x;
+            v0.y += q.y;
+            v0.z += q.z;
+            v0.w += q.w;
         }
     }
-    const int rr = i >> 3, q = i & 7;
-    if (rr == 0) {
-        const int kq = r.k0 + 4 * q;
-        if (kq >= a.T) v.x = 0;
-        if (kq + 1 >= a.T) v.y = 0;
-        if (kq + 2 >= a.T) v.z = 0;
-        if (kq + 3 >= a.T) v.w = 0;
+    const int nout = a.part16 ? 2 : 1;
+    for (int e = 0; e < nout; e++) {
+        int4 v = e ? v1 : v0;
+        const int oi = o + e;
+        const int rr = oi >> 3, q = oi & 7;
+        if (rr == 0) {
+            const int kq = r.k0 + 4 * q;
+            if (kq >= a.T) v.x = 0;
+            if (kq + 1 >= a.T) v.y = 0;
+            if (kq + 2 >= a.T) v.z = 0;
+            if (kq + 3 >= a.T) v.w = 0;
+        }
+        a.acc[r.off4 + (size_t)rr * a.pitch4 + q] = v;
     }
-    a.acc[r.off4 + (size_t)rr * a.pitch4 + q] = v;
 }
 
 cudaError_t hl_launch_merge(const hl_merge_args *a, int max_rows, cudaStream_t s)
 {
     if (a->nreg <= 0)
         return cudaSuccess;
-    const unsigned gx = (unsigned)((max_rows * (HL_SLICE / 4) + 255) / 256);
+    const int per_thread = a->part16 ? 2 : 1;   /* output int4 per thread */
+    const unsigned gx =
+        (unsigned)((max_rows * (HL_SLICE / 4) / per_thread + 255) / 256);
     return hl_launch_pdl(hl_merge_kernel, dim3(gx, (unsigned)a->nreg), dim3(256), 0, s, false,
                          *a);
 }
