@@ -87,12 +87,10 @@ __device__ __forceinline__ void ct_walk(int x0, int y0, int r, int xw, int yh, u
         ct_red(rd + 4u * (unsigned)xc, fxc && fyd);
         ct_red(rc + 4u * (unsigned)xd, fxd && fyc);
         ct_red(rd + 4u * (unsigned)xd, fxd && fyd);
-        if (d < y)
-            d += 4 * x + 6;
-        else {
-            d += 4 * (x - y) + 10;
-            y--;
-        }
+        /* d < y: d += 4x + 6; else d += 4(x - y) + 10, y - 1 (as selects) */
+        const bool up = d < y;
+        d += up ? 4 * x + 6 : 4 * (x - y) + 10;
+        y -= up ? 0 : 1;
         x++;
     }
 }

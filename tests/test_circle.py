@@ -182,3 +182,46 @@ def test_piece_circle(hc_mod):
     assert [c.astuple() for c in got] == want[:12]
     assert (im.roiX1, im.roiY1, im.roiX2, im.roiY2) == (220, 160, 329, 239)
 
+
+
+def test_random_configurations(hc_mod):
+    """Seeded sweep: image sizes 1-400, ROIs covering at least the middle
+    third, radius ranges from 0 to 70 (some wider than the ROI), thresholds
+    at 20-90% of the ROI's largest count, noise and rings; accumulator and
+    circles against the oracle."""
+    HoughCircle, Image, _ = hc_mod
+    rng = np.random.default_rng(2024)
+    found = 0
+    for trial in range(24):
+        w, h = int(rng.integers(1, 401)), int(rng.integers(1, 301))
+        rings = [(int(rng.integers(0, w)), int(rng.integers(0, h)), int(rng.integers(2, 60)))
+                 for _ in range(int(rng.integers(1, 6)))]
+        img = ring_image(w, h, rings, float(rng.choice([0.0, 0.01, 0.03])),
+                         seed=int(rng.integers(1 << 30)))
+        x1, y1 = int(rng.integers(0, w // 3 + 1)), int(rng.integers(0, h // 3 + 1))
+        x2 = int(rng.integers(max(x1 + 1, 2 * w // 3), w + 1))
+        y2 = int(rng.integers(max(y1 + 1, 2 * h // 3), h + 1))
+        rmin = int(rng.integers(0, 30))
+        rmax = rmin + int(rng.integers(0, 41))
+        dist, rth, cm = float(rng.uniform(1, 60)), int(rng.integers(1, 20)), int(rng.integers(0, 20))
+        frac = float(rng.uniform(0.2, 0.9))
+        im = Image.from_host(img, (x1, y1, x2, y2))
+        roi = img[y1:y2, x1:x2]
+        want_acc = O.circle_vote(roi, rmin, rmax)
+        acc = HoughCircle(rmin, rmax).accumulator(im).cpu().numpy()
+        assert np.array_equal(acc, want_acc), (trial, w, h, rmin, rmax)
+        thr = int(frac * int(want_acc.max()))
+        rc, got = HoughCircle(rmin, rmax, dist, rth, thr).houghcircle(im, None, cm)
+        want, n = O.houghcircle(roi, rmin, rmax, thr, dist, rth, cm)
+        if n > 4096:
+            assert rc == _lib_overflow(), trial
+            continue
+        assert rc == 0, (trial, rc)
+        assert [c.astuple() for c in got] == [(a + x1, b + y1, r, v) for a, b, r, v in want], trial
+        found += len(want)
+    assert found > 24
+
+
+def _lib_overflow():
+    from opencuda_gb300 import _lib
+    return _lib.OP_OVERFLOW
