@@ -47,8 +47,19 @@ typedef struct hl_circle_params {
 int hl_circles(hl_handle *h, const hl_image_desc *img, const hl_circle_params *p,
                int *circlemax, hl_circle *out, void *stream);
 
+/* Circles of nimg ROIs (of one image or of several) in one pipeline: one
+ * compaction, one tile launch and one tail launch for all of them, one copy of
+ * the results.  counts[i] receives the circles of ROI i, written to
+ * out[i * circlemax ..] (circlemax <= 4096); each ROI as hl_circles.  Returns
+ * the first failing ROI's error (HL_OP_OVERFLOW: more than 4096 local maxima;
+ * its count is 0); synchronises.  pieceCircle's pieces are one such call. */
+int hl_circles_batch(hl_handle *h, const hl_image_desc *imgs, int nimg,
+                     const hl_circle_params *p, int circlemax, hl_circle *out, int *counts,
+                     void *stream);
+
 /* The vote accumulator alone, for parity checks: acc_dev is a DEVICE array
- * of (radius_max - radius_min + 1) x roi_h x roi_w int32, [radius][row][col]. */
+ * of (radius_max - radius_min + 1) x roi_h x roi_w int32, [radius][row][col].
+ * Synchronises (HL_CUDA_ERROR when a device-side wait gave up). */
 int hl_circle_accumulator(hl_handle *h, const hl_image_desc *img,
                           const hl_circle_params *p, int32_t *acc_dev, void *stream);
 

@@ -114,6 +114,7 @@ SIGNATURES = {
     "hl_set_batch_graph": (I, [H, I]),
     "hl_tiles": (I, [H, C.POINTER(hl_image_desc), I, I, P, PI, P]),
     "hl_circles": (I, [H, C.POINTER(hl_image_desc), C.POINTER(hl_circle_params), PI, P, P]),
+    "hl_circles_batch": (I, [H, P, I, C.POINTER(hl_circle_params), I, P, PI, P]),
     "hl_circle_accumulator": (I, [H, C.POINTER(hl_image_desc), C.POINTER(hl_circle_params),
                                   P, P]),
     "hl_autotune": (I, [H, C.POINTER(hl_image_desc), I, PI, I, C.POINTER(hl_tune_entry),

@@ -133,27 +133,42 @@ int HoughCircle::pieceCircle(Image *inimg, int piecenum, int *circleMax,
     (void)writetofile;
     if (!inimg || !circleMax)
         return NULL_POINTER;
-    if (piecenum <= 0)
+    if (piecenum <= 0 || piecenum > 4096)
         return INVALID_DATA;
-    int pointer = 0;
+    int rc = ensure();
+    if (rc != NO_ERROR)
+        return rc;
+    rc = ImageBasicOp::copyToCurrentDevice(inimg);
+    if (rc != NO_ERROR)
+        return rc;
+    /* the pieces of :1340-1352 (ROI [x * c, x * c + c - 1), 10 circles
+     * each), all in one hl_circles_batch call */
     const int cx = (int)inimg->width / piecenum, cy = (int)inimg->height / piecenum;
+    const int np = piecenum * piecenum;
+    std::vector<hl_image_desc> d((size_t)np);
     for (int y = 0; y < piecenum; y++)
         for (int x = 0; x < piecenum; x++) {
-            CircleParam piece[10];                          /* :1345-1352 */
-            int pm = 10;
             inimg->roiX1 = x * cx;
             inimg->roiX2 = x * cx + cx - 1;
             inimg->roiY1 = y * cy;
             inimg->roiY2 = y * cy + cy - 1;
-            const int rc = houghcircle(inimg, NULL, &pm, piece, false);
-            if (rc != NO_ERROR)
-                return rc;
-            for (int i = 0; i < pm; i++) {
-                if (pointer >= *circleMax)
-                    break;
-                circleparam[pointer++] = piece[i];
-            }
+            desc_of(inimg, &d[(size_t)y * piecenum + x]);
         }
+    hl_circle_params p;
+    p.radius_min = radiusMin;
+    p.radius_max = radiusMax;
+    p.dist_thres = distThres;
+    p.r_thres = (int)rThres;
+    p.threshold = cirThreshold;
+    std::vector<hl_circle> res((size_t)np * 10);
+    std::vector<int> cnt((size_t)np);
+    rc = hl_circles_batch(gpu_, d.data(), np, &p, 10, res.data(), cnt.data(), NULL);
+    if (rc != NO_ERROR)
+        return rc;
+    int pointer = 0;
+    for (int i = 0; i < np; i++)
+        for (int k = 0; k < cnt[i] && pointer < *circleMax; k++)
+            circleparam[pointer++] = *reinterpret_cast<const CircleParam *>(&res[(size_t)i * 10 + k]);
     *circleMax = pointer;
     return NO_ERROR;
 }

@@ -72,7 +72,9 @@ struct hl_handle {
     size_t cap_merge;
     int4 *d_scratch;
     size_t cap_scratch;
-    /* HoughCircle: candidate keys, [ncand, status] counters, results */
+    /* HoughCircle: candidate keys, [ncand, status] counters, results; the
+     * workspace of circle batches */
+    struct hl_cb_ws *cb;
     unsigned long long *d_ckeys;
     int *d_ccnt;
     unsigned char *d_cres;
@@ -236,12 +238,14 @@ extern "C" int hl_create(hl_handle **out, const hl_params *params)
 }
 
 static void batch_free(hl_handle *h);
+static void circle_batch_free(hl_handle *h);
 
 extern "C" int hl_destroy(hl_handle *h)
 {
     if (!h)
         return HL_NULL_POINTER;
     batch_free(h);
+    circle_batch_free(h);
     void *ptrs[] = {h->d_cos, h->d_sin, h->d_pts, h->d_tile_state,
                     h->d_tile_off, h->d_acc, h->d_keys, h->d_aux,
                     h->d_result, h->d_counters, h->order_dev,
@@ -2452,7 +2456,17 @@ extern "C" int hl_circle_accumulator(hl_handle *h, const hl_image_desc *img,
     int rc = circle_prepare(h, img, p, &roi, &g);
     if (rc != HL_NO_ERROR)
         return rc;
-    return circle_run(h, roi, g, p, acc_dev, false, s);
+    if ((rc = circle_run(h, roi, g, p, acc_dev, false, s)) != HL_NO_ERROR)
+        return rc;
+    /* the compaction's status word (a bounded wait that gave up) */
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, h->d_counters + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (st != 0) {
+        reset_counters(h, s);
+        return HL_CUDA_ERROR;
+    }
+    return HL_NO_ERROR;
 }
 
 extern "C" int hl_circles(hl_handle *h, const hl_image_desc *img, const hl_circle_params *p,
@@ -2490,6 +2504,7 @@ extern "C" int hl_circles(hl_handle *h, const hl_image_desc *img, const hl_circl
     if ((rc = circle_run(h, roi, g, p, nullptr, true, s)) != HL_NO_ERROR)
         return rc;
     hl_circle_final_args fa;
+    fa.imgs = nullptr;
     fa.keys = h->d_ckeys;
     fa.ncand = h->d_ccnt;
     fa.w = roi.w;
@@ -2503,7 +2518,7 @@ extern "C" int hl_circles(hl_handle *h, const hl_image_desc *img, const hl_circl
     fa.out = reinterpret_cast<hl_circle *>(h->d_cres + sizeof(hl_result_hdr));
     fa.hdr = reinterpret_cast<hl_result_hdr *>(h->d_cres);
     fa.status = h->d_ccnt + 1;
-    CK(hl_launch_circle_final(&fa, s));
+    CK(hl_launch_circle_final(&fa, 1, s));
     /* the results and the compaction's status word */
     int *cstat = reinterpret_cast<int *>(h->h_cres + kResCap);
     CK(cudaMemcpyAsync(h->h_cres, h->d_cres, rbytes, cudaMemcpyDeviceToHost, s));
@@ -2521,3 +2536,213 @@ extern "C" int hl_circles(hl_handle *h, const hl_image_desc *img, const hl_circl
     *circlemax = hdr->count;
     return HL_NO_ERROR;
 }
+
+/* ---- HoughCircle batches -------------------------------------------------- */
+
+struct hl_cb_ws {
+    float2 *d_pts;
+    size_t cap_pts;
+    int *d_toff;
+    size_t cap_toff;
+    unsigned long long *d_state;
+    size_t cap_state;
+    unsigned char *d_tab;
+    size_t cap_tab;
+    unsigned char *h_tab;
+    size_t cap_htab;
+    unsigned long long *d_keys;
+    size_t cap_keys;
+    int *d_cnt;
+    size_t cap_cnt;
+    unsigned char *d_res;
+    size_t cap_res;
+    unsigned char *h_res;
+    size_t cap_hres;
+};
+
+static void circle_batch_free(hl_handle *h)
+{
+    hl_cb_ws *c = h->cb;
+    if (!c)
+        return;
+    void *dp[] = {c->d_pts, c->d_toff, c->d_state, c->d_tab, c->d_keys, c->d_cnt, c->d_res};
+    for (void *q : dp)
+        if (q)
+            cudaFree(q);
+    if (c->h_tab)
+        cudaFreeHost(c->h_tab);
+    if (c->h_res)
+        cudaFreeHost(c->h_res);
+    delete c;
+    h->cb = nullptr;
+}
+
+/* Circles of many ROIs (of one image or several) in one pipeline: one
+ * compaction over every ROI (the batch form of the compaction kernel, each
+ * ROI its own point region and tile offsets), one tile launch over every
+ * ROI's (tile, radius) CTAs, one tail CTA per ROI, one copy of the results. */
+extern "C" int hl_circles_batch(hl_handle *h, const hl_image_desc *imgs, int nimg,
+                                const hl_circle_params *p, int circlemax, hl_circle *out,
+                                int *counts, void *stream)
+{
+    if (!h || !p || !counts || (nimg > 0 && !imgs) || (nimg > 0 && circlemax > 0 && !out))
+        return HL_NULL_POINTER;
+    if (nimg < 0 || circlemax < 0 || circlemax > HL_CIRCLE_MAXCAND)
+        return HL_INVALID_DATA;
+    if (p->radius_min < 0 || p->radius_max < p->radius_min || p->radius_max >= 65536 ||
+        p->threshold < 0 || !(p->dist_thres == p->dist_thres))
+        return HL_INVALID_DATA;
+    if (nimg == 0)
+        return HL_NO_ERROR;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const int nr = p->radius_max - p->radius_min + 1;
+    std::vector<hl_roi> rois((size_t)nimg);
+    std::vector<hl_geom> gs((size_t)nimg);
+    std::vector<long long> pts_base((size_t)nimg);
+    std::vector<int> tile_base((size_t)nimg), group_base((size_t)nimg), cta_base((size_t)nimg);
+    std::vector<int> group_img;
+    long long pts = 0, ctas = 0, tiles = 0, groups = 0;
+    for (int i = 0; i < nimg; i++) {
+        int rc = roi_of(&imgs[i], &rois[i]);
+        if (rc != HL_NO_ERROR)
+            return rc;
+        if ((rc = hl_geometry(h, rois[i].w, rois[i].h, &gs[i])) != HL_NO_ERROR)
+            return rc;
+        if ((size_t)nr * rois[i].w * rois[i].h >= (size_t)0xffffffffu)
+            return HL_OP_OVERFLOW;   /* the candidate key holds a 32-bit index */
+        const int nt = gs[i].tiles_x * gs[i].tiles_y;
+        const int ng = (nt + HL_COMPACT_GROUP - 1) / HL_COMPACT_GROUP;
+        tile_base[i] = (int)tiles;
+        group_base[i] = (int)groups;
+        for (int q = 0; q < ng; q++)
+            group_img.push_back(i);
+        tiles += nt + 1;   /* the ROI's tile offsets and its end */
+        groups += ng;
+        /* every pixel and one pad per tile, even so each region starts on
+         * 16 bytes */
+        pts_base[i] = pts;
+        pts += ((long long)rois[i].w * rois[i].h + nt + 16 + 1) & ~1LL;
+        const long long ntx = (rois[i].w + HL_CIRCLE_TW - 1) / HL_CIRCLE_TW;
+        const long long nty = (rois[i].h + HL_CIRCLE_TH - 1) / HL_CIRCLE_TH;
+        cta_base[i] = (int)std::min(ctas, (long long)0x7fffffff);
+        ctas += ntx * nty * nr;
+        if (ctas > 0x7fffffffLL || tiles > 0x7fffffffLL || groups > 0x7fffffffLL)
+            return HL_OP_OVERFLOW;
+    }
+    if (!h->cb && !(h->cb = new (std::nothrow) hl_cb_ws()))
+        return HL_OUT_OF_MEM;
+    hl_cb_ws *c = h->cb;
+    const size_t rstride =
+        align16(sizeof(hl_result_hdr) + sizeof(hl_circle) * (size_t)std::max(circlemax, 1));
+    const size_t off_cimg = 0;
+    const size_t off_gimg = align16(sizeof(hl_compact_img) * (size_t)nimg);
+    const size_t off_circ = align16(off_gimg + sizeof(int) * (size_t)groups);
+    const size_t tab_bytes = align16(off_circ + sizeof(hl_circle_img) * (size_t)nimg);
+    const size_t ncnt = 4 + 2 * (size_t)nimg;   /* ticket, count, status, pad, per ROI */
+    int rc;
+    if ((rc = grow((void **)&c->d_pts, &c->cap_pts, sizeof(float2) * (size_t)pts)) != HL_NO_ERROR ||
+        (rc = grow((void **)&c->d_toff, &c->cap_toff, sizeof(int) * (size_t)tiles)) != HL_NO_ERROR ||
+        (rc = grow((void **)&c->d_state, &c->cap_state,
+                   sizeof(unsigned long long) * (size_t)(groups + 1))) != HL_NO_ERROR ||
+        (rc = grow((void **)&c->d_tab, &c->cap_tab, tab_bytes)) != HL_NO_ERROR ||
+        (rc = grow_host(&c->h_tab, &c->cap_htab, tab_bytes)) != HL_NO_ERROR ||
+        (rc = grow((void **)&c->d_keys, &c->cap_keys,
+                   sizeof(unsigned long long) * HL_CIRCLE_MAXCAND * (size_t)nimg)) != HL_NO_ERROR ||
+        (rc = grow((void **)&c->d_cnt, &c->cap_cnt, sizeof(int) * ncnt)) != HL_NO_ERROR ||
+        (rc = grow((void **)&c->d_res, &c->cap_res, rstride * (size_t)nimg)) != HL_NO_ERROR ||
+        (rc = grow_host(&c->h_res, &c->cap_hres, rstride * (size_t)nimg + 16)) != HL_NO_ERROR)
+        return rc;
+    hl_compact_img *ci = reinterpret_cast<hl_compact_img *>(c->h_tab + off_cimg);
+    hl_circle_img *im = reinterpret_cast<hl_circle_img *>(c->h_tab + off_circ);
+    for (int i = 0; i < nimg; i++) {
+        const hl_geom &g = gs[i];
+        const int nt = g.tiles_x * g.tiles_y;
+        ci[i].roi = rois[i];
+        ci[i].tiles_x = g.tiles_x;
+        ci[i].ntiles = nt;
+        ci[i].tile_base = tile_base[i];
+        ci[i].group_base = group_base[i];
+        ci[i].ngroups = (nt + HL_COMPACT_GROUP - 1) / HL_COMPACT_GROUP;
+        ci[i].pad = 0;
+        ci[i].pts_base = pts_base[i];
+        im[i].pts = c->d_pts + pts_base[i];
+        im[i].tile_off = c->d_toff + tile_base[i];
+        im[i].ctiles_x = g.tiles_x;
+        im[i].ctiles_y = g.tiles_y;
+        im[i].w = rois[i].w;
+        im[i].h = rois[i].h;
+        im[i].ntx = (rois[i].w + HL_CIRCLE_TW - 1) / HL_CIRCLE_TW;
+        im[i].nty = (rois[i].h + HL_CIRCLE_TH - 1) / HL_CIRCLE_TH;
+        im[i].roi_x = imgs[i].roi_x1;
+        im[i].roi_y = imgs[i].roi_y1;
+        im[i].cta_base = cta_base[i];
+        im[i].pad = 0;
+        im[i].keys = c->d_keys + (size_t)HL_CIRCLE_MAXCAND * i;
+        im[i].ncand = c->d_cnt + 4 + 2 * i;
+        im[i].hdr = reinterpret_cast<hl_result_hdr *>(c->d_res + rstride * i);
+        im[i].out = reinterpret_cast<hl_circle *>(c->d_res + rstride * i + sizeof(hl_result_hdr));
+    }
+    memcpy(c->h_tab + off_gimg, group_img.data(), sizeof(int) * group_img.size());
+    unsigned char *dt = c->d_tab;
+    CK(cudaMemsetAsync(c->d_cnt, 0, sizeof(int) * ncnt, s));
+    CK(cudaMemsetAsync(c->d_state, 0, sizeof(unsigned long long) * (size_t)(groups + 1), s));
+    CK(cudaMemcpyAsync(dt, c->h_tab, tab_bytes, cudaMemcpyHostToDevice, s));
+    hl_compact_args ca;
+    memset(&ca, 0, sizeof(ca));
+    ca.imgs = reinterpret_cast<const hl_compact_img *>(dt + off_cimg);
+    ca.group_img = reinterpret_cast<const int *>(dt + off_gimg);
+    ca.nimg = nimg;
+    ca.ngroups = (int)groups;
+    ca.tile_state = c->d_state;
+    ca.ticket = reinterpret_cast<unsigned *>(c->d_cnt + 0);
+    ca.ticket_base = 0;
+    ca.epoch = 1;
+    ca.pts = nullptr;
+    ca.pts_f2 = c->d_pts;
+    ca.tile_off = c->d_toff;
+    ca.count = c->d_cnt + 1;
+    ca.status = c->d_cnt + 2;
+    CK(hl_launch_compact(&ca, s));
+    hl_circle_tile_args ta;
+    memset(&ta, 0, sizeof(ta));
+    ta.imgs = reinterpret_cast<const hl_circle_img *>(dt + off_circ);
+    ta.nimg = nimg;
+    ta.nctas = (int)ctas;
+    ta.rmin = p->radius_min;
+    ta.nr = nr;
+    ta.acc = nullptr;
+    ta.threshold = p->threshold;
+    ta.cap = HL_CIRCLE_MAXCAND;
+    CK(hl_launch_circle_tiles(&ta, s));
+    hl_circle_final_args fa;
+    memset(&fa, 0, sizeof(fa));
+    fa.imgs = reinterpret_cast<const hl_circle_img *>(dt + off_circ);
+    fa.rmin = p->radius_min;
+    fa.dist_thres = p->dist_thres;
+    fa.r_thres = p->r_thres;
+    fa.circlemax = circlemax;
+    CK(hl_launch_circle_final(&fa, nimg, s));
+    int *cstat = reinterpret_cast<int *>(c->h_res + rstride * (size_t)nimg);
+    CK(cudaMemcpyAsync(c->h_res, c->d_res, rstride * (size_t)nimg, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(cstat, c->d_cnt + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (*cstat != 0)
+        return HL_CUDA_ERROR;
+    rc = HL_NO_ERROR;
+    for (int i = 0; i < nimg; i++) {
+        const hl_result_hdr *hdr =
+            reinterpret_cast<const hl_result_hdr *>(c->h_res + rstride * (size_t)i);
+        if (hdr->status != 0) {
+            counts[i] = 0;
+            if (rc == HL_NO_ERROR)
+                rc = (hdr->status & HL_ST_CAND_OVERFLOW) ? HL_OP_OVERFLOW : HL_CUDA_ERROR;
+            continue;
+        }
+        counts[i] = hdr->count;
+        if (hdr->count > 0)
+            memcpy(out + (size_t)circlemax * i, c->h_res + rstride * (size_t)i + sizeof(hl_result_hdr),
+                   sizeof(hl_circle) * (size_t)hdr->count);
+    }
+    return rc;
+}
+

@@ -21,6 +21,8 @@
  *       neighbours; the keys (votes << 32 | ~index) are appended with one
  *       atomic per warp.  The accumulator never goes to HBM on the circle
  *       path.
+ *   Both kernels also take a batch (a table of images): the tile launch covers
+ *       every image's (tile, radius) CTAs, the tail runs one CTA per image.
  *   hl_circle_final_kernel -- one CTA: rank sort (votes descending, index
  *       ascending: the deviation from the reference's shear sort is only the
  *       order of equal votes), decode (:632-657), the greedy merge of
@@ -100,25 +102,51 @@ __device__ __forceinline__ void ct_walk(int x0, int y0, int r, int xw, int yh, u
 #define CT_NOWHERE (-(1 << 20))
 
 __global__ void __launch_bounds__(CT_THREADS, 2)
-hl_circle_tile_kernel(hl_circle_tile_args a)
+hl_circle_tile_kernel(hl_circle_tile_args a0)
 {
     extern __shared__ __align__(16) unsigned char ct_raw[];
     CircleTileSmem &sm = *reinterpret_cast<CircleTileSmem *>(ct_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int ntile = a.ntx * a.nty;
-    const int z = a.nr - 1 - (int)(blockIdx.x / (unsigned)ntile);
-    const int tile = (int)(blockIdx.x % (unsigned)ntile);
-    const int r = a.rmin + z;
-    const int tx0 = (tile % a.ntx) * HL_CIRCLE_TW, ty0 = (tile / a.ntx) * HL_CIRCLE_TH;
-    /* counted cells, image coordinates: the tile and its apron within the ROI */
-    const int cx0 = max(tx0 - 1, 0), cy0 = max(ty0 - 1, 0);
-    const int cx1 = min(tx0 + HL_CIRCLE_TW + 1, a.w), cy1 = min(ty0 + HL_CIRCLE_TH + 1, a.h);
     {
         int4 *c4 = reinterpret_cast<int4 *>(sm.cnt);
         for (int i = tid; i < CT_CELLS / 4; i += CT_THREADS)
             c4[i] = make_int4(0, 0, 0, 0);
     }
     hl_pdl_begin();
+    hl_circle_tile_args a = a0;
+    unsigned bid = blockIdx.x;
+    if (a0.imgs) {
+        /* a batch: the image whose CTA range holds this CTA */
+        int lo = 0, hi = a0.nimg - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if ((unsigned)a0.imgs[mid].cta_base <= bid)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const hl_circle_img im = a0.imgs[lo];
+        a.pts = im.pts;
+        a.tile_off = im.tile_off;
+        a.ctiles_x = im.ctiles_x;
+        a.ctiles_y = im.ctiles_y;
+        a.w = im.w;
+        a.h = im.h;
+        a.ntx = im.ntx;
+        a.nty = im.nty;
+        a.keys = im.keys;
+        a.ncand = im.ncand;
+        a.status = im.ncand + 1;
+        bid -= (unsigned)im.cta_base;
+    }
+    const int ntile = a.ntx * a.nty;
+    const int z = a.nr - 1 - (int)(bid / (unsigned)ntile);
+    const int tile = (int)(bid % (unsigned)ntile);
+    const int r = a.rmin + z;
+    const int tx0 = (tile % a.ntx) * HL_CIRCLE_TW, ty0 = (tile / a.ntx) * HL_CIRCLE_TH;
+    /* counted cells, image coordinates: the tile and its apron within the ROI */
+    const int cx0 = max(tx0 - 1, 0), cy0 = max(ty0 - 1, 0);
+    const int cx1 = min(tx0 + HL_CIRCLE_TW + 1, a.w), cy1 = min(ty0 + HL_CIRCLE_TH + 1, a.h);
     __syncthreads();
     if (r > 0) {
         const int xlo = cx0 - tx0 + CT_OX, xw = cx1 - cx0;
@@ -297,11 +325,24 @@ __device__ __forceinline__ bool circle_close(int4 ci, int4 cj, float d2, int r_t
 }
 
 __global__ void __launch_bounds__(1024)
-hl_circle_final_kernel(hl_circle_final_args a)
+hl_circle_final_kernel(hl_circle_final_args a0)
 {
     extern __shared__ __align__(16) unsigned char c_raw[];
     CircleSmem &sm = *reinterpret_cast<CircleSmem *>(c_raw);
     hl_pdl_begin();
+    hl_circle_final_args a = a0;
+    if (a0.imgs) {
+        const hl_circle_img im = a0.imgs[blockIdx.x];
+        a.keys = im.keys;
+        a.ncand = im.ncand;
+        a.status = im.ncand + 1;
+        a.w = im.w;
+        a.h = im.h;
+        a.roi_x = im.roi_x;
+        a.roi_y = im.roi_y;
+        a.out = im.out;
+        a.hdr = im.hdr;
+    }
     const int tid = threadIdx.x;
     const int ncand = *a.ncand;
     /* past the key buffer the call fails (OP_OVERFLOW): nothing to rank */
@@ -401,19 +442,22 @@ cudaError_t hl_launch_circle_tiles(const hl_circle_tile_args *a, cudaStream_t s)
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return e;
-    const long long grid = (long long)a->ntx * a->nty * a->nr;
+    const long long grid = a->imgs ? (long long)a->nctas : (long long)a->ntx * a->nty * a->nr;
     if (grid <= 0 || grid > 0x7fffffffLL)
         return cudaErrorInvalidConfiguration;
     return hl_launch_pdl(hl_circle_tile_kernel, dim3((unsigned)grid), dim3(CT_THREADS), smem, s,
                          false, *a);
 }
 
-cudaError_t hl_launch_circle_final(const hl_circle_final_args *a, cudaStream_t s)
+cudaError_t hl_launch_circle_final(const hl_circle_final_args *a, int nimg, cudaStream_t s)
 {
     const size_t smem = sizeof(CircleSmem);
     cudaError_t e = cudaFuncSetAttribute(hl_circle_final_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return e;
-    return hl_launch_pdl(hl_circle_final_kernel, dim3(1), dim3(1024), smem, s, false, *a);
+    if (nimg < 1)
+        return cudaErrorInvalidValue;
+    return hl_launch_pdl(hl_circle_final_kernel, dim3((unsigned)nimg), dim3(1024), smem, s,
+                         false, *a);
 }

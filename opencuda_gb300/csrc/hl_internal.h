@@ -263,7 +263,29 @@ static inline cudaError_t hl_launch_pdl(void (*kernel)(Params...), dim3 grid, di
  * its local maxima appended to keys. */
 #define HL_CIRCLE_TW 192
 #define HL_CIRCLE_TH 128
+/* One image of a circle batch: its points and tile offsets (the batch
+ * compaction's region of the image), its ROI, its candidate keys and
+ * counters, its result records, and the first CTA of its tile launch. */
+typedef struct hl_circle_img {
+    const float2 *pts;
+    const int *tile_off;
+    int ctiles_x, ctiles_y;
+    int w, h;
+    int ntx, nty;
+    int roi_x, roi_y;
+    int cta_base;
+    int pad;
+    unsigned long long *keys; /* [HL_CIRCLE_MAXCAND] */
+    int *ncand;               /* [ncand, status] */
+    hl_circle *out;
+    hl_result_hdr *hdr;
+} hl_circle_img;
 typedef struct hl_circle_tile_args {
+    /* a batch: the CTA's image is the last with cta_base <= blockIdx.x, and
+     * its fields replace pts .. nty, keys, ncand and status below */
+    const hl_circle_img *imgs;
+    int nimg;
+    int nctas;                /* CTAs of a batch (every image's tiles x radii) */
     const float2 *pts;        /* the compaction's points (odd tiles padded) */
     const int *tile_off;      /* [ctiles_x * ctiles_y + 1] */
     int ctiles_x, ctiles_y;   /* compaction tiles (HL_TILE_W x HL_TILE_H) */
@@ -278,6 +300,8 @@ typedef struct hl_circle_tile_args {
     int *status;
 } hl_circle_tile_args;
 typedef struct hl_circle_final_args {
+    /* a batch: CTA i takes image i's keys, counters, ROI and outputs */
+    const hl_circle_img *imgs;
     const unsigned long long *keys;
     int *ncand;
     int w, h, rmin;
@@ -290,7 +314,8 @@ typedef struct hl_circle_final_args {
     int *status;
 } hl_circle_final_args;
 cudaError_t hl_launch_circle_tiles(const hl_circle_tile_args *a, cudaStream_t s);
-cudaError_t hl_launch_circle_final(const hl_circle_final_args *a, cudaStream_t s);
+/* grid: one CTA, or nimg CTAs for a batch */
+cudaError_t hl_launch_circle_final(const hl_circle_final_args *a, int nimg, cudaStream_t s);
 
 cudaError_t hl_launch_compact(const hl_compact_args *a, cudaStream_t s);
 /* one image (a->imgs == NULL) with hl_compact_persist_ctas(ntiles, sms) CTAs

@@ -113,26 +113,45 @@ class HoughCircle:
             return rc, []
         return rc, [CircleParam(*out[i].as_tuple()) for i in range(max(cm.value, 0))]
 
+    def houghcircleBatch(self, images, circleMax: int, stream=None):
+        """Circles of every image's ROI through one hl_circles_batch call:
+        (errcode, [circles of image 0, circles of image 1, ...])."""
+        n = len(images)
+        if n == 0:
+            return _lib.NO_ERROR, []
+        descs = (_lib.hl_image_desc * n)(*[im.desc() for im in images])
+        out = (_lib.hl_circle * max(n * circleMax, 1))()
+        counts = (C.c_int * n)()
+        p = self._params()
+        rc = self._L.hl_circles_batch(self._h, descs, n, C.byref(p), circleMax, out, counts,
+                                      _stream(stream))
+        res = [[CircleParam(*out[i * circleMax + k].as_tuple()) for k in range(counts[i])]
+               for i in range(n)]
+        return rc, res
+
     def pieceCircle(self, inimg: Image, piecenum: int, circleMax: int, stream=None):
         """okano_3_0/HoughCircle.cu:1323-1400: piecenum x piecenum pieces of
         (width // piecenum) x (height // piecenum), ROI [x*c, x*c + c - 1),
         up to 10 circles each in image coordinates, concatenated in row-major
-        piece order up to circleMax; the last piece's ROI stays on inimg."""
+        piece order up to circleMax; the last piece's ROI stays on inimg.  The
+        pieces run as one hl_circles_batch call."""
         if inimg is None:
             return _lib.NULL_POINTER, []
         if piecenum <= 0:
             return _lib.INVALID_DATA, []
         cx, cy = inimg.width // piecenum, inimg.height // piecenum
-        out = []
+        pieces = []
         for y in range(piecenum):
             for x in range(piecenum):
-                inimg.roiX1, inimg.roiX2 = x * cx, x * cx + cx - 1
-                inimg.roiY1, inimg.roiY2 = y * cy, y * cy + cy - 1
-                rc, got = self.houghcircle(inimg, None, 10, stream)
-                if rc != _lib.NO_ERROR:
-                    return rc, []
-                out += got[:max(circleMax - len(out), 0)]
-        return _lib.NO_ERROR, out
+                pieces.append(Image(inimg.data, (x * cx, y * cy, x * cx + cx - 1,
+                                                 y * cy + cy - 1)))
+        rc, per = self.houghcircleBatch(pieces, 10, stream)
+        inimg.roiX1, inimg.roiY1 = (piecenum - 1) * cx, (piecenum - 1) * cy
+        inimg.roiX2, inimg.roiY2 = piecenum * cx - 1, piecenum * cy - 1
+        if rc != _lib.NO_ERROR:
+            return rc, []
+        out = [c for p in per for c in p]
+        return _lib.NO_ERROR, out[:max(circleMax, 0)]
 
     def accumulator(self, inimg: Image, stream=None):
         """The vote accumulator [radius][row][col] of the ROI (CUDA tensor)."""

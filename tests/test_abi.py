@@ -69,6 +69,7 @@ def test_batch_entry_points_reject_null_without_gpu():
     assert lib.hl_tiles(None, None, 4, 16, None, None, None) == _lib.NULL_POINTER
     assert lib.hl_circles(None, None, None, None, None, None) == _lib.NULL_POINTER
     assert lib.hl_circle_accumulator(None, None, None, None, None) == _lib.NULL_POINTER
+    assert lib.hl_circles_batch(None, None, 0, None, 0, None, None, None) == _lib.NULL_POINTER
     assert lib.hl_set_batch_graph(None, 1) == _lib.NULL_POINTER
     assert lib.hl_autotune(None, None, 0, None, 0, None, None, 0, None, None) == \
         _lib.NULL_POINTER

@@ -225,3 +225,34 @@ def test_random_configurations(hc_mod):
 def _lib_overflow():
     from opencuda_gb300 import _lib
     return _lib.OP_OVERFLOW
+
+
+def test_batch_matches_each_roi(hc_mod):
+    """hl_circles_batch over ROIs of different images and sizes (one 1 x 1,
+    one without edge pixels) against the oracle on each ROI; then a batch in
+    which one ROI has more than 4096 candidates: OP_OVERFLOW, that ROI's
+    count 0, the others unchanged."""
+    HoughCircle, Image, _ = hc_mod
+    from opencuda_gb300 import _lib
+    a = ring_image(300, 200, [(80, 90, 35), (200, 100, 22), (150, 40, 9)], 0.01, seed=1)
+    b = ring_image(160, 120, [(50, 60, 20), (110, 40, 12)], 0.0)
+    c = ring_image(700, 330, [(100, 100, 40), (400, 200, 45), (600, 150, 30)], 0.005, seed=2)
+    rois = [(a, (17, 11, 283, 190)), (b, None), (c, (5, 7, 690, 325)), (a, (0, 0, 1, 1)),
+            (b, (0, 0, 20, 20)), (c, (300, 100, 520, 300))]
+    hc = HoughCircle(5, 50, 20.0, 5, 30)
+    imgs = [Image.from_host(x, r) for x, r in rois]
+    rc, per = hc.houghcircleBatch(imgs, 12)
+    assert rc == 0
+    for (x, r), got in zip(rois, per):
+        x1, y1, x2, y2 = r if r else (0, 0, x.shape[1], x.shape[0])
+        want, _ = O.houghcircle(x[y1:y2, x1:x2], 5, 50, 30, 20.0, 5, 12)
+        assert [q.astuple() for q in got] == [(p + x1, s + y1, rr, v) for p, s, rr, v in want]
+    assert sum(len(g) for g in per) > 5
+    noisy = ring_image(400, 400, [], noise=0.3, seed=7)
+    hc2 = HoughCircle(5, 8, 10.0, 5, 0)
+    rc, per = hc2.houghcircleBatch([Image.from_host(b), Image.from_host(noisy),
+                                    Image.from_host(b)], 8)
+    assert rc == _lib.OP_OVERFLOW
+    want, _ = O.houghcircle(b, 5, 8, 0, 10.0, 5, 8)
+    assert per[1] == [] and [q.astuple() for q in per[0]] == list(want)
+    assert [q.astuple() for q in per[2]] == list(want)
