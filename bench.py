@@ -411,6 +411,30 @@ def circle_workload(L, Image, dev, sp, atom_peak: float, reps: int, cpu: bool):
                         "frac": votes / (t / 1e3) / atom_peak,
                         "note": "whole call (all launches and the result copy) as the time"},
            "reps": reps, "l2": "flushed between calls"}
+    # pieceCircle: 4 x 4 pieces of the same scene as one hl_circles_batch call,
+    # against the pieces looped through hl_circles
+    pieces = []
+    for y in range(4):
+        for x in range(4):
+            pieces.append(Image(img.data, (x * 256, y * 256, x * 256 + 255, y * 256 + 255)))
+    for _ in range(3):
+        hc.houghcircleBatch(pieces, 10, stream=sp)
+    bt, lt = [], []
+    for _ in range(reps):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        rc, _ = hc.houghcircleBatch(pieces, 10, stream=sp)
+        bt.append((time.perf_counter() - t0) * 1e3)
+        t0 = time.perf_counter()
+        for pc in pieces:
+            hc.houghcircle(pc, None, 10, stream=sp)
+        lt.append((time.perf_counter() - t0) * 1e3)
+    if rc != 0:
+        raise RuntimeError(f"hl_circles_batch returned {rc}")
+    out["pieces"] = {"workload": "pieceCircle 4 x 4 of the same scene (256 x 256 pieces, "
+                                 "ROI [x*c, x*c + c - 1)), 10 circles per piece",
+                     "batch_ms": statistics.median(bt), "loop_ms": statistics.median(lt),
+                     "timing": "host wall time of synchronous calls, image resident"}
     if cpu:
         t0 = time.perf_counter()
         want, _ = O.houghcircle(host, 5, 50, 100, 50.0, 20, cm)
