@@ -51,6 +51,8 @@ struct CircleTileSmem {
     int start[CT_ROWS];       /* first point of each halo row */
     int red[CT_WARPS];
     unsigned char rank_lane[CT_WARPS][32];   /* lane of the k-th queued point */
+    int2 left[CT_WARPS * 32];                /* the warps' last, partial queues */
+    int nleft;
 };
 
 /* one vote at the shared-memory word addr when p holds: a predicated
@@ -112,6 +114,8 @@ hl_circle_tile_kernel(hl_circle_tile_args a0)
         for (int i = tid; i < CT_CELLS / 4; i += CT_THREADS)
             c4[i] = make_int4(0, 0, 0, 0);
     }
+    if (tid == 0)
+        sm.nleft = 0;
     hl_pdl_begin();
     hl_circle_tile_args a = a0;
     unsigned bid = blockIdx.x;
@@ -246,8 +250,17 @@ hl_circle_tile_kernel(hl_circle_tile_args a0)
             }
             __syncthreads();   /* before the next pass rewrites pre / start */
         }
-        if (qn > 0)
-            ct_walk(qx, qy, r, xw, yh, pbase);
+        /* the partial queues left in every warp are pooled and walked 32 at
+         * a time, not as up to 16 part-empty walks */
+        if (lane < qn)
+            sm.left[atomicAdd(&sm.nleft, 1)] = make_int2(qx, qy);
+        __syncthreads();
+        const int nl = sm.nleft;
+        for (int b0 = warp * 32; b0 < nl; b0 += CT_THREADS) {
+            const int k = b0 + lane;
+            const int2 q = k < nl ? sm.left[k] : make_int2(CT_NOWHERE, CT_NOWHERE);
+            ct_walk(q.x, q.y, r, xw, yh, pbase);
+        }
     }
     __syncthreads();
     /* the interior: written out and/or its local maxima taken (cells
@@ -324,31 +337,28 @@ __device__ __forceinline__ bool circle_close(int4 ci, int4 cj, float d2, int r_t
     return dist < d2 && abs(ci.z - cj.z) < r_thres;
 }
 
-__global__ void __launch_bounds__(1024)
+__global__ void __launch_bounds__(1024, 1)
 hl_circle_final_kernel(hl_circle_final_args a0)
 {
     extern __shared__ __align__(16) unsigned char c_raw[];
     CircleSmem &sm = *reinterpret_cast<CircleSmem *>(c_raw);
     hl_pdl_begin();
-    hl_circle_final_args a = a0;
-    if (a0.imgs) {
-        const hl_circle_img im = a0.imgs[blockIdx.x];
-        a.keys = im.keys;
-        a.ncand = im.ncand;
-        a.status = im.ncand + 1;
-        a.w = im.w;
-        a.h = im.h;
-        a.roi_x = im.roi_x;
-        a.roi_y = im.roi_y;
-        a.out = im.out;
-        a.hdr = im.hdr;
-    }
+    const hl_circle_final_args &a = a0;
+    /* a batch: this CTA's image */
+    const hl_circle_img *im = a.imgs ? a.imgs + blockIdx.x : nullptr;
+    const unsigned long long *keys = im ? im->keys : a.keys;
+    int *const ncandp = im ? im->ncand : a.ncand;
+    int *const statusp = im ? im->ncand + 1 : a.status;
+    const int W = im ? im->w : a.w, H = im ? im->h : a.h;
+    const int roi_x = im ? im->roi_x : a.roi_x, roi_y = im ? im->roi_y : a.roi_y;
+    hl_circle *const outp = im ? im->out : a.out;
+    hl_result_hdr *const hdrp = im ? im->hdr : a.hdr;
     const int tid = threadIdx.x;
-    const int ncand = *a.ncand;
+    const int ncand = *ncandp;
     /* past the key buffer the call fails (OP_OVERFLOW): nothing to rank */
     const int n = ncand > HL_CIRCLE_MAXCAND ? 0 : ncand;
     for (int i = tid; i < n; i += blockDim.x)
-        sm.keys[i] = a.keys[i];
+        sm.keys[i] = keys[i];
     __syncthreads();
     /* rank sort, descending (keys are unique: the index is part of them) */
     for (int i = tid; i < n; i += blockDim.x) {
@@ -359,12 +369,12 @@ hl_circle_final_kernel(hl_circle_final_args a0)
         sm.sorted[rank] = ki;
     }
     __syncthreads();
-    const long long plane = (long long)a.w * a.h;
+    const long long plane = (long long)W * H;
     for (int i = tid; i < n; i += blockDim.x) {
         const unsigned long long k = sm.sorted[i];
         const long long idx = (long long)(unsigned)(~(unsigned)(k & 0xffffffffu));
         const long long z = idx / plane, t = idx - z * plane;
-        sm.cir[i] = make_int4((int)(t % a.w), (int)(t / a.w), (int)z + a.rmin, (int)(k >> 32));
+        sm.cir[i] = make_int4((int)(t % W), (int)(t / W), (int)z + a.rmin, (int)(k >> 32));
     }
     __syncthreads();
     if (tid < 32) {
@@ -415,21 +425,21 @@ hl_circle_final_kernel(hl_circle_final_args a0)
             const int4 c = sm.cir[i];
             if (c.w != 0) {
                 hl_circle o;
-                o.a = c.x + a.roi_x;
-                o.b = c.y + a.roi_y;
+                o.a = c.x + roi_x;
+                o.b = c.y + roi_y;
                 o.radius = c.z;
                 o.votes = c.w;
-                a.out[k++] = o;
+                outp[k++] = o;
             }
         }
-        a.hdr->count = k;
-        a.hdr->ncand = ncand;
-        int st = *a.status;
+        hdrp->count = k;
+        hdrp->ncand = ncand;
+        int st = *statusp;
         if (ncand > HL_CIRCLE_MAXCAND)
             st |= HL_ST_CAND_OVERFLOW;
-        a.hdr->status = st;
-        *a.status = 0;
-        *a.ncand = 0;
+        hdrp->status = st;
+        *statusp = 0;
+        *ncandp = 0;
     }
 }
 
