@@ -53,6 +53,7 @@ struct CircleTileSmem {
     unsigned char rank_lane[CT_WARPS][32];   /* lane of the k-th queued point */
     int2 left[CT_WARPS * 32];                /* the warps' last, partial queues */
     int nleft;
+    int nextb;                               /* next candidate batch of the pass */
 };
 
 /* one vote at the shared-memory word addr when p holds: a predicated
@@ -190,14 +191,23 @@ hl_circle_tile_kernel(hl_circle_tile_args a0)
                     off += sm.red[k];
                 sm.pre[tid + 1] = off + v;
             }
-            if (tid == 0)
+            if (tid == 0) {
                 sm.pre[0] = 0;
+                sm.nextb = 0;
+            }
             __syncthreads();
             const int total = sm.pre[nrow];
-            /* a warp takes 32 consecutive candidates at a time and queues
-             * those inside the halo, one per lane; a full queue walks its 32
+            /* a warp takes the next 32 consecutive candidates (a shared
+             * counter: a warp busy walking takes fewer) and queues those
+             * inside the halo, one per lane; a full queue walks its 32
              * circles at once */
-            for (int ib = warp * 32; ib < total; ib += CT_THREADS) {
+            while (true) {
+                int ib = 0;
+                if (lane == 0)
+                    ib = atomicAdd(&sm.nextb, 32);
+                ib = __shfl_sync(FULL, ib, 0);
+                if (ib >= total)
+                    break;
                 const int i = ib + lane;
                 int cx = CT_NOWHERE, cy = CT_NOWHERE;
                 bool ok = false;
