@@ -12,8 +12,9 @@ top-256 lines: compaction -> vote -> peak NMS -> rank/merge, all on the GPU.
           events between the kernels would serialise their launches)
   e2e   : images/s through the C ABI with host buffers: every step copies
           its image from pinned host memory and reads its LineParam records
-          back (hl_plain_async + copies), the next image's copy overlapping
-          the current image's kernels (copy stream, two device buffers)
+          back (hl_plain_async; upload and read-back streams, two device image
+          and two device result buffers), overlapping the neighbouring steps'
+          kernels
   roofline : the vote kernel against the measured shared-memory atomic
           ceiling of this GPU (conflict-free int32 atomicAdd micro-kernel);
           the whole pipeline against measured HBM bandwidth is reported
@@ -570,20 +571,22 @@ def run_gb300(args):
     L.hl_profile(hl.handle, 0)
     votes = sum(npts[i % len(npts)] * T for i in range(args.steps))
     # e2e through the public API, pipelined: every step copies its image from
-    # pinned host memory (a copy stream, two device buffers) and reads its
-    # line count and lines back to pinned host memory; the copy of step i+1
-    # overlaps the kernels of step i.  Timed from the first copy to the last
-    # read-back, on the device.
+    # pinned host memory (upload stream) and reads its line count and lines
+    # back to pinned host memory (read-back stream); two device image buffers
+    # and two device result buffers let the upload of step i+1 and the
+    # read-back of step i overlap the kernels.  Timed from the first copy to the
+    # last read-back, on the device.
     pinned = [torch.from_numpy(im).pin_memory() for im in imgs_host]
-    copy_stream = torch.cuda.Stream(dev)
+    copy_stream = torch.cuda.Stream(dev)   # uploads
+    back_stream = torch.cuda.Stream(dev)   # read-backs (in order behind their pipelines)
     stg = [torch.empty((H, W), dtype=torch.uint8, device=dev) for _ in range(2)]
     stg_img = [Image(t) for t in stg]
-    ready = [torch.cuda.Event() for _ in range(2)]
-    free = [torch.cuda.Event() for _ in range(2)]
-    lines_e2e = torch.empty(LINESMAX * 3, dtype=torch.int32, device=dev)
-    count_e2e = torch.zeros(1, dtype=torch.int32, device=dev)
-    host_lines = [torch.empty(LINESMAX * 3, dtype=torch.int32).pin_memory() for _ in range(2)]
-    host_count = [torch.empty(1, dtype=torch.int32).pin_memory() for _ in range(2)]
+    ready = [torch.cuda.Event() for _ in range(2)]     # image b uploaded
+    done = [torch.cuda.Event() for _ in range(2)]      # pipeline of buffer b finished
+    fetched = [torch.cuda.Event() for _ in range(2)]   # results of buffer b read back
+    # results: LINESMAX records then the count, one read-back per step
+    res_dev = [torch.empty(LINESMAX * 3 + 1, dtype=torch.int32, device=dev) for _ in range(2)]
+    res_host = [torch.empty(LINESMAX * 3 + 1, dtype=torch.int32).pin_memory() for _ in range(2)]
 
     def e2e_run(nsteps, start_ev=None):
         for i in range(nsteps):
@@ -592,19 +595,23 @@ def run_gb300(args):
                 if start_ev is not None and i == 0:
                     copy_stream.wait_event(start_ev)
                 if i >= 2:
-                    copy_stream.wait_event(free[b])
+                    copy_stream.wait_event(done[b])
                 stg[b].copy_(pinned[i % len(pinned)], non_blocking=True)
                 ready[b].record(copy_stream)
             stream.wait_event(ready[b])
+            if i >= 2:
+                stream.wait_event(fetched[b])
             d = stg_img[b].desc()
             rc = L.hl_plain_async(hl.handle, C.byref(d), LINESMAX,
-                                  C.c_void_p(lines_e2e.data_ptr()),
-                                  C.c_void_p(count_e2e.data_ptr()), sp)
+                                  C.c_void_p(res_dev[b].data_ptr()),
+                                  C.c_void_p(res_dev[b].data_ptr() + 4 * LINESMAX * 3), sp)
             if rc != 0:
                 raise RuntimeError(f"hl_plain_async returned {rc}")
-            free[b].record(stream)
-            host_count[b].copy_(count_e2e, non_blocking=True)
-            host_lines[b].copy_(lines_e2e, non_blocking=True)
+            done[b].record(stream)
+            with torch.cuda.stream(back_stream):
+                back_stream.wait_event(done[b])
+                res_host[b].copy_(res_dev[b], non_blocking=True)
+                fetched[b].record(back_stream)
 
     e2e_run(args.warmup)
     torch.cuda.synchronize(dev)
@@ -612,12 +619,25 @@ def run_gb300(args):
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     e2e_run(args.steps, start_ev=e0)
+    stream.wait_stream(back_stream)
     e1.record(stream)
     torch.cuda.synchronize(dev)
     e2e_ms = e0.elapsed_time(e1)
     _lib.check(L.hl_last_status(hl.handle, C.byref(st), sp), "hl_last_status")
     if st.value != 0:
         raise RuntimeError(f"device status {st.value} in the end-to-end run")
+    # the last step's read-back equals the same image through the device path
+    last = args.steps - 1
+    chk = torch.empty(LINESMAX * 3 + 1, dtype=torch.int32, device=dev)
+    d = dimgs[last % len(dimgs)].desc()
+    _lib.check(L.hl_plain_async(hl.handle, C.byref(d), LINESMAX, C.c_void_p(chk.data_ptr()),
+                                C.c_void_p(chk.data_ptr() + 4 * LINESMAX * 3), sp),
+               "hl_plain_async")
+    torch.cuda.synchronize(dev)
+    got, want = res_host[last % 2], chk.cpu()
+    n = int(want[-1])
+    if int(got[-1]) != n or not torch.equal(got[:3 * min(n, LINESMAX)], want[:3 * min(n, LINESMAX)]):
+        raise RuntimeError("end-to-end read-back differs from the device path")
 
     dev_ms, e2e_ms, vote_ms, votes_all = reduce_over_ranks(
         [dev_ms, e2e_ms, stage[1]], float(votes), ws, dev)
@@ -663,8 +683,9 @@ def run_gb300(args):
         "e2e": {"value": images / (e2e_ms / 1e3), "unit": "images/s",
                 "h2d_bytes_per_step": W * H,
                 "d2h_bytes_per_step": 4 + 12 * LINESMAX,
-                "pipeline": "copy stream + 2 device buffers: the H2D of step i+1 overlaps "
-                            "the kernels of step i; no L2 flush (each image arrives by H2D)"},
+                "pipeline": "upload and read-back streams, 2 device image and 2 device result buffers: the "
+                            "H2D of step i+1 and the D2H of step i overlap the kernels; "
+                            "no L2 flush (each image arrives by H2D)"},
         "gpu_launches": launches_per_step * args.steps,
         "clocks": ck,
         "wall_s_timed_loop": t_wall,
