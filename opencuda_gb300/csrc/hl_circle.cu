@@ -41,7 +41,7 @@
 #define CT_AW (HL_CIRCLE_TW + 8)
 #define CT_AH (HL_CIRCLE_TH + 2)
 #define CT_CELLS (CT_AH * CT_AW)
-#define CT_THREADS 512
+#define CT_THREADS 1024
 #define CT_WARPS (CT_THREADS / 32)
 #define CT_ROWS 256   /* compaction-tile rows of the halo taken per pass */
 
@@ -104,7 +104,7 @@ __device__ __forceinline__ void ct_walk(int x0, int y0, int r, int xw, int yh, u
  * coordinate stays negative for radii below 65536, and y * CT_AW fits an int */
 #define CT_NOWHERE (-(1 << 20))
 
-__global__ void __launch_bounds__(CT_THREADS, 2)
+__global__ void __launch_bounds__(CT_THREADS, 1)
 hl_circle_tile_kernel(hl_circle_tile_args a0)
 {
     extern __shared__ __align__(16) unsigned char ct_raw[];

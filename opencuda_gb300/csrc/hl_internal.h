@@ -261,8 +261,8 @@ static inline cudaError_t hl_launch_pdl(void (*kernel)(Params...), dim3 grid, di
  * counted in shared memory from the points of the halo (the compaction tiles
  * within the radius of the tile); then the interior is written to acc and/or
  * its local maxima appended to keys. */
-#define HL_CIRCLE_TW 192
-#define HL_CIRCLE_TH 128
+#define HL_CIRCLE_TW 256
+#define HL_CIRCLE_TH 192
 /* One image of a circle batch: its points and tile offsets (the batch
  * compaction's region of the image), its ROI, its candidate keys and
  * counters, its result records, and the first CTA of its tile launch. */
