@@ -24,7 +24,7 @@ top-256 lines: compaction -> vote -> peak NMS -> rank/merge, all on the GPU.
   circle : HoughCircle (include/hl_circle.h) at the reference's default
           parameters on a 1024 x 1024 ring scene: device and e2e images/s,
           votes against the shared-memory atomic ceiling, the C restatement
-          (oracle/circle_oracle.c) on one core beside it
+          (oracle/circle_oracle.c) on this host's cores beside it
 
 --impl reference times that CPU transcription alone (the reference's path
 has no CPU implementation of its own; its GPU kernels are the K40-era code
@@ -76,6 +76,14 @@ def reduce_over_ranks(times, votes: float, ws: int, device):
         dist.all_reduce(vt, op=dist.ReduceOp.SUM)
         t = torch.cat([tt, vt])
     return tuple(float(x) for x in t.tolist())
+
+
+def bench_config(n_gpus: int) -> dict:
+    """The workload description both arms print (identical dicts)."""
+    return {"workload": "plain HoughLine 4096x4096, T=720, R=11587, thr 300, top-256",
+            "images_per_step_per_gpu": 1,
+            "parallelism": f"replicas x{n_gpus} (images sharded, no collective)",
+            "l2": "flushed between device-timed steps (256 MiB write, not timed)"}
 
 
 def make_images(rank: int, n: int):
@@ -171,11 +179,14 @@ def cpu_reference_images(imgs, budget_s: float, min_images: int = 1):
     return n, el, votes, O.max_threads()
 
 
-def batched_workload(L, HoughLine, Image, dev, sp, reps: int):
+def batched_workload(L, HoughLine, Image, dev, sp, reps: int, atom_peak: float, cpu: bool):
     """The batched configuration: 256 seeded uneven images (sides 256-2048),
     theta step 0.5 deg, threshold 0.15 * max(w, h) per image, top-32, through
     one hl_batch_async pipeline (CUDA-graph replay, autotuned vote shape);
-    images resident in HBM, L2 flushed between batches."""
+    images resident in HBM, L2 flushed between batches.  Untimed afterwards:
+    every image's batched result against hl_plain on that image, and (in the
+    CPU-baseline leg) every 16th image against the C restatement of the
+    reference path, timed as the batched CPU baseline."""
     import torch
     import cases
     n, K, det = 256, 32, math.pi / 360
@@ -215,12 +226,65 @@ def batched_workload(L, HoughLine, Image, dev, sp, reps: int):
     if st.value != 0:
         raise RuntimeError(f"batched device status {st.value}")
     t = statistics.median(ms)
-    return {"workload": "batched plain HoughLine: 256 uneven images (w, h in [256, 2048]), "
-                        "T=360, rho +-diag per image, thr 0.15*max(w,h), top-32",
-            "value": n / (t / 1e3), "unit": "images/s", "ms_per_batch": t,
-            "gvotes_per_s": votes / (t / 1e3) / 1e9, "pixels": int(sum(im.size for im in imgs)),
-            "reps": reps, "graph": True, "l2": "flushed between batches",
-            "vote_shape": {"window_rows": best[0], "threads": best[1]}}
+    # parity at the benched size: every image's batched lines against hl_plain
+    # on that image alone (same handle parameters, that image's threshold)
+    T = int(math.pi / det)
+    got = lines.view(n, K, 3).cpu().numpy()
+    got_n = counts.cpu().numpy()
+    ref = HoughLine(detheta=det)
+    _lib = _lib_mod()
+    out = (_lib.hl_line * K)()
+    differ = []
+    for i in range(n):
+        ref.setThreshold(thr[i])
+        lm = C.c_int(K)
+        d = dimgs[i].desc()
+        rc = L.hl_plain(ref.handle, C.byref(d), C.byref(lm), out, sp)
+        if rc != 0:
+            raise RuntimeError(f"hl_plain returned {rc}")
+        want = np.frombuffer(bytes(out), np.int32).reshape(K, 3)[:lm.value]
+        if int(got_n[i]) != lm.value or not np.array_equal(got[i, :lm.value], want):
+            differ.append(i)
+    pix = int(sum(im.size for im in imgs))
+    acc_bytes = sum(4 * T * ref.geometry(im.shape[1], im.shape[0]).numrho for im in imgs)
+    res = {"workload": "batched plain HoughLine: 256 uneven images (w, h in [256, 2048]), "
+                       "T=360, rho +-diag per image, thr 0.15*max(w,h), top-32",
+           "value": n / (t / 1e3), "unit": "images/s", "ms_per_batch": t,
+           "gvotes_per_s": votes / (t / 1e3) / 1e9, "pixels": pix,
+           "reps": reps, "graph": True, "l2": "flushed between batches",
+           "vote_shape": {"window_rows": best[0], "threads": best[1]},
+           "matches_plain": not differ, "images_checked_against_plain": n,
+           "roofline": {"bound": "smem_atomic", "achieved": votes / (t / 1e3) / 1e12,
+                        "peak": atom_peak / 1e12, "unit": "T atomics/s",
+                        "frac": votes / (t / 1e3) / atom_peak,
+                        "note": "whole batch call (every launch) as the time",
+                        "hbm": {"bytes_per_batch": pix + acc_bytes,
+                                "achieved_gbs": (pix + acc_bytes) / (t / 1e3) / 1e9,
+                                "scope": "images read once + accumulators written once"}}}
+    if differ:
+        res["differs_from_plain"] = differ[:16]
+    if cpu:
+        from oracle import oracle as O
+        cosv, sinv = ref.trig_table()
+        sample = list(range(0, n, 16))
+        bad, t0 = [], time.perf_counter()
+        for i in sample:
+            w_lines, _, _ = O.houghline(imgs[i], cosv, sinv, det, 1.0, thr[i],
+                                        ref.getThresAng(), ref.getThresDis(), K)
+            a = got[i, :got_n[i]]
+            mine = [(float(np.int32(r[0]).view(np.float32)), int(r[1]), int(r[2])) for r in a]
+            if mine != [tuple(x) for x in w_lines]:
+                bad.append(i)
+        tc = time.perf_counter() - t0
+        res["matches_oracle"] = not bad
+        res["images_checked_against_oracle"] = len(sample)
+        res["cpu_baseline"] = {"value": len(sample) / tc, "unit": "images/s",
+                               "cores": O.max_threads(), "kind": "port",
+                               "sample": f"{len(sample)} of the 256 images (every 16th) through "
+                                         "the C restatement of the reference path, OpenMP "
+                                         "over theta columns; their lines compared with the "
+                                         "batched result"}
+    return res
 
 
 def latency_512(L, HoughLine, Image, dev, reps: int = 300):
@@ -440,9 +504,10 @@ def circle_workload(L, Image, dev, sp, atom_peak: float, reps: int, cpu: bool):
         t0 = time.perf_counter()
         want, _ = O.houghcircle(host, 5, 50, 100, 50.0, 20, cm)
         tc = time.perf_counter() - t0
-        out["cpu_baseline"] = {"value": 1 / tc, "unit": "images/s", "cores": 1, "kind": "port",
-                               "sample": "1 image through the C restatement (vote, local "
-                                         "maxima, sort, merge), one thread"}
+        out["cpu_baseline"] = {"value": 1 / tc, "unit": "images/s", "cores": O.max_threads(),
+                               "kind": "port",
+                               "sample": "1 image through the C restatement (vote with OpenMP "
+                                         "over radii, local maxima, sort, merge)"}
         out["matches_oracle"] = [c.astuple() for c in got] == list(want)
     return out
 
@@ -468,8 +533,7 @@ def run_reference(args):
             "ms_per_step": el / n * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32 votes, f32 rho", "data": "synthetic",
             "gvotes_per_s": votes / el / 1e9,
-            "config": {"workload": "plain HoughLine 4096x4096, T=720, R=11587, thr 300, top-256",
-                       "images_per_step": 1, "parallelism": "replicas"},
+            "config": bench_config(args.gpus),
             "cpu_baseline": {"value": ips, "unit": "images/s", "cores": cores, "kind": "port",
                              "sample": f"{n} full 4096x4096 images (vote + peaks + host tail), "
                                        "OpenMP over theta columns"},
@@ -663,10 +727,8 @@ def run_gb300(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "int32 votes, f32 rho (bit-exact)", "data": "synthetic",
         "gvotes_per_s": votes_all / (dev_ms / 1e3) / 1e9,
-        "config": {"workload": "plain HoughLine 4096x4096, T=720, R=11587, thr 300, top-256",
-                   "edge_points_avg": n_avg, "images_per_step_per_gpu": 1,
-                   "parallelism": f"replicas x{ws} (images sharded, no collective)",
-                   "l2": "flushed between steps (256 MiB write, not timed)"},
+        "config": bench_config(ws),
+        "edge_points_avg": n_avg,
         "stage_ms_avg": {"compact": stage[0] / max(calls.value, 1),
                          "vote": stage[1] / max(calls.value, 1),
                          "peaks": stage[2] / max(calls.value, 1),
@@ -692,7 +754,8 @@ def run_gb300(args):
     }
     line["latency_512"] = latency_512(L, HoughLine, Image, dev)
     if not args.no_batch:
-        line["batched"] = batched_workload(L, HoughLine, Image, dev, sp, min(max(args.steps, 5), 50))
+        line["batched"] = batched_workload(L, HoughLine, Image, dev, sp, min(max(args.steps, 5), 50),
+                                           atom.value, ws == 1 and not args.no_cpu_baseline)
     if not args.no_batch and not args.no_proposal:
         line["proposal"] = [proposal_workload(L, HoughLine, Image, dev, sp, 4, 128, 5),
                             proposal_workload(L, HoughLine, Image, dev, sp, 5, 1024, 3)]

@@ -182,15 +182,23 @@ int hl_compact(hl_handle *h, const hl_image_desc *img, uint32_t *pts_dev,
  * callers that may not call cudaMalloc after start-up (their device memory is
  * owned by another memory manager or fixed by a budget, or an allocation
  * would stall a latency-bound loop).  No counterpart in the reference.  The
- * look-back scratch lives in a static device array of this library (about
- * 512 KiB on every device that loads it, kept until exit), so the ROI may
- * cover at most 65536 tiles of 128 x 32 pixels (HL_OP_OVERFLOW beyond).  The
- * first call on a device looks up that array's device address and should
- * come before any stream capture.  No handle is needed; every call shares
- * the one array and clears what it uses, so calls that overlap on the GPU
- * (two streams at once) race.  Asynchronous on `stream`. */
+ * look-back scratch lives in a static device array of this library (one
+ * state per group of four tiles: about 128 KiB on every device that loads
+ * it, kept until exit), so the ROI may cover at most 65536 tiles of 128 x 32
+ * pixels (HL_OP_OVERFLOW beyond).  The first call on a device looks up that
+ * array's device address and should come before any stream capture.  No
+ * handle is needed; every call shares the one array and clears what it
+ * uses, so calls that overlap on the GPU (two streams at once) race.
+ * Asynchronous on `stream`; a device-side wait that gave up is reported by
+ * hl_compact_noalloc_status, which callers should check before using the
+ * points. */
 int hl_compact_noalloc(const hl_image_desc *img, uint32_t *pts_dev,
                        int *tile_off_dev, int *count_dev, void *stream);
+
+/* Status word of the last hl_compact_noalloc call on this device (0 = fine,
+ * bit 0x1 set = a look-back wait gave up and the tile offsets are not
+ * valid).  Synchronises `stream`; allocates nothing. */
+int hl_compact_noalloc_status(int *status, void *stream);
 
 /* Stages (a)+(b): the int32 accumulator of the ROI in the tight layout
  * acc[(rho - rho_min) * T + k] (R * T ints, DEVICE), for parity checks. */

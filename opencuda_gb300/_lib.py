@@ -122,6 +122,7 @@ SIGNATURES = {
     "hl_plain_points": (I, [H, P, I, PI, P, P]),
     "hl_compact": (I, [H, C.POINTER(hl_image_desc), P, P, P, P]),
     "hl_compact_noalloc": (I, [C.POINTER(hl_image_desc), P, P, P, P]),
+    "hl_compact_noalloc_status": (I, [PI, P]),
     "hl_accumulator": (I, [H, C.POINTER(hl_image_desc), P, P]),
     "hl_accumulator_ref_layout": (I, [H, C.POINTER(hl_image_desc), P, P]),
     "hl_lines_from_accumulator": (I, [H, P, I, I, PI, P, P]),

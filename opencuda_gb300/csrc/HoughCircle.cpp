@@ -163,7 +163,11 @@ int HoughCircle::pieceCircle(Image *inimg, int piecenum, int *circleMax,
     std::vector<hl_circle> res((size_t)np * 10);
     std::vector<int> cnt((size_t)np);
     rc = hl_circles_batch(gpu_, d.data(), np, &p, 10, res.data(), cnt.data(), NULL);
-    if (rc != NO_ERROR)
+    /* the reference ignores each piece's return code and keeps the other
+     * pieces' circles (:1366-1375); a piece with more local maxima than the
+     * candidate buffer holds (OP_OVERFLOW) contributes none here, its count
+     * being 0, and the rest are kept */
+    if (rc != NO_ERROR && rc != OP_OVERFLOW)
         return rc;
     int pointer = 0;
     for (int i = 0; i < np; i++)

@@ -11,8 +11,11 @@
  * 128 x 32 tile, a tile ticket, a status word); hl_compact keeps that scratch
  * in a handle, which allocates.  hl_compact_noalloc instead keeps it in the
  * file-scope device array below, which every GPU that loads this library
- * holds until the process exits (HL_NOALLOC_MAX_TILES state words plus two
- * counters, about 512 KiB), and launches the same compaction kernel on it.
+ * holds until the process exits, and launches the same compaction kernel on
+ * it.  The kernel keeps one look-back state per group of HL_COMPACT_GROUP
+ * tiles, so the array holds HL_NOALLOC_MAX_TILES / HL_COMPACT_GROUP states
+ * plus two counters (about 128 KiB).  hl_compact_noalloc_status reads the
+ * status word the last call left in it.
  */
 #include <mutex>
 
@@ -20,9 +23,12 @@
 
 #include "hl_internal.h"
 
-/* [0] tile ticket, [1] status word, [2 ..] one look-back state per tile */
+#define NOALLOC_MAX_GROUPS (HL_NOALLOC_MAX_TILES / HL_COMPACT_GROUP)
+
+/* [0] group ticket, [1] status word, [2 ..] one look-back state per group
+ * of HL_COMPACT_GROUP tiles */
 static __device__ __align__(256) unsigned long long
-    g_noalloc_scratch[HL_NOALLOC_MAX_TILES + 2];
+    g_noalloc_scratch[NOALLOC_MAX_GROUPS + 2];
 
 /* Host-side stand-in of the array above: its name is not a device address in
  * host code, so each device's address is looked up once, with that device
@@ -65,7 +71,8 @@ extern "C" int hl_compact_noalloc(const hl_image_desc *img, uint32_t *pts_dev,
         return HL_INVALID_DATA;
     const int tiles_x = (w + HL_TILE_W - 1) / HL_TILE_W;
     const long long ntiles = (long long)tiles_x * ((h + HL_TILE_H - 1) / HL_TILE_H);
-    if (ntiles > HL_NOALLOC_MAX_TILES)
+    const long long ngroups = (ntiles + HL_COMPACT_GROUP - 1) / HL_COMPACT_GROUP;
+    if (ngroups > NOALLOC_MAX_GROUPS)
         return HL_OP_OVERFLOW;   /* the ROI needs more look-back states */
     unsigned long long *scratch = nullptr;
     int rc = scratch_for_current_device(&scratch);
@@ -73,8 +80,8 @@ extern "C" int hl_compact_noalloc(const hl_image_desc *img, uint32_t *pts_dev,
         return rc;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     /* the array keeps the previous call's contents: the ticket, the status
-     * and the states this call uses start from zero */
-    if (cudaMemsetAsync(scratch, 0, sizeof(unsigned long long) * (size_t)(ntiles + 2),
+     * and the group states this call uses start from zero */
+    if (cudaMemsetAsync(scratch, 0, sizeof(unsigned long long) * (size_t)(ngroups + 2),
                         s) != cudaSuccess)
         return HL_CUDA_ERROR;
     hl_compact_args ca;
@@ -99,4 +106,21 @@ extern "C" int hl_compact_noalloc(const hl_image_desc *img, uint32_t *pts_dev,
     ca.tile_off = tile_off_dev;
     ca.count = count_dev;
     return hl_launch_compact(&ca, s) == cudaSuccess ? HL_NO_ERROR : HL_CUDA_ERROR;
+}
+
+extern "C" int hl_compact_noalloc_status(int *status, void *stream)
+{
+    if (!status)
+        return HL_NULL_POINTER;
+    unsigned long long *scratch = nullptr;
+    int rc = scratch_for_current_device(&scratch);
+    if (rc != HL_NO_ERROR)
+        return rc;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int v = 0;
+    if (cudaMemcpyAsync(&v, scratch + 1, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return HL_CUDA_ERROR;
+    *status = v;
+    return HL_NO_ERROR;
 }

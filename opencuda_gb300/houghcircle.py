@@ -148,7 +148,9 @@ class HoughCircle:
         rc, per = self.houghcircleBatch(pieces, 10, stream)
         inimg.roiX1, inimg.roiY1 = (piecenum - 1) * cx, (piecenum - 1) * cy
         inimg.roiX2, inimg.roiY2 = piecenum * cx - 1, piecenum * cy - 1
-        if rc != _lib.NO_ERROR:
+        # the reference keeps the other pieces when one fails (:1366-1375):
+        # a piece that overflowed its candidate buffer has no circles here
+        if rc not in (_lib.NO_ERROR, _lib.OP_OVERFLOW):
             return rc, []
         out = [c for p in per for c in p]
         return _lib.NO_ERROR, out[:max(circleMax, 0)]

@@ -36,12 +36,17 @@ long long hc_vote(const uint8_t *roi, long pitch, int w, int h, int rmin, int rm
     memset(acc, 0, sizeof(int32_t) * (size_t)nr * w * h);
     long long n = 0;
     for (int y0 = 0; y0 < h; y0++)
-        for (int x0 = 0; x0 < w; x0++) {
-            if (roi[(size_t)y0 * pitch + x0] != 255)
-                continue;
-            n++;
-            for (int z = 0; z < nr; z++) {
-                const int radius = z + rmin;
+        for (int x0 = 0; x0 < w; x0++)
+            n += roi[(size_t)y0 * pitch + x0] == 255;
+    /* the radii are independent layers of the accumulator: one thread per
+     * radius at a time, every pixel's votes for it in the reference order */
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int z = 0; z < nr; z++) {
+        const int radius = z + rmin;
+        for (int y0 = 0; y0 < h; y0++)
+            for (int x0 = 0; x0 < w; x0++) {
+                if (roi[(size_t)y0 * pitch + x0] != 255)
+                    continue;
                 int x = 0, y = radius, d = 3 - 2 * radius;
                 while (x < y) {
                     vote1(acc, w, h, x0 + x, y0 + y, z);
@@ -61,7 +66,7 @@ long long hc_vote(const uint8_t *roi, long pitch, int w, int h, int rmin, int rm
                     x++;
                 }
             }
-        }
+    }
     return n;
 }
 

@@ -71,6 +71,32 @@ int main(int argc, char **argv)
     rc = hc.houghcircle(NULL, cst, &cm, cir, false);
     print_circles("points", rc, cm, cir);
 
+    // pieceCircle with one piece that overflows the candidate buffer (argv[4]:
+    // a second W x H image whose bottom-right piece is dense noise): the
+    // other pieces' circles are kept, as the reference keeps them
+    if (argc > 4) {
+        Image *ov = NULL;
+        ImageBasicOp::newImage(&ov);
+        ImageBasicOp::makeAtHost(ov, W, H);
+        FILE *g = fopen(argv[4], "rb");
+        if (!g || fread(ov->imgData, 1, (size_t)W * H, g) != (size_t)W * H)
+            return 4;
+        fclose(g);
+        ov->roiX1 = W / 2;
+        ov->roiY1 = H / 2;
+        ov->roiX2 = W / 2 + W / 2 - 1;
+        ov->roiY2 = H / 2 + H / 2 - 1;
+        cm = 32;
+        printf("ovrc=%d\n", hc.houghcircle(ov, NULL, &cm, cir, false));
+        ov->roiX1 = ov->roiY1 = 0;
+        ov->roiX2 = W;
+        ov->roiY2 = H;
+        cm = 64;
+        rc = hc.pieceCircle(ov, 2, &cm, cir, false);
+        print_circles("pieceov", rc, cm, cir);
+        ImageBasicOp::deleteImage(ov);
+    }
+
     // argument checks and the setters' validation
     printf("null=%d\n", hc.houghcircle(NULL, NULL, &cm, cir, false));
     HoughCircle d;

@@ -216,5 +216,7 @@ def main(out_dir: str, circle_only: bool = False) -> int:
 
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    sys.exit(main(args[0] if args else str(ROOT / "gpurun_out" / "golden"),
-                  circle_only="--circle-only" in sys.argv))
+    if len(args) != 1:
+        sys.exit("usage: make_golden.py OUTPUT_DIR [--circle-only]  (run on a GPU host; "
+                 "copy OUTPUT_DIR/golden.json next to this script to commit it)")
+    sys.exit(main(args[0], circle_only="--circle-only" in sys.argv))

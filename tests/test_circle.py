@@ -183,6 +183,32 @@ def test_piece_circle(hc_mod):
     assert (im.roiX1, im.roiY1, im.roiX2, im.roiY2) == (220, 160, 329, 239)
 
 
+def test_piece_circle_keeps_pieces_when_one_overflows(hc_mod):
+    """A piece with more than 4096 local maxima above the threshold (dense
+    noise) fails alone: pieceCircle keeps the other pieces' circles, as the
+    reference does (okano_3_0/HoughCircle.cu:1366-1375)."""
+    HoughCircle, Image, _ = hc_mod
+    from opencuda_gb300 import _lib
+    img = ring_image(330, 240, [(50, 40, 20), (170, 120, 30), (280, 200, 25), (90, 190, 15)],
+                     0.01, seed=3)
+    rng = np.random.default_rng(9)
+    img[80:159, 110:219] = np.where(rng.random((79, 109)) < 0.4, 255, 0)   # piece (1, 1)
+    hc = HoughCircle(5, 30, 20.0, 5, 20)
+    rc, _ = hc.houghcircle(Image.from_host(img, (110, 80, 219, 159)), None, 10)
+    assert rc == _lib.OP_OVERFLOW
+    rc, got = hc.pieceCircle(Image.from_host(img), 3, 40)
+    assert rc == 0
+    want = []
+    for y in range(3):
+        for x in range(3):
+            if (x, y) == (1, 1):
+                continue
+            x1, y1 = x * 110, y * 80
+            w, _ = O.houghcircle(img[y1:y1 + 79, x1:x1 + 109], 5, 30, 20, 20.0, 5, 10)
+            want += [(a + x1, b + y1, r, v) for a, b, r, v in w]
+    assert [c.astuple() for c in got] == want[:40]
+
+
 
 def test_random_configurations(hc_mod):
     """Seeded sweep: image sizes 1-400, ROIs covering at least the middle

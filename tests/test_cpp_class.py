@@ -123,7 +123,14 @@ def test_cpp_circle_class_matches_oracle(cuda, tmp_path):
     img = cases.circle_scene(W, H, 8, 8, 45, 3000, 21)
     raw = tmp_path / "scene.raw"
     raw.write_bytes(img.tobytes())
-    r = subprocess.run([str(exe), str(raw), str(W), str(H)], capture_output=True,
+    # the same scene with its bottom-right piece replaced by 40% noise: that
+    # piece has far more than 4096 local maxima above the threshold
+    ov = img.copy()
+    rng = np.random.default_rng(5)
+    ov[H // 2:, W // 2:] = np.where(rng.random((H - H // 2, W - W // 2)) < 0.4, 255, 0)
+    raw_ov = tmp_path / "overflow.raw"
+    raw_ov.write_bytes(ov.tobytes())
+    r = subprocess.run([str(exe), str(raw), str(W), str(H), str(raw_ov)], capture_output=True,
                        text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     got, rcn, misc = {}, {}, {}
@@ -153,6 +160,16 @@ def test_cpp_circle_class_matches_oracle(cuda, tmp_path):
     pieces = pieces[:64]
     assert rcn["piece"] == (0, len(pieces)) and got.get("piece", []) == pieces
     assert misc["lastroi"] == [str(cx), str(cy), str(2 * cx - 1), str(2 * cy - 1)]
+    # one overflowing piece: OP_OVERFLOW for that piece alone, the other three
+    # pieces' circles kept by pieceCircle (okano_3_0/HoughCircle.cu:1366-1375)
+    assert "ovrc=-3" in r.stdout
+    kept = []
+    for y in range(2):
+        for x in range(2):
+            if (x, y) != (1, 1):
+                x1, y1 = x * cx, y * cy
+                kept += oracle(ov[y1:y1 + cy - 1, x1:x1 + cx - 1], 10, x1, y1)
+    assert rcn["pieceov"] == (0, len(kept)) and got.get("pieceov", []) == kept
     ys, xs = np.nonzero(img == 255)
     pim = np.zeros((ys.max() + 2, xs.max() + 2), np.uint8)
     pim[ys, xs] = 255

@@ -220,3 +220,50 @@ def test_trig_tables_recorded():
         rec = g["tables"][f"T{T}"]
         assert O.fnv1a(z[f"cos_T{T}"]) == rec["fnv_cos"]
         assert O.fnv1a(z[f"sin_T{T}"]) == rec["fnv_sin"]
+
+
+def _tie_report(images, det, thresholds, linesmax):
+    """Per image: does the reference's Shell order (okano_3_0/HoughLine.cu:
+    853-873, unstable on equal votes) give another final list than the
+    canonical order?  Also counts candidates that share their vote count
+    with another candidate."""
+    c, s = _table(det)
+    differ, tied, total = 0, 0, 0
+    for img, thr in zip(images, thresholds):
+        acc, rho_min, _ = O.vote_image(img, c, s)
+        R, T = acc.shape
+        h, w = img.shape
+        pk = O.peaks(acc, thr)
+        g = O.geom(T, rho_min, R, O.ref_numrho(w, h), det, 50, np.float32(O.default_thresang()))
+        can, _, _ = O.rank_merge(acc, g, pk, linesmax, O.RANK_CANONICAL)
+        ref, _, _ = O.rank_merge(acc, g, pk, linesmax, O.RANK_REF_SHELL)
+        differ += can != ref
+        v = acc.reshape(-1)[pk]
+        _, cnt = np.unique(v, return_counts=True)
+        tied += int(cnt[cnt > 1].sum())
+        total += len(pk)
+    return differ, tied, total
+
+
+def test_tie_order_disagreement_report(capsys):
+    """How often the reference's tie order would change the reported lines
+    on the benchmark configurations (the canonical order is the contract;
+    the Shell mode exists to measure this).  Printed, not asserted: the
+    numbers are recorded beside the parity contract."""
+    rows = []
+    imgs1 = [cases.synth(1, 1234 + i, 0) for i in range(16)]
+    rows.append(("512x512 T=180 thr 100 top-16", *_tie_report(imgs1, math.pi / 180,
+                                                               [100] * 16, 16)))
+    img2 = [cases.synth(2, 1234, 0)]
+    rows.append(("4096x4096 T=720 thr 300 top-256", *_tie_report(img2, math.pi / 720,
+                                                                  [300], 256)))
+    imgs3 = [cases.synth(3, 1234, i) for i in range(0, 256, 16)]
+    rows.append(("uneven 256-2048 T=360 thr 0.15max top-32",
+                 *_tie_report(imgs3, math.pi / 360, [int(0.15 * max(im.shape)) for im in imgs3],
+                              32)))
+    with capsys.disabled():
+        for name, differ, tied, total in rows:
+            print(f"\ntie order [{name}]: final lists differ on {differ} image(s); "
+                  f"{tied} of {total} peaks share their vote count")
+    for _, differ, tied, total in rows:
+        assert 0 <= tied <= total

@@ -44,6 +44,9 @@ def _compact_noalloc(L, t, roi, torch):
     assert L.hl_compact_noalloc(C.byref(d), C.c_void_p(pts.data_ptr()),
                                 C.c_void_p(off.data_ptr()),
                                 C.c_void_p(cnt.data_ptr()), None) == 0
+    st = C.c_int(-1)
+    assert L.hl_compact_noalloc_status(C.byref(st), None) == 0
+    assert st.value == 0, "a look-back wait gave up"
     torch.cuda.synchronize()
     return pts, off, cnt
 
@@ -77,7 +80,8 @@ def test_noalloc_rejects_oversized_roi(cuda):
     import torch
     from opencuda_gb300 import _lib
     L = _lib.load()
-    # 65536 tiles of 128 x 32 is the limit; 16512 x 16384 needs 129 x 512.
+    # 65536 tiles of 128 x 32 (16384 groups of four) is the limit;
+    # 16512 x 16384 needs 129 x 512 tiles = 16512 groups.
     # Inputs and outputs are sized for the ROI all the same, so nothing could
     # be touched out of bounds even if the size check were missing.
     w, h = 16512, 16384
