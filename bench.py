@@ -115,6 +115,74 @@ def ncu_traffic():
     return None
 
 
+class NvmlClockSampler:
+    """SM clock and clock-event reasons read from NVML (the driver's
+    libnvidia-ml, through ctypes; read-only queries) by a thread every
+    millisecond while it runs, so a timed region of a few milliseconds still
+    gets samples.  None when NVML is unavailable."""
+    SM = 1
+    REASONS = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown", 0x20: "sw_thermal_slowdown",
+               0x4: "sw_power_cap"}
+
+    def __init__(self, torch_device):
+        import threading
+        self.rows, self.h, self.nv = [], None, None
+        try:
+            nv = C.CDLL("libnvidia-ml.so.1")
+            if nv.nvmlInit_v2() != 0:
+                return
+            import torch
+            pr = torch.cuda.get_device_properties(torch_device)
+            h = C.c_void_p()
+            bus = getattr(pr, "pci_bus_id", None)
+            dom = getattr(pr, "pci_domain_id", 0)
+            devid = getattr(pr, "pci_device_id", 0)
+            ok = False
+            if bus is not None:
+                ident = f"{dom:08x}:{bus:02x}:{devid:02x}.0".encode()
+                ok = nv.nvmlDeviceGetHandleByPciBusId_v2(ident, C.byref(h)) == 0
+            if not ok and nv.nvmlDeviceGetHandleByIndex_v2(
+                    int(torch_device.index or 0), C.byref(h)) != 0:
+                return
+            self.nv, self.h = nv, h
+            mx = C.c_uint()
+            self.max_mhz = float(mx.value) if nv.nvmlDeviceGetMaxClockInfo(
+                h, self.SM, C.byref(mx)) == 0 else None
+        except (OSError, AttributeError):
+            return
+        self.stop_flag = threading.Event()
+        self.t = threading.Thread(target=self._run, daemon=True)
+        self.t.start()
+
+    def _sample(self):
+        mhz, rs = C.c_uint(), C.c_ulonglong()
+        if self.nv.nvmlDeviceGetClockInfo(self.h, self.SM, C.byref(mhz)) != 0:
+            return
+        f = getattr(self.nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        r = rs.value if f(self.h, C.byref(rs)) == 0 else 0
+        self.rows.append((float(mhz.value), r))
+
+    def _run(self):
+        while not self.stop_flag.is_set():
+            self._sample()
+            time.sleep(0.001)
+
+    def stop(self):
+        if self.h is None:
+            return None
+        self.stop_flag.set()
+        self.t.join(timeout=5)
+        if not self.rows:
+            self._sample()
+        if not self.rows:
+            return None
+        reasons = sorted({n for _, r in self.rows for b, n in self.REASONS.items() if r & b})
+        return {"sm_mhz": statistics.median(m for m, _ in self.rows),
+                "sm_max_mhz": self.max_mhz, "reasons": reasons, "samples": len(self.rows),
+                "source": "NVML every 1 ms during the timed steps"}
+
+
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -605,7 +673,9 @@ def run_gb300(args):
            for _ in range(args.steps)]
     gpu_index = os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[local] \
         if os.environ.get("CUDA_VISIBLE_DEVICES") else str(local)
-    clocks = ClockSampler(gpu_index)
+    clocks = NvmlClockSampler(dev)
+    if clocks.h is None:
+        clocks = ClockSampler(gpu_index)
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(dev)

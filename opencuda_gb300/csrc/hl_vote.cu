@@ -3,17 +3,18 @@
  *
  * Vote rule (okano_3_0/HoughLine.cu:86-130): an edge point (x, y) adds one
  * to bin (k, trunc(fl(x*cos_k) + fl(y*sin_k))) for every k.  The products and
- * the sum are rounded separately (__fmul_rn / __fadd_rn: no FMA contraction),
- * the float is truncated toward zero (the reference's +-0.5 step after the
- * (int) cast is a no-op), and cos_k/sin_k come from the GPU-evaluated table.
+ * the sum are rounded separately (packed f32x2 products as fma(a, b, +0) and
+ * a packed add: no FMA contraction, see f2_mul), the float is truncated
+ * toward zero (the reference's +-0.5 step after the (int) cast is a no-op),
+ * and cos_k/sin_k come from the GPU-evaluated table.
  *
  * Work decomposition.  A work item is one (theta slice, rho window) block of
- * the accumulator, held in shared memory as acc[row][lane]: 32 thetas (one
- * per lane) x win_rows rho bins.  A warp votes one point at a time; its 32
- * lanes add to 32 different thetas of the same point -- 32 different banks --
- * so every shared-memory reduction is conflict-free and no two lanes ever hit
- * one address (the aggregation a warp-aggregated atomic would buy is built
- * into the layout).
+ * the accumulator, held in shared memory as acc[row][column]: 32 thetas x
+ * win_rows rho bins.  A warp votes 8 points at a time on the diagonal
+ * schedule (DiagTab): at every step its 32 lanes add to 32 different theta
+ * columns -- 32 different banks -- so every shared-memory reduction is
+ * conflict-free and no two lanes ever hit one address (the aggregation a
+ * warp-aggregated atomic would buy is built into the layout).
  *
  * Pipeline.  Persistent CTAs of one producer warp and consumer warps that
  * meet only on mbarriers.  The producer takes items heaviest-first from a
@@ -38,14 +39,16 @@
  * slot, summed into the block by hl_merge_kernel) and clear it; every bin is
  * written exactly once, so the accumulator needs no clearing.
  *
- * Per point and consumer warp: half a broadcast shared load (16-byte loads
- * of point pairs), two multiplies, two adds (the second one rounds to an
- * integer, see vote_row), one subtract, one unsigned min, one address
- * multiply-add and one red.shared -- under nine issue slots and no branch
- * per vote.
+ * Per vote: one packed multiply of x and one of y (two thetas per f32x2
+ * instruction, so half of each), half a packed add, half a packed
+ * magic-constant add (the float -> integer, see RHO_MAGIC), one clamp to the
+ * dump row, one address add and one red.shared -- about five issue slots --
+ * plus an eighth of a point load (the diagonal schedule, see DiagTab); no
+ * branch per vote.
  *
- * Bounds: every vote's row is clamped to the window's dump row (lanes past
- * the last theta to row 0 of their padding column, zeroed before the store).
+ * Bounds: every vote's row is clamped to the window's dump row, one row past
+ * the window in every column; the padding columns (thetas >= T) are stored
+ * as zero.
  * After the start there is no block-wide barrier, and every mbarrier wait is
  * bounded: a time-out sets a status bit that the host reads with the result
  * and an abort flag on which every other waiting warp gives up too; the
@@ -71,23 +74,6 @@
 #define RHO_MAGIC 12582912.0f
 #define RHO_MAGIC_BITS 0x4B400000
 enum { CV_EXACT = 0, CV_FLOOR = 1, CV_CEIL = 2 };
-
-/* window-relative row of a point for this lane's theta; base is the rho of
- * row 0 (CV_EXACT) or RHO_MAGIC_BITS plus that rho */
-template <bool UNIT, int CV>
-__device__ __forceinline__ unsigned vote_row(float x, float y, float c,
-                                             float s, float irho, int base)
-{
-    const float v = rho_f<UNIT>(x, y, c, s, irho);
-    int r;
-    if (CV == CV_FLOOR)
-        r = __float_as_int(__fadd_rz(v, RHO_MAGIC));
-    else if (CV == CV_CEIL)
-        r = __float_as_int(__fadd_ru(v, RHO_MAGIC));
-    else
-        r = __float2int_rz(v);
-    return (unsigned)(r - base);
-}
 
 /* ---- mbarrier + bulk copy ---------------------------------------------- */
 __device__ __forceinline__ unsigned smem_u32(const void *p)
@@ -144,79 +130,142 @@ __device__ __forceinline__ bool mbar_wait_sleep(unsigned long long *bar,
     return false;
 }
 
-/* 32 points (16 float4 pairs) of one consumer warp's share, no bounds */
-template <bool UNIT, int CV>
-__device__ __forceinline__ void vote_share32(const float2 *pts, float c,
-                                             float s, float irho, int base,
-                                             unsigned acc_l, unsigned lim);
-
 /* one vote, no returned value */
 __device__ __forceinline__ void red_smem(unsigned addr)
 {
     asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(addr));
 }
 
-/* Votes of a consumer warp for points j, j + step, ... < n of a ring slot.
- * A row outside the window (rl >= lim as unsigned) is sent to row lim: the
- * dump row just past the window (lim = window rows) or, for lanes past the
- * last theta (lim = 0), row 0 of the lane's own padding column.  No vote is
- * predicated, so the loop has no branch per vote. */
-template <bool UNIT, int CV>
-__device__ __forceinline__ void vote_batch(const float2 *pts, int n, int j,
-                                           int step, float c, float s,
-                                           float irho, int base,
-                                           unsigned acc_l, unsigned lim)
+/* ---- packed f32x2 arithmetic ------------------------------------------ *
+ * Two lanes of a 64-bit register pair per instruction.  The products are
+ * formed as fma.rn(a, b, +0): exactly fl(a*b) for the finite operands here
+ * (a -0 product becomes +0, which no later sum or truncation can tell
+ * apart).  A plain mul.rn.f32x2 followed by add.rn.f32x2 is contracted by
+ * ptxas into one fused multiply-add, which changes rho in a small fraction
+ * of votes; the fma form is never contracted (checked on the GPU against
+ * the scalar __fmul_rn/__fadd_rn rule for every (x, y) of a 4096 x 4096
+ * image at T = 720: no difference). */
+typedef unsigned long long f2x;
+__device__ __forceinline__ f2x f2_pack(float a, float b)
 {
-    for (; j + 3 * step < n; j += 4 * step) {
-        const float2 p0 = pts[j];
-        const float2 p1 = pts[j + step];
-        const float2 p2 = pts[j + 2 * step];
-        const float2 p3 = pts[j + 3 * step];
-        const unsigned l0 = min(vote_row<UNIT, CV>(p0.x, p0.y, c, s, irho, base), lim);
-        const unsigned l1 = min(vote_row<UNIT, CV>(p1.x, p1.y, c, s, irho, base), lim);
-        const unsigned l2 = min(vote_row<UNIT, CV>(p2.x, p2.y, c, s, irho, base), lim);
-        const unsigned l3 = min(vote_row<UNIT, CV>(p3.x, p3.y, c, s, irho, base), lim);
-        red_smem(acc_l + 128u * l0);
-        red_smem(acc_l + 128u * l1);
-        red_smem(acc_l + 128u * l2);
-        red_smem(acc_l + 128u * l3);
-    }
-    for (; j < n; j += step) {
-        const float2 p0 = pts[j];
-        red_smem(acc_l + 128u * min(vote_row<UNIT, CV>(p0.x, p0.y, c, s, irho, base), lim));
-    }
+    f2x r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(f2x r, unsigned &a, unsigned &b)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=r"(a), "=r"(b) : "l"(r));
+}
+__device__ __forceinline__ f2x f2_mul(f2x a, f2x b)
+{
+    f2x d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(0ull));
+    return d;
+}
+__device__ __forceinline__ f2x f2_add(f2x a, f2x b)
+{
+    f2x d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2x f2_add_rz(f2x a, f2x b)
+{
+    f2x d;
+    asm("add.rz.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2x f2_add_rp(f2x a, f2x b)
+{
+    f2x d;
+    asm("add.rp.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
 }
 
-template <bool UNIT, int CV>
-__device__ __forceinline__ void vote_share32(const float2 *pts, float c,
-                                             float s, float irho, int base,
-                                             unsigned acc_l, unsigned lim)
+/* Diagonal vote schedule.  A consumer warp votes 8 points at a time, each
+ * point on 4 lanes: lane = p + 8 j (point p, theta group j).  At step i the
+ * lane votes theta column 8 j + (p + i) % 8 of the slice, so at every step
+ * the 32 lanes address 32 different columns -- 32 different banks, whatever
+ * rows their points reach -- and over the 8 steps every point votes all 32
+ * thetas.  A lane loads its point once per 8 votes (one shared-memory
+ * wavefront for the warp's 8 points), where a broadcast load per point
+ * would cost as many wavefronts as the atomics themselves: the shared
+ * pipe serves loads, shuffles and reductions alike at about one wavefront
+ * per SM-clock.  Each lane keeps its 8 columns' cos/sin as f32x2 pairs of
+ * consecutive steps and the columns' shared-memory addresses. */
+struct DiagTab {
+    f2x c[4], s[4];        /* cos / sin of the lane's columns, steps (2i, 2i + 1) */
+    unsigned col[8];       /* address of the lane's column at step i, row 0 */
+};
+
+__device__ __forceinline__ void diag_table(DiagTab &t, const float *cs, const float *sn,
+                                           unsigned acc_base, int lane)
 {
-    const float4 *q = reinterpret_cast<const float4 *>(pts);
+    const int p = lane & 7, j = lane >> 3;
 #pragma unroll
-    for (int i = 0; i < 16; i += 2) {
-        const float4 u = q[i], w = q[i + 1];
-        const unsigned l0 = min(vote_row<UNIT, CV>(u.x, u.y, c, s, irho, base), lim);
-        const unsigned l1 = min(vote_row<UNIT, CV>(u.z, u.w, c, s, irho, base), lim);
-        const unsigned l2 = min(vote_row<UNIT, CV>(w.x, w.y, c, s, irho, base), lim);
-        const unsigned l3 = min(vote_row<UNIT, CV>(w.z, w.w, c, s, irho, base), lim);
-        red_smem(acc_l + 128u * l0);
-        red_smem(acc_l + 128u * l1);
-        red_smem(acc_l + 128u * l2);
-        red_smem(acc_l + 128u * l3);
+    for (int i = 0; i < 8; i += 2) {
+        const int c0 = 8 * j + ((p + i) & 7), c1 = 8 * j + ((p + i + 1) & 7);
+        t.c[i / 2] = f2_pack(cs[c0], cs[c1]);
+        t.s[i / 2] = f2_pack(sn[c0], sn[c1]);
+        t.col[i] = acc_base + 4u * (unsigned)c0;
+        t.col[i + 1] = acc_base + 4u * (unsigned)c1;
     }
 }
 
-/* a consumer warp's share of a slot: up to 32 points starting at pts */
+/* The 8 steps of one point (x, y) on this lane.  rho per the vote rule
+ * (okano_3_0/HoughLine.cu:115-121), the row relative to the window clamped
+ * to the dump row `lim`; float -> integer by the magic constant (CV_FLOOR /
+ * CV_CEIL, see RHO_MAGIC) or by the exact conversion (CV_EXACT). */
 template <bool UNIT, int CV>
-__device__ __forceinline__ void vote_share(const float2 *pts, int m, float c,
-                                           float s, float irho, int base,
-                                           unsigned acc_l, unsigned lim)
+__device__ __forceinline__ void diag_point(float x, float y, const DiagTab &t, f2x ir,
+                                           int base, unsigned lim)
 {
-    if (m >= 32)
-        vote_share32<UNIT, CV>(pts, c, s, irho, base, acc_l, lim);
-    else if (m > 0)
-        vote_batch<UNIT, CV>(pts, m, 0, 1, c, s, irho, base, acc_l, lim);
+    const f2x X = f2_pack(x, x), Y = f2_pack(y, y);
+    const f2x M = f2_pack(RHO_MAGIC, RHO_MAGIC);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        f2x a = f2_mul(X, t.c[i]), b = f2_mul(Y, t.s[i]);
+        if (!UNIT) {
+            a = f2_mul(a, ir);
+            b = f2_mul(b, ir);
+        }
+        const f2x v = f2_add(a, b);
+        unsigned r0, r1;
+        if (CV == CV_FLOOR) {
+            f2_unpack(f2_add_rz(v, M), r0, r1);
+        } else if (CV == CV_CEIL) {
+            f2_unpack(f2_add_rp(v, M), r0, r1);
+        } else {
+            unsigned u0, u1;
+            f2_unpack(v, u0, u1);
+            r0 = (unsigned)__float2int_rz(__uint_as_float(u0));
+            r1 = (unsigned)__float2int_rz(__uint_as_float(u1));
+        }
+        red_smem(t.col[2 * i] + 128u * min(r0 - (unsigned)base, lim));
+        red_smem(t.col[2 * i + 1] + 128u * min(r1 - (unsigned)base, lim));
+    }
+}
+
+/* A consumer warp's share of a slot: points [0, m) of pts, m <= 64, 8 per
+ * round.  Entries past m (stale ring data) vote as the sentinel (1e30, 0),
+ * whose rows lie outside every window and go to the dump row. */
+template <bool UNIT, int CV>
+__device__ __forceinline__ void vote_share(const float2 *pts, int m, const DiagTab &t,
+                                           f2x ir, int base, unsigned lim, int p)
+{
+    if (m >= 64) {
+#pragma unroll 2
+        for (int r = 0; r < 64; r += 8) {
+            const float2 q = pts[r + p];
+            diag_point<UNIT, CV>(q.x, q.y, t, ir, base, lim);
+        }
+    } else {
+        for (int r = 0; r < m; r += 8) {
+            float2 q = pts[r + p];
+            if (r + p >= m)
+                q = make_float2(1e30f, 0.0f);
+            diag_point<UNIT, CV>(q.x, q.y, t, ir, base, lim);
+        }
+    }
 }
 
 /* Bounded wait that also gives up as soon as another warp of the CTA has
@@ -609,11 +658,14 @@ hl_vote_kernel(hl_vote_args a)
 
     const int cw = warp - 1;
     const int ctid = tid - 32, nct = nthr - 32;
-    const unsigned acc_l = smem_u32(s_acc) + 4u * lane;
+    const unsigned acc_base = smem_u32(s_acc);
+    const f2x ir = f2_pack(a.irho, a.irho);
+    const int pl = lane & 7;
     int4 *src4 = reinterpret_cast<int4 *>(s_acc);
     unsigned seq = 0, nseg = 0, cpar = 0;
     /* the current item */
-    float c = 0.0f, s = 0.0f;
+    DiagTab tab;
+    diag_table(tab, a.cosv, a.sinv, acc_base, lane);
     int cv = CV_EXACT, vbase = 0, rows = 0, w0 = 0, k0 = 0;
     unsigned lrows = 0;
     int32_t *acc_g = nullptr;
@@ -630,12 +682,14 @@ hl_vote_kernel(hl_vote_args a)
         if (item >= 0 && g.first) {
             const int slice = item % nslices, win = item / nslices;
             k0 = slice * HL_SLICE;
-            c = g.c[lane];
-            s = g.s[lane];
+            diag_table(tab, g.c, g.s, acc_base, lane);
             w0 = win * a.win_rows;
             rows = min(a.win_rows, g.R - w0);
             const int row_base = g.rho_min + w0;   /* rho bin of local row 0 */
-            lrows = (k0 + lane < a.T) ? (unsigned)rows : 0u;
+            /* every column's dump row is row `rows`; the padding columns
+             * (thetas >= T, cos = sin = 0) vote there or into their own
+             * column, which the store writes as zero */
+            lrows = (unsigned)rows;
             cv = row_base >= 1 ? CV_FLOOR
                                : (row_base + rows - 1 <= -1 ? CV_CEIL : CV_EXACT);
             vbase = cv == CV_EXACT ? row_base : RHO_MAGIC_BITS + row_base;
@@ -656,20 +710,15 @@ hl_vote_kernel(hl_vote_args a)
                               a.status))
                 return;
             seq++;
-            /* this warp's share: points [64 cw, 64 cw + 64), two 32-point
-             * halves */
+            /* this warp's share: points [64 cw, 64 cw + 64) */
             const int m = min(64, total - b * batch - 64 * cw);
             const float2 *pts = sm.raw[slot] + 64 * cw;
-            if (cv == CV_FLOOR) {
-                vote_share<UNIT, CV_FLOOR>(pts, m, c, s, a.irho, vbase, acc_l, lrows);
-                vote_share<UNIT, CV_FLOOR>(pts + 32, m - 32, c, s, a.irho, vbase, acc_l, lrows);
-            } else if (cv == CV_CEIL) {
-                vote_share<UNIT, CV_CEIL>(pts, m, c, s, a.irho, vbase, acc_l, lrows);
-                vote_share<UNIT, CV_CEIL>(pts + 32, m - 32, c, s, a.irho, vbase, acc_l, lrows);
-            } else {
-                vote_share<UNIT, CV_EXACT>(pts, m, c, s, a.irho, vbase, acc_l, lrows);
-                vote_share<UNIT, CV_EXACT>(pts + 32, m - 32, c, s, a.irho, vbase, acc_l, lrows);
-            }
+            if (cv == CV_FLOOR)
+                vote_share<UNIT, CV_FLOOR>(pts, m, tab, ir, vbase, lrows, pl);
+            else if (cv == CV_CEIL)
+                vote_share<UNIT, CV_CEIL>(pts, m, tab, ir, vbase, lrows, pl);
+            else
+                vote_share<UNIT, CV_EXACT>(pts, m, tab, ir, vbase, lrows, pl);
             __syncwarp();
             if (lane == 0)
                 mbar_arrive(&sm.empty[slot]);
@@ -681,9 +730,9 @@ hl_vote_kernel(hl_vote_args a)
          * acc[(w0 + i) * Tp + k0 ..], then clear it for the next item */
         if (!cons_sync(sm, cpar, a.status))
             return;
-        /* a whole block goes to acc (row 0 of the padding columns, thetas
-         * >= T, holds dumped votes and is stored as zero), a part of a
-         * split block to its scratch slot as it is; each thread stores and
+        /* a whole block goes to acc (the padding columns, thetas >= T,
+         * hold dumped votes and are stored as zero), a part of a split
+         * block to its scratch slot as it is; each thread stores and
          * clears the same elements */
         const int tp4 = a.Tp >> 2;
         const int n4 = rows * (HL_SLICE / 4);
@@ -695,7 +744,7 @@ hl_vote_kernel(hl_vote_args a)
                 const int rr = i >> 3, q = i & 7;
                 int4 v = src4[i];
                 if (nparts == 1) {
-                    if (rr == 0) {
+                    if (k0 + 4 * q + 3 >= a.T) {
                         const int kq = k0 + 4 * q;
                         if (kq >= a.T) v.x = 0;
                         if (kq + 1 >= a.T) v.y = 0;
@@ -718,7 +767,7 @@ hl_vote_kernel(hl_vote_args a)
 }
 
 /* The blocks voted in parts: block region = sum of its parts' scratch
- * slots, row 0 of the padding columns (thetas >= T) stored as zero.  A
+ * slots, the padding columns (thetas >= T) stored as zero.  A
  * thread takes 16 bytes of every part of its region (grid.y = region): two
  * output int4 when the parts hold 16-bit counts, one otherwise; every slot
  * is read once, from L2 where the vote launch just wrote it. */
@@ -800,7 +849,7 @@ hl_merge_kernel(hl_merge_args a)
         int4 v = e ? v1 : v0;
         const int oi = o + e;
         const int rr = oi >> 3, q = oi & 7;
-        if (rr == 0) {
+        if (r.k0 + 4 * q + 3 >= a.T) {
             const int kq = r.k0 + 4 * q;
             if (kq >= a.T) v.x = 0;
             if (kq + 1 >= a.T) v.y = 0;
