@@ -417,14 +417,27 @@ def gpu_scenes(L, Image, dev, kind: int, n: int, seed: int):
     return imgs
 
 
-def proposal_workload(L, HoughLine, Image, dev, sp, kind: int, n: int, reps: int):
+def proposal_selection():
+    """The calibrated selection settings saved beside the network weights."""
+    from opencuda_gb300.proposal import WEIGHTS
+    p = WEIGHTS.with_name("proposal_selection.json")
+    return json.loads(p.read_text())
+
+
+def proposal_workload(L, HoughLine, Image, dev, sp, kind: int, n: int, reps: int,
+                      check_counts: bool):
     """Proposal-guided batched HoughLine against the plain batched path on
     the same images: spec 4 = 2048 x 2048 scenes (8-48 segments, 1-4% noise),
-    spec 5 = uneven 512-4096 scenes, 30% cluttered (fall back to plain).
-    Theta step 0.5 deg, threshold 0.15 * max(w, h), top-32.  Both timed with
-    CUDA events around whole batch calls (the proposal call synchronises
-    once to decide its fall-back set); recall = plain top-32 lines the
-    proposal path also reports, over all images."""
+    spec 5 = uneven 512-4096 scenes, 30% cluttered.  Theta step 0.5 deg,
+    threshold 0.15 * max(w, h), top-32.  Two operating points: `calibrated`
+    (local maxima of the coarse heatmap, the 64 best grown by one cell, and
+    the confidence fall-back whose threshold was calibrated on held-out
+    scenes for 99% top-32 recall) and `no_fallback` (the same selection, no
+    fall-back).  Timed with CUDA events around whole batch calls (the
+    proposal call synchronises once to decide its fall-back set); recall =
+    plain top-32 lines the proposal path also reports, over all images.
+    With check_counts, every line the calibrated run reports is checked
+    against the plain accumulator of its image (untimed)."""
     import torch
     from opencuda_gb300.proposal import WEIGHTS, HoughNet, proposal_batch
     K, det = 32, math.pi / 360
@@ -434,24 +447,23 @@ def proposal_workload(L, HoughLine, Image, dev, sp, kind: int, n: int, reps: int
     hl.set_batch_graph(True)
     net = HoughNet()
     net.load(WEIGHTS)
+    sel = proposal_selection()
+    sel = dict(sel, **sel.get("per_spec", {}).get(str(kind), {}))
     _lib = _lib_mod()
     descs = (_lib.hl_image_desc * n)(*[d.desc() for d in imgs])
     th = (C.c_int * n)(*thr)
     lines = torch.empty(n * K * 3, dtype=torch.int32, device=dev)
     counts = torch.zeros(n, dtype=torch.int32, device=dev)
-    opts = dict(p_cut=0.9, max_props=400, dilate_theta=1, dilate_rho=1, top_m=64)
+    base = dict(p_cut=sel["p_cut"], max_props=sel["max_props"], dilate_theta=sel["dilate_theta"],
+                dilate_rho=sel["dilate_rho"], top_m=sel["top_m"], nms=bool(sel["nms"]))
+    points = {"calibrated": dict(base, p_conf=sel["p_conf"]),
+              "no_fallback": dict(base, p_conf=0.0, max_props=90 * 128)}
 
     def plain():
         rc = L.hl_batch_async(hl.handle, descs, n, th, K, C.c_void_p(lines.data_ptr()),
                               C.c_void_p(counts.data_ptr()), sp)
         if rc != 0:
             raise RuntimeError(f"hl_batch_async returned {rc}")
-
-    def prop():
-        rc, _, st = proposal_batch(hl, net, imgs, K, thr, stream=sp, **opts)
-        if rc != 0:
-            raise RuntimeError(f"hl_proposal_batch returned {rc}")
-        return st
 
     def timed(f):
         for _ in range(2):
@@ -468,21 +480,107 @@ def proposal_workload(L, HoughLine, Image, dev, sp, kind: int, n: int, reps: int
             ms.append(e0.elapsed_time(e1))
         return statistics.median(ms)
     t_plain = timed(plain)
-    t_prop = timed(prop)
-    rc, _, st = proposal_batch(hl, net, imgs, K, thr, stream=sp, judge_every=1, **opts)
-    if rc != 0:
-        raise RuntimeError(f"hl_proposal_batch returned {rc}")
-    return {"workload": ("proposal-guided vs plain batched HoughLine: "
-                         + ("2048x2048 scenes, 8-48 segments, 1-4% noise" if kind == 4 else
-                            "uneven 512-4096 scenes, 30% cluttered")
-                         + f", {n} images, T=360, thr 0.15*max(w,h), top-32"),
-            "images": n, "plain_images_per_s": n / (t_plain / 1e3),
-            "proposal_images_per_s": n / (t_prop / 1e3),
-            "speedup": t_plain / t_prop,
-            "recall_top32": st["judged_found"] / max(st["judged_lines"], 1),
-            "fallback_rate": st["fallback"] / n, "windows_per_image": st["windows"] / n,
-            "executed_votes_per_image": st["votes"] / n, "selection": opts,
-            "network": "6 conv3x3 (tcgen05), 32 ch, trained on 64K GPU-generated scenes"}
+    out = {"workload": ("proposal-guided vs plain batched HoughLine: "
+                        + ("2048x2048 scenes, 8-48 segments, 1-4% noise" if kind == 4 else
+                           "uneven 512-4096 scenes, 30% cluttered")
+                        + f", {n} images, T=360, thr 0.15*max(w,h), top-32"),
+           "images": n, "plain_images_per_s": n / (t_plain / 1e3),
+           "network": sel.get("network", ""), "selection": base,
+           "calibration": sel.get("calibration")}
+    for name, opts in points.items():
+        def prop(opts=opts):
+            rc, _, st = proposal_batch(hl, net, imgs, K, thr, stream=sp, **opts)
+            if rc != 0:
+                raise RuntimeError(f"hl_proposal_batch returned {rc}")
+        t_prop = timed(prop)
+        rc, got, st = proposal_batch(hl, net, imgs, K, thr, stream=sp, judge_every=1, **opts)
+        if rc != 0:
+            raise RuntimeError(f"hl_proposal_batch returned {rc}")
+        out[name] = {"p_conf": opts["p_conf"], "images_per_s": n / (t_prop / 1e3),
+                     "speedup_vs_plain": t_plain / t_prop,
+                     "recall_top32": st["judged_found"] / max(st["judged_lines"], 1),
+                     "fallback_rate": st["fallback"] / n,
+                     "fallback_confidence": st["fallback_conf"] / n,
+                     "windows_per_image": st["windows"] / n,
+                     "executed_votes_per_image": st["votes"] / n}
+        if check_counts and name == "calibrated":
+            # every reported line is a peak bin of the plain accumulator with
+            # its exact count (the reference decode reports negative rho
+            # bins one higher, so d <= 0 may stand for bin d or d - 1)
+            bad = checked = 0
+            for i, im in enumerate(imgs):
+                if not got[i]:
+                    continue
+                acc, rho_min = hl.accumulator(im)
+                R = acc.shape[0]
+                ks = [int(round(ln.angle / det)) for ln in got[i]]
+                r0 = [min(max(ln.distance - rho_min, 0), R - 1) for ln in got[i]]
+                r1 = [min(max(ln.distance - 1 - rho_min, 0), R - 1) for ln in got[i]]
+                kt = torch.tensor(ks, device=dev)
+                v0 = acc[torch.tensor(r0, device=dev), kt].tolist()
+                v1 = acc[torch.tensor(r1, device=dev), kt].tolist()
+                for q, ln in enumerate(got[i]):
+                    ok = (0 <= ln.distance - rho_min < R and v0[q] == ln.votes) or \
+                         (ln.distance <= 0 and 0 <= ln.distance - 1 - rho_min < R and
+                          v1[q] == ln.votes)
+                    bad += not ok
+                    checked += 1
+                del acc
+            out[name]["exact_counts"] = {"lines_checked": checked, "mismatches": bad,
+                                         "images": n}
+    return out
+
+
+def proposal_single_image(L, HoughLine, Image, dev, sp, reps: int):
+    """The single-image learned-proposal configuration: one 2048 x 2048 scene
+    (8-48 segments, 1-4% noise).  Device time (CUDA events) of the network
+    forward alone (occupancy map in HBM) and wall time of one synchronous
+    proposal-guided call (calibrated selection) against hl_plain on the same
+    image."""
+    import torch
+    from opencuda_gb300.proposal import WEIGHTS, HoughNet, proposal_batch
+    K, det = 32, math.pi / 360
+    img = gpu_scenes(L, Image, dev, 4, 1, 4325)
+    thr = [int(0.15 * max(img[0].width, img[0].height))]
+    hl = HoughLine(detheta=det)
+    net = HoughNet()
+    net.load(WEIGHTS)
+    sel = proposal_selection()
+    sel = dict(sel, **sel.get("per_spec", {}).get("4", {}))
+    opts = dict(p_cut=sel["p_cut"], max_props=sel["max_props"], dilate_theta=sel["dilate_theta"],
+                dilate_rho=sel["dilate_rho"], top_m=sel["top_m"], nms=bool(sel["nms"]),
+                p_conf=sel["p_conf"])
+    occ, geo = net.occupancy(hl, img)
+    fs = torch.cuda.Stream(dev)
+    for _ in range(5):
+        net.forward(occ, geo, stream=fs)
+    torch.cuda.synchronize(dev)
+    ms = []
+    for _ in range(reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(fs)
+        net.forward(occ, geo, stream=fs)
+        e1.record(fs)
+        fs.synchronize()
+        ms.append(e0.elapsed_time(e1))
+
+    def wall(f):
+        for _ in range(5):
+            f()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            f()
+        return (time.perf_counter() - t0) / reps * 1e6
+    hl.setThreshold(thr[0])
+    plain_us = wall(lambda: hl.houghLine(img[0], None, K))
+    prop_us = wall(lambda: proposal_batch(hl, net, img, K, thr, stream=sp, **opts))
+    rc, _, st = proposal_batch(hl, net, img, K, thr, stream=sp, **opts)
+    return {"workload": "learned proposal, one 2048x2048 scene (8-48 segments, 1-4% noise), "
+                        "T=360, top-32", "network_forward_us": statistics.median(ms) * 1e3,
+            "proposal_call_us": prop_us, "hl_plain_us": plain_us,
+            "fell_back": bool(st.get("fallback", 0)), "calls": reps,
+            "timing": "network: CUDA events, device time; calls: host wall time, synchronous"}
 
 
 def circle_workload(L, Image, dev, sp, atom_peak: float, reps: int, cpu: bool):
@@ -827,8 +925,9 @@ def run_gb300(args):
         line["batched"] = batched_workload(L, HoughLine, Image, dev, sp, min(max(args.steps, 5), 50),
                                            atom.value, ws == 1 and not args.no_cpu_baseline)
     if not args.no_batch and not args.no_proposal:
-        line["proposal"] = [proposal_workload(L, HoughLine, Image, dev, sp, 4, 128, 5),
-                            proposal_workload(L, HoughLine, Image, dev, sp, 5, 1024, 3)]
+        line["proposal"] = [proposal_workload(L, HoughLine, Image, dev, sp, 4, 128, 5, False),
+                            proposal_workload(L, HoughLine, Image, dev, sp, 5, 1024, 3, True)]
+        line["proposal_single"] = proposal_single_image(L, HoughLine, Image, dev, sp, 50)
     if not args.no_circle:
         line["circle"] = circle_workload(L, Image, dev, sp, atom.value,
                                          min(max(args.steps, 5), 50),

@@ -86,22 +86,28 @@ int hl_occupancy(hl_handle *h, const hl_image_desc *imgs, int nimg,
 /* ---- proposal-guided batched HoughLine ------------------------------------
  * hl_batch's contract (DEVICE images, per-image thresholds, linesmax lines
  * per image into DEVICE arrays), but the exact vote runs only in the coarse
- * cells the network scores above p_cut (grown by dilate_theta / dilate_rho
- * cells; with top_m > 0 also in the image's top_m cells whatever their
- * score): every reported line is a peak of the full accumulator with its
- * exact vote count; lines the proposals miss are absent.  An image with more
- * than max_props cells above the cutoff (a cluttered scene), or too large
- * for the window kernel, runs the full plain method instead.  Every
- * judge_every-th other image (0: none) also runs the plain method and the
- * stats report how many of its lines the proposal path found.  Synchronises
- * `stream` (the fall-back set is decided on the host). */
+ * cells the network selects: the candidates (every cell, or with nms the
+ * local maxima of the logits over 3 x 3 cells) scored above p_cut, and with
+ * top_m > 0 also the image's top_m candidates whatever their score, each
+ * grown by dilate_theta / dilate_rho cells.  Every reported line is a peak of
+ * the full accumulator with its exact vote count; lines the proposals miss
+ * are absent.  An image runs the full plain method instead when the network
+ * is not confident its budget covers the lines: more than max_props
+ * candidates above p_cut (a cluttered scene), or, with 0 < p_conf < 1, the
+ * best candidate left out of the top_m scored above p_conf; an image too
+ * large for the window kernel falls back too.  Every judge_every-th other
+ * image (0: none) also runs the plain method and the stats report how many
+ * of its lines the proposal path found.  Synchronises `stream` (the
+ * fall-back set is decided on the host). */
 typedef struct hl_proposal_opts {
     float p_cut;
     int max_props;
     int dilate_theta;
     int dilate_rho;
     int judge_every;
-    int top_m;          /* also vote each image's top_m cells (0: none) */
+    int top_m;          /* also vote each image's top_m candidates (0: none) */
+    int nms;            /* candidates are the local maxima of the logits */
+    float p_conf;       /* confidence fall-back threshold (0: off) */
 } hl_proposal_opts;
 
 typedef struct hl_proposal_stats {
@@ -110,7 +116,7 @@ typedef struct hl_proposal_stats {
     int judged;          /* images also run through the plain method */
     int judged_lines;    /* lines the plain method gave them */
     int judged_found;    /* of those, reported by the proposal path */
-    int pad;
+    int fallback_conf;   /* of the fall-backs, decided by the confidence test */
     long long votes;     /* executed votes of the windows */
 } hl_proposal_stats;
 

@@ -80,13 +80,14 @@ class hl_coarse_geom(C.Structure):
 
 class hl_proposal_opts(C.Structure):
     _fields_ = [("p_cut", C.c_float), ("max_props", C.c_int), ("dilate_theta", C.c_int),
-                ("dilate_rho", C.c_int), ("judge_every", C.c_int), ("top_m", C.c_int)]
+                ("dilate_rho", C.c_int), ("judge_every", C.c_int), ("top_m", C.c_int),
+                ("nms", C.c_int), ("p_conf", C.c_float)]
 
 
 class hl_proposal_stats(C.Structure):
     _fields_ = [("fallback", C.c_int), ("windows", C.c_int), ("judged", C.c_int),
-                ("judged_lines", C.c_int), ("judged_found", C.c_int), ("pad", C.c_int),
-                ("votes", C.c_longlong)]
+                ("judged_lines", C.c_int), ("judged_found", C.c_int),
+                ("fallback_conf", C.c_int), ("votes", C.c_longlong)]
 
 
 class hl_tune_entry(C.Structure):

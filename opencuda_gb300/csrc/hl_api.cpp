@@ -2153,7 +2153,8 @@ extern "C" int hl_proposal_batch(hl_handle *h, hl_net *net,
         return HL_NULL_POINTER;
     if (nimg <= 0 || nimg > 0xffff || !(opts->p_cut > 0.0f && opts->p_cut < 1.0f) ||
         opts->max_props < 0 || opts->dilate_rho < 0 || opts->dilate_theta < 0 ||
-        opts->judge_every < 0 || opts->top_m < 0 || opts->top_m > 1024)
+        opts->judge_every < 0 || opts->top_m < 0 || opts->top_m > 1024 ||
+        !(opts->p_conf >= 0.0f && opts->p_conf < 1.0f))
         return HL_INVALID_DATA;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     const int K = std::max(linesmax, 0);
@@ -2252,6 +2253,9 @@ extern "C" int hl_proposal_batch(hl_handle *h, hl_net *net,
     sa.dil_t = opts->dilate_theta;
     sa.dil_r = opts->dilate_rho;
     sa.force_fallback = 0;
+    sa.nms = opts->nms ? 1 : 0;
+    sa.use_conf = opts->p_conf > 0.0f ? 1 : 0;
+    sa.zconf = sa.use_conf ? logf(opts->p_conf / (1.0f - opts->p_conf)) : 0.0f;
     sa.fallback = pw->d_fb;
     sa.win = pw->d_win;
     sa.nwin = pw->d_cnt + 0;
@@ -2295,7 +2299,9 @@ extern "C" int hl_proposal_batch(hl_handle *h, hl_net *net,
             sub_fb.push_back(fb ? 1 : 0);
         }
     }
-    int n_fb = 0, judged = 0, jl = 0, jf = 0;
+    int n_fb = 0, judged = 0, jl = 0, jf = 0, n_conf = 0;
+    for (int i = 0; i < nimg; i++)
+        n_conf += pw->h_fb[i] == 2;
     if (!sub.empty()) {
         const int ns = (int)sub.size();
         std::vector<hl_image_desc> sd((size_t)ns);
@@ -2383,6 +2389,7 @@ extern "C" int hl_proposal_batch(hl_handle *h, hl_net *net,
         stats->judged = judged;
         stats->judged_lines = jl;
         stats->judged_found = jf;
+        stats->fallback_conf = n_conf;
         unsigned long long v = 0;
         memcpy(&v, &st_host[2], sizeof(v));
         stats->votes = (long long)v;

@@ -577,19 +577,22 @@ __device__ __forceinline__ int head_bin(const hl_head_geom &g, int qy, int qx,
 }
 
 /* logits[b][t][r] = alpha * sum_{cells with bin r at angle t} e[b][cell] + beta
- * One CTA per image, the [T][R] sums in shared memory. */
-__global__ void __launch_bounds__(512)
+ * One CTA per (image, group of HEAD_TG angles): the group's [HEAD_TG][R] sums
+ * in shared memory, every evidence cell added to each angle's bin. */
+#define HEAD_TG 6
+__global__ void __launch_bounds__(256)
 hl_head_fwd_kernel(const float *e, int ev, const hl_head_geom *geo,
                    const float *ab, float *hsum, float *logits, HeadTrig tr)
 {
-    __shared__ float sh[HL_HEAD_T * HL_HEAD_R];
-    __shared__ float cs[HL_HEAD_T], sn[HL_HEAD_T];
-    const int b = blockIdx.x;
-    for (int i = threadIdx.x; i < HL_HEAD_T * HL_HEAD_R; i += blockDim.x)
+    __shared__ float sh[HEAD_TG * HL_HEAD_R];
+    __shared__ float cs[HEAD_TG], sn[HEAD_TG];
+    const int b = blockIdx.y, t0 = blockIdx.x * HEAD_TG;
+    const int nt = min(HEAD_TG, HL_HEAD_T - t0);
+    for (int i = threadIdx.x; i < HEAD_TG * HL_HEAD_R; i += blockDim.x)
         sh[i] = 0.0f;
-    if (threadIdx.x < HL_HEAD_T) {
-        cs[threadIdx.x] = tr.c[threadIdx.x];
-        sn[threadIdx.x] = tr.s[threadIdx.x];
+    if (threadIdx.x < nt) {
+        cs[threadIdx.x] = tr.c[t0 + threadIdx.x];
+        sn[threadIdx.x] = tr.s[t0 + threadIdx.x];
     }
     __syncthreads();
     const hl_head_geom g = geo[b];
@@ -601,26 +604,28 @@ hl_head_fwd_kernel(const float *e, int ev, const hl_head_geom *geo,
         const float v = eb[qy * ev + qx];
         if (v == 0.0f)
             continue;
-        for (int t = 0; t < HL_HEAD_T; t++)
+        for (int t = 0; t < nt; t++)
             atomicAdd(&sh[t * HL_HEAD_R + head_bin(g, qy, qx, cs[t], sn[t])], v);
     }
     __syncthreads();
     const float alpha = ab[0], beta = ab[1];
-    for (int i = threadIdx.x; i < HL_HEAD_T * HL_HEAD_R; i += blockDim.x) {
-        hsum[(size_t)b * HL_HEAD_T * HL_HEAD_R + i] = sh[i];
-        logits[(size_t)b * HL_HEAD_T * HL_HEAD_R + i] = alpha * sh[i] + beta;
+    for (int i = threadIdx.x; i < nt * HL_HEAD_R; i += blockDim.x) {
+        const size_t o = (size_t)b * HL_HEAD_T * HL_HEAD_R + (size_t)t0 * HL_HEAD_R + i;
+        hsum[o] = sh[i];
+        logits[o] = alpha * sh[i] + beta;
     }
 }
 
 /* de[b][cell] = alpha * sum_t dz[b][t][bin(cell, t)] (the gather transpose of
- * the head); one CTA per image */
+ * the head); one CTA per (image, 512 cells), each thread one cell summing its
+ * angles in order */
 __global__ void __launch_bounds__(512)
 hl_head_bwd_kernel(const float *dz, int ev, const hl_head_geom *geo,
                    const float *ab, float *de, HeadTrig tr)
 {
     __shared__ float sd[HL_HEAD_T * HL_HEAD_R];
     __shared__ float cs[HL_HEAD_T], sn[HL_HEAD_T];
-    const int b = blockIdx.x;
+    const int b = blockIdx.y;
     for (int i = threadIdx.x; i < HL_HEAD_T * HL_HEAD_R; i += blockDim.x)
         sd[i] = dz[(size_t)b * HL_HEAD_T * HL_HEAD_R + i];
     if (threadIdx.x < HL_HEAD_T) {
@@ -630,7 +635,8 @@ hl_head_bwd_kernel(const float *dz, int ev, const hl_head_geom *geo,
     __syncthreads();
     const hl_head_geom g = geo[b];
     const float alpha = ab[0];
-    for (int p = threadIdx.x; p < ev * ev; p += blockDim.x) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < ev * ev;
+         p += gridDim.x * blockDim.x) {
         const int qy = p / ev, qx = p % ev;
         float acc = 0.0f;
         if (qy < g.qh && qx < g.qw)
@@ -644,14 +650,16 @@ cudaError_t hl_launch_head_fwd(const float *e, int ev, const hl_head_geom *geo,
                                int nimg, const float *ab, float *hsum,
                                float *logits, cudaStream_t s)
 {
-    hl_head_fwd_kernel<<<nimg, 512, 0, s>>>(e, ev, geo, ab, hsum, logits, head_trig());
+    hl_head_fwd_kernel<<<dim3((HL_HEAD_T + HEAD_TG - 1) / HEAD_TG, nimg), 256, 0, s>>>(
+        e, ev, geo, ab, hsum, logits, head_trig());
     return cudaGetLastError();
 }
 
 cudaError_t hl_launch_head_bwd(const float *dz, int ev, const hl_head_geom *geo,
                                int nimg, const float *ab, float *de, cudaStream_t s)
 {
-    hl_head_bwd_kernel<<<nimg, 512, 0, s>>>(dz, ev, geo, ab, de, head_trig());
+    hl_head_bwd_kernel<<<dim3((unsigned)((ev * ev + 511) / 512), nimg), 512, 0, s>>>(
+        dz, ev, geo, ab, de, head_trig());
     return cudaGetLastError();
 }
 

@@ -2,9 +2,10 @@
  * hl_window.cu -- the exact vote of the proposal-guided path.
  *
  * hl_select_kernel: one CTA per image reads the network's 90 x 128 logits,
- * keeps the cells above the cutoff (too many: the image falls back to the
- * full method), grows them by the dilation and appends one window per kept
- * cell.
+ * keeps the candidates (local maxima, or every cell) above the cutoff and
+ * the image's best top_m, falls back to the full method when the network
+ * sees more likely lines than that (count and confidence tests), grows the
+ * kept cells by the dilation and appends one window per cell.
  *
  * hl_window_vote_kernel: one CTA per window.  A coarse cell (t, r) owns the
  * fine thetas k with floor(90 k / T) = t and the rho rows j with
@@ -23,74 +24,131 @@
 
 #define FULL 0xffffffffu
 
+#define NCELL (HL_COARSE_T * HL_COARSE_R)
+
+/* Is coarse cell i a local maximum of the logits (3 x 3 neighbourhood, ties
+ * to the earlier cell in raster order)? */
+__device__ __forceinline__ bool local_max(const float *z, int i)
+{
+    const int t = i / HL_COARSE_R, r = i % HL_COARSE_R;
+    const float v = z[i];
+    for (int dt = -1; dt <= 1; dt++) {
+        const int tt = t + dt;
+        if (tt < 0 || tt >= HL_COARSE_T)
+            continue;
+        for (int dr = -1; dr <= 1; dr++) {
+            const int rr = r + dr;
+            if ((dt == 0 && dr == 0) || rr < 0 || rr >= HL_COARSE_R)
+                continue;
+            const int j = tt * HL_COARSE_R + rr;
+            const float u = z[j];
+            if (u > v || (u == v && j < i))
+                return false;
+        }
+    }
+    return true;
+}
+
+/* Value level with at least `target` of the n candidate values cv above it
+ * (bisection on the value; the block's threads count in parallel).  Returns
+ * -inf when there are at most `target` candidates. */
+__device__ float level_for(const float *cv, int n, int target, float *red, int *s_cnt)
+{
+    if (n <= target)
+        return -3.0e38f;
+    float mn = 3.0e38f, mx = -3.0e38f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        mn = fminf(mn, cv[i]);
+        mx = fmaxf(mx, cv[i]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = fminf(mn, __shfl_xor_sync(FULL, mn, o));
+        mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, o));
+    }
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) {
+        red[threadIdx.x >> 5] = mn;
+        red[16 + (threadIdx.x >> 5)] = mx;
+    }
+    __syncthreads();
+    float lo = red[0], hi = red[16];
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+        lo = fminf(lo, red[w]);
+        hi = fmaxf(hi, red[16 + w]);
+    }
+    lo -= 1.0f;   /* count(cv > lo) = n >= target */
+    for (int it = 0; it < 24; it++) {
+        const float mid = 0.5f * (lo + hi);
+        __syncthreads();
+        if (threadIdx.x == 0)
+            *s_cnt = 0;
+        __syncthreads();
+        int c = 0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x)
+            c += cv[i] > mid;
+        atomicAdd(s_cnt, c);
+        __syncthreads();
+        if (*s_cnt >= target)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+/* One CTA per image.  Candidates are the coarse cells (with nms: the local
+ * maxima of the logits); selected are the candidates above the cutoff and
+ * the image's top_m candidates, each grown by the dilation into windows.
+ * The image falls back to the plain method when more than max_props
+ * candidates clear the cutoff (a cluttered scene), or -- the confidence
+ * test -- when the best candidate left out of the top_m is itself above
+ * zconf: the network sees more likely lines than the budget covers. */
 __global__ void __launch_bounds__(512)
 hl_select_kernel(hl_select_args a)
 {
-    __shared__ unsigned mark[HL_COARSE_T * HL_COARSE_R / 32];
-    __shared__ int cnt;
+    extern __shared__ float zs[];          /* [NCELL] logits, [NCELL] candidate values */
+    float *cv = zs + NCELL;
+    __shared__ unsigned mark[NCELL / 32];
+    __shared__ int cnt, ncand, s_cnt;
+    __shared__ float red[32];
     const int b = blockIdx.x;
-    const float *z = a.logits + (size_t)b * HL_COARSE_T * HL_COARSE_R;
-    for (int i = threadIdx.x; i < HL_COARSE_T * HL_COARSE_R / 32; i += blockDim.x)
+    const float *z = a.logits + (size_t)b * NCELL;
+    for (int i = threadIdx.x; i < NCELL; i += blockDim.x)
+        zs[i] = z[i];
+    for (int i = threadIdx.x; i < NCELL / 32; i += blockDim.x)
         mark[i] = 0u;
-    if (threadIdx.x == 0)
+    if (threadIdx.x == 0) {
         cnt = 0;
+        ncand = 0;
+    }
     __syncthreads();
     int mine = 0;
-    for (int i = threadIdx.x; i < HL_COARSE_T * HL_COARSE_R; i += blockDim.x)
-        mine += z[i] > a.zcut;
+    for (int i = threadIdx.x; i < NCELL; i += blockDim.x) {
+        if (a.nms && !local_max(zs, i))
+            continue;
+        cv[atomicAdd(&ncand, 1)] = zs[i];
+        mine += zs[i] > a.zcut;
+    }
     atomicAdd(&cnt, mine);
     __syncthreads();
-    const bool fallback = cnt > a.max_props || a.force_fallback;
-    if (threadIdx.x == 0)
-        a.fallback[b] = fallback ? 1 : 0;
-    if (fallback)
-        return;
-    /* selection level: the cutoff, lowered to about the image's top_m-th
-     * logit (bisection on the value keeps count(z > lo) >= top_m) */
+    const int nc = ncand;
+    int fb = (cnt > a.max_props || a.force_fallback) ? 1 : 0;
     float level = a.zcut;
-    if (a.top_m > 0) {
-        __shared__ float red[2][16];
-        __shared__ int s_cnt;
-        float mn = 3.0e38f, mx = -3.0e38f;
-        for (int i = threadIdx.x; i < HL_COARSE_T * HL_COARSE_R; i += blockDim.x) {
-            mn = fminf(mn, z[i]);
-            mx = fmaxf(mx, z[i]);
+    if (!fb && a.top_m > 0) {
+        level = fminf(level, level_for(cv, nc, a.top_m, red, &s_cnt));
+        if (a.use_conf && nc > a.top_m) {
+            /* the (top_m + 1)-th candidate lies above this level */
+            const float next = level_for(cv, nc, a.top_m + 1, red, &s_cnt);
+            if (next >= a.zconf)
+                fb = 2;
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            mn = fminf(mn, __shfl_xor_sync(FULL, mn, o));
-            mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, o));
-        }
-        if ((threadIdx.x & 31) == 0) {
-            red[0][threadIdx.x >> 5] = mn;
-            red[1][threadIdx.x >> 5] = mx;
-        }
-        __syncthreads();
-        float lo = red[0][0], hi = red[1][0];
-        for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
-            lo = fminf(lo, red[0][w]);
-            hi = fmaxf(hi, red[1][w]);
-        }
-        lo -= 1.0f;   /* count(z > lo) = all cells >= top_m */
-        for (int it = 0; it < 24; it++) {
-            const float mid = 0.5f * (lo + hi);
-            __syncthreads();
-            if (threadIdx.x == 0)
-                s_cnt = 0;
-            __syncthreads();
-            int c = 0;
-            for (int i = threadIdx.x; i < HL_COARSE_T * HL_COARSE_R; i += blockDim.x)
-                c += z[i] > mid;
-            atomicAdd(&s_cnt, c);
-            __syncthreads();
-            if (s_cnt >= a.top_m)
-                lo = mid;
-            else
-                hi = mid;
-        }
-        level = fminf(level, lo);
     }
-    for (int i = threadIdx.x; i < HL_COARSE_T * HL_COARSE_R; i += blockDim.x) {
-        if (!(z[i] > level))
+    if (threadIdx.x == 0)
+        a.fallback[b] = fb;
+    if (fb)
+        return;
+    for (int i = threadIdx.x; i < NCELL; i += blockDim.x) {
+        if (!(zs[i] > level) || (a.nms && !local_max(zs, i)))
             continue;
         const int t = i / HL_COARSE_R, r = i % HL_COARSE_R;
         for (int dt = -a.dil_t; dt <= a.dil_t; dt++) {
@@ -107,7 +165,7 @@ hl_select_kernel(hl_select_args a)
         }
     }
     __syncthreads();
-    for (int wd = threadIdx.x; wd < HL_COARSE_T * HL_COARSE_R / 32; wd += blockDim.x) {
+    for (int wd = threadIdx.x; wd < NCELL / 32; wd += blockDim.x) {
         unsigned m = mark[wd];
         if (!m)
             continue;
@@ -129,7 +187,12 @@ hl_select_kernel(hl_select_args a)
 
 cudaError_t hl_launch_select(const hl_select_args *a, int nimg, cudaStream_t s)
 {
-    hl_select_kernel<<<nimg, 512, 0, s>>>(*a);
+    const int smem = (int)(2 * NCELL * sizeof(float));
+    cudaError_t e = cudaFuncSetAttribute(hl_select_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess)
+        return e;
+    hl_select_kernel<<<nimg, 512, smem, s>>>(*a);
     return cudaGetLastError();
 }
 

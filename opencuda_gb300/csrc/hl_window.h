@@ -16,11 +16,14 @@
 typedef struct hl_select_args {
     const float *logits;   /* [nimg][90][128] */
     float zcut;            /* logit of the probability cutoff */
-    int max_props;         /* more cells above the cutoff: fall back */
-    int top_m;             /* also take each image's top_m cells (0: none) */
+    int max_props;         /* more candidates above the cutoff: fall back */
+    int top_m;             /* also take each image's top_m candidates (0: none) */
     int dil_t, dil_r;      /* window dilation in coarse cells */
     int force_fallback;
-    int *fallback;         /* out [nimg] */
+    int nms;               /* candidates: local maxima of the logits (else every cell) */
+    int use_conf;          /* confidence test on (zconf) */
+    float zconf;           /* fall back when the best unselected candidate is above */
+    int *fallback;         /* out [nimg]: 0, 1 (count test) or 2 (confidence test) */
     int4 *win;             /* out: {image, t, r, 0} */
     int *nwin;             /* window counter (zeroed before) */
     int cap;

@@ -76,11 +76,16 @@ class HoughNet:
         return occ, geo
 
     def forward(self, occ, geo, stream=None):
+        """Logits [B, 90, 128] on `stream` (a torch stream, a raw handle, or
+        None for the current torch stream)."""
         import torch
         B = int(occ.shape[0])
         out = torch.empty((B, HEAD_T, HEAD_R), dtype=torch.float32, device=occ.device)
+        if stream is None:
+            stream = torch.cuda.current_stream(occ.device)
+        sp = C.c_void_p(getattr(stream, "cuda_stream", stream))
         _lib.check(self._L.hl_net_forward(self._n, C.c_void_p(occ.data_ptr()), geo, B,
-                                          C.c_void_p(out.data_ptr()), None), "hl_net_forward")
+                                          C.c_void_p(out.data_ptr()), sp), "hl_net_forward")
         return out
 
     def train_step(self, occ, geo, target, lr: float, pos_weight: float) -> float:
@@ -118,7 +123,7 @@ def line_targets(lines_per_image, geo) -> np.ndarray:
 def proposal_batch(hl, net: HoughNet, images, linesmax: int, thresholds=None,
                    p_cut: float = 0.5, max_props: int = 96, dilate_theta: int = 0,
                    dilate_rho: int = 1, judge_every: int = 0, top_m: int = 0,
-                   stream=None):
+                   nms: bool = False, p_conf: float = 0.0, stream=None):
     """hl_proposal_batch over a list of device Images: (rc, [[LineParam]],
     stats dict)."""
     import torch
@@ -132,7 +137,7 @@ def proposal_batch(hl, net: HoughNet, images, linesmax: int, thresholds=None,
     if thresholds is not None:
         thr = (C.c_int * n)(*[int(t) for t in thresholds])
     opts = _lib.hl_proposal_opts(p_cut, max_props, dilate_theta, dilate_rho, judge_every,
-                                 top_m)
+                                 top_m, 1 if nms else 0, p_conf)
     st = _lib.hl_proposal_stats()
     L = _lib.load()
     rc = L.hl_proposal_batch(hl.handle, net.handle, descs, n, thr, linesmax, C.byref(opts),
@@ -150,5 +155,5 @@ def proposal_batch(hl, net: HoughNet, images, linesmax: int, thresholds=None,
             out.append(LineParam(a, int(raw[i, j, 1]), int(raw[i, j, 2])))
         res.append(out)
     stats = {k: getattr(st, k) for k in ("fallback", "windows", "judged", "judged_lines",
-                                         "judged_found", "votes")}
+                                         "judged_found", "fallback_conf", "votes")}
     return rc, res, stats

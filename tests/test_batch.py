@@ -69,6 +69,33 @@ def test_batch_matches_oracle_and_plain(hl_mod):
         assert [l.astuple() for l in single] == want, i
 
 
+def test_full_benchmark_batch_matches_plain(hl_mod):
+    """The whole benchmarked batch (all 256 uneven images of the batched
+    workload, theta step 0.5 deg, threshold 0.15 * max(w, h), top-32) through
+    one hl_batch call with graph replay and the autotuned vote shape: every
+    image's lines equal hl_plain on that image alone, and every 16th image's
+    equal the oracle's."""
+    HoughLine, Image = hl_mod
+    n = 256
+    imgs = [cases.synth(3, 1234, i) for i in range(n)]
+    thr = [int(0.15 * max(im.shape)) for im in imgs]
+    dev = [Image.from_host(im) for im in imgs]
+    hl = HoughLine(detheta=DEG05)
+    hl.autotune(dev, 32, thr)
+    hl.set_batch_graph(True)
+    for _ in range(2):          # the second call replays the captured graph
+        rc, res = hl.houghLineBatch(dev, 32, thr)
+        assert rc == 0 and len(res) == n
+    ref = HoughLine(detheta=DEG05)
+    for i in range(n):
+        ref.setThreshold(thr[i])
+        rc, single = ref.houghLine(dev[i], None, 32)
+        assert rc == 0
+        assert [l.astuple() for l in res[i]] == [l.astuple() for l in single], i
+    for i in range(0, n, 16):
+        assert [l.astuple() for l in res[i]] == _oracle(ref, imgs[i], None, thr[i], 32), i
+
+
 def test_batch_default_threshold_and_small_k(hl_mod):
     HoughLine, Image = hl_mod
     imgs, rois = _batch_images(3, seed=99)

@@ -81,3 +81,83 @@ def test_reported_lines_carry_exact_votes(env):
             # the reference decode reports negative rho bins one higher
             cand = [ln.distance - rho_min, ln.distance - 1 - rho_min]
             assert any(0 <= j < a.shape[0] and a[j, k] == ln.votes for j in cand), (i, ln)
+
+
+def _scenes(kind, n, seed):
+    """n seeded scenes of workload spec `kind` generated on the GPU."""
+    import ctypes as C
+    import torch
+    from opencuda_gb300 import _lib
+    from opencuda_gb300.houghline import Image
+    L = _lib.load()
+    ps = (_lib.hl_scene_params * n)()
+    assert L.hl_synth_spec(kind, seed, n, ps) == 0
+    imgs, descs = [], (_lib.hl_image_desc * n)()
+    for i in range(n):
+        w, h = ps[i].width, ps[i].height
+        pitch = (w + 511) // 512 * 512
+        buf = torch.empty((h, pitch), dtype=torch.uint8, device="cuda")
+        descs[i] = _lib.hl_image_desc(buf.data_ptr(), pitch, w, h, 0, 0, w, h)
+        im = Image(buf[:, :w])
+        im._buf = buf
+        imgs.append(im)
+    assert L.hl_synth_scenes_device(ps, n, descs, None) == 0
+    return imgs, [ps[i] for i in range(n)]
+
+
+def _recall(plain, prop):
+    found = sum(l.astuple() in {q.astuple() for q in b} for a, b in zip(plain, prop) for l in a)
+    return found / max(sum(len(a) for a in plain), 1)
+
+
+def test_trained_network_gains_over_untrained(env):
+    """The ablation: the same selection (the 32 best local maxima of the
+    coarse heatmap, grown by one cell, no fall-back) with the trained
+    network's logits and with an untrained network's, on 2048 x 2048 scenes.
+    The trained network must find far more of the plain method's top-32
+    lines for about the same number of windows (the same executed-vote
+    budget)."""
+    HoughLine, Image, HoughNet, proposal_batch = env
+    from opencuda_gb300.proposal import WEIGHTS
+    imgs, _ = _scenes(4, 32, 4242)
+    thr = [int(0.15 * max(im.width, im.height)) for im in imgs]
+    hl = HoughLine(detheta=DEG05)
+    rc, plain = hl.houghLineBatch(imgs, 32, thr)
+    assert rc == 0
+    res = {}
+    for name in ("trained", "untrained"):
+        net = HoughNet(seed=11)
+        if name == "trained":
+            net.load(WEIGHTS)
+        rc, got, st = proposal_batch(hl, net, imgs, 32, thr, p_cut=0.999, max_props=11520,
+                                     dilate_theta=1, dilate_rho=1, top_m=32, nms=True)
+        assert rc == 0 and st["fallback"] == 0
+        res[name] = (_recall(plain, got), st["windows"], st["votes"])
+    (rt, wt, vt), (ru, wu, vu) = res["trained"], res["untrained"]
+    print(f"\nablation: trained recall {rt:.3f} ({wt} windows, {vt} votes), "
+          f"untrained {ru:.3f} ({wu} windows, {vu} votes)")
+    assert rt > ru + 0.25
+    assert wt <= 1.3 * wu
+
+
+def test_confidence_fallback_on_cluttered_scenes(env):
+    """Cluttered scenes (64-128 segments, Bezier curves, 8% noise) hold more
+    likely lines than a small budget covers: the confidence test sends them
+    to the plain method, whose results they then carry."""
+    HoughLine, Image, HoughNet, proposal_batch = env
+    from opencuda_gb300.proposal import WEIGHTS
+    imgs, ps = _scenes(5, 40, 515)
+    clutter = [i for i, p in enumerate(ps) if p.nbezier > 0][:4]
+    assert clutter, "the spec draws cluttered scenes"
+    sub = [imgs[i] for i in clutter]
+    thr = [int(0.15 * max(im.width, im.height)) for im in sub]
+    hl = HoughLine(detheta=DEG05)
+    rc, plain = hl.houghLineBatch(sub, 32, thr)
+    assert rc == 0
+    net = HoughNet()
+    net.load(WEIGHTS)
+    rc, got, st = proposal_batch(hl, net, sub, 32, thr, p_cut=0.999, max_props=11520,
+                                 dilate_theta=1, dilate_rho=1, top_m=8, nms=True, p_conf=0.5)
+    assert rc == 0
+    assert st["fallback_conf"] == len(sub) == st["fallback"]
+    assert [[l.astuple() for l in r] for r in got] == [[l.astuple() for l in r] for r in plain]
