@@ -577,19 +577,26 @@ __device__ __forceinline__ int head_bin(const hl_head_geom &g, int qy, int qx,
 }
 
 /* logits[b][t][r] = alpha * sum_{cells with bin r at angle t} e[b][cell] + beta
- * One CTA per (image, group of HEAD_TG angles): the group's [HEAD_TG][R] sums
- * in shared memory, every evidence cell added to each angle's bin. */
+ * One CTA per (image, group of HEAD_TG angles), the group's [HEAD_TG][R] sums
+ * in shared memory.  A thread walks one line of evidence cells for one angle
+ * -- a column when the angle's rho changes less along y (|sin| < |cos|), else
+ * a row -- keeping a running sum while consecutive cells fall in one bin and
+ * adding it to that bin when the bin changes: the cells of a line mostly
+ * share bins, so this issues a few shared reductions per line instead of one
+ * per cell.  The sums are 64-bit fixed point (2^-24 units), so they do not
+ * depend on the order of the additions. */
 #define HEAD_TG 6
-__global__ void __launch_bounds__(256)
+#define HEAD_FIX 16777216.0f
+__global__ void __launch_bounds__(384)
 hl_head_fwd_kernel(const float *e, int ev, const hl_head_geom *geo,
                    const float *ab, float *hsum, float *logits, HeadTrig tr)
 {
-    __shared__ float sh[HEAD_TG * HL_HEAD_R];
+    __shared__ unsigned long long sh[HEAD_TG * HL_HEAD_R];
     __shared__ float cs[HEAD_TG], sn[HEAD_TG];
     const int b = blockIdx.y, t0 = blockIdx.x * HEAD_TG;
     const int nt = min(HEAD_TG, HL_HEAD_T - t0);
     for (int i = threadIdx.x; i < HEAD_TG * HL_HEAD_R; i += blockDim.x)
-        sh[i] = 0.0f;
+        sh[i] = 0ull;
     if (threadIdx.x < nt) {
         cs[threadIdx.x] = tr.c[t0 + threadIdx.x];
         sn[threadIdx.x] = tr.s[t0 + threadIdx.x];
@@ -597,22 +604,38 @@ hl_head_fwd_kernel(const float *e, int ev, const hl_head_geom *geo,
     __syncthreads();
     const hl_head_geom g = geo[b];
     const float *eb = e + (size_t)b * ev * ev;
-    for (int p = threadIdx.x; p < g.qh * ev; p += blockDim.x) {
-        const int qy = p / ev, qx = p % ev;
-        if (qx >= g.qw)
-            continue;
-        const float v = eb[qy * ev + qx];
-        if (v == 0.0f)
-            continue;
-        for (int t = 0; t < nt; t++)
-            atomicAdd(&sh[t * HL_HEAD_R + head_bin(g, qy, qx, cs[t], sn[t])], v);
+    for (int job = threadIdx.x; job < nt * ev; job += blockDim.x) {
+        const int t = job / ev, line = job % ev;
+        const float c = cs[t], sv = sn[t];
+        const bool walk_y = fabsf(sv) < fabsf(c);
+        unsigned long long run = 0ull;
+        int cur = -1;
+        for (int i = 0; i < ev; i++) {
+            const int qy = walk_y ? i : line, qx = walk_y ? line : i;
+            if (qy >= g.qh || qx >= g.qw)
+                continue;
+            const float v = eb[qy * ev + qx];
+            if (v == 0.0f)
+                continue;
+            const int bin = head_bin(g, qy, qx, c, sv);
+            if (bin != cur) {
+                if (cur >= 0)
+                    atomicAdd(&sh[t * HL_HEAD_R + cur], run);
+                cur = bin;
+                run = 0ull;
+            }
+            run += (unsigned long long)__float2ll_rn(v * HEAD_FIX);
+        }
+        if (cur >= 0)
+            atomicAdd(&sh[t * HL_HEAD_R + cur], run);
     }
     __syncthreads();
     const float alpha = ab[0], beta = ab[1];
     for (int i = threadIdx.x; i < nt * HL_HEAD_R; i += blockDim.x) {
         const size_t o = (size_t)b * HL_HEAD_T * HL_HEAD_R + (size_t)t0 * HL_HEAD_R + i;
-        hsum[o] = sh[i];
-        logits[o] = alpha * sh[i] + beta;
+        const float sum = (float)((double)(long long)sh[i] * (1.0 / HEAD_FIX));
+        hsum[o] = sum;
+        logits[o] = alpha * sum + beta;
     }
 }
 
@@ -650,7 +673,7 @@ cudaError_t hl_launch_head_fwd(const float *e, int ev, const hl_head_geom *geo,
                                int nimg, const float *ab, float *hsum,
                                float *logits, cudaStream_t s)
 {
-    hl_head_fwd_kernel<<<dim3((HL_HEAD_T + HEAD_TG - 1) / HEAD_TG, nimg), 256, 0, s>>>(
+    hl_head_fwd_kernel<<<dim3((HL_HEAD_T + HEAD_TG - 1) / HEAD_TG, nimg), 384, 0, s>>>(
         e, ev, geo, ab, hsum, logits, head_trig());
     return cudaGetLastError();
 }
