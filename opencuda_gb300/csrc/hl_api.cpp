@@ -808,6 +808,32 @@ static int run_ab(hl_handle *h, const hl_roi &roi, const hl_geom &g,
 }
 
 /* stage (c) over h->d_acc */
+/* the tail's arguments for one image: the handle's keys and counters, the
+ * result records into lines_dev (or the handle's result buffer) */
+static void final_args(hl_handle *h, const hl_geom &g, int linesmax, hl_line *lines_dev,
+                       int *count_dev, hl_final_args *fa)
+{
+    memset(fa, 0, sizeof(*fa));
+    fa->imgs = nullptr;
+    fa->img0.keys = h->d_keys;
+    fa->img0.ncand = h->d_counters + 0;
+    fa->img0.cap = key_cap(h);
+    fa->img0.rho_min = g.rho_min;
+    fa->img0.ref_numrho = g.ref_numrho;
+    fa->img0.pad = 0;
+    fa->T = h->T;
+    fa->detheta = h->p.detheta;
+    fa->thresdis = h->p.thresdis;
+    fa->thresang = h->p.thresang;
+    fa->linesmax = linesmax;
+    fa->hdr = reinterpret_cast<hl_result_hdr *>(h->d_result);
+    fa->img0.lines = lines_dev ? lines_dev
+                               : reinterpret_cast<hl_line *>(h->d_result +
+                                                             sizeof(hl_result_hdr));
+    fa->status = h->d_counters + 1;
+    fa->img0.count_out = count_dev;
+}
+
 static int run_c(hl_handle *h, const hl_geom &g, int linesmax,
                  hl_line *lines_dev, int *count_dev, cudaStream_t s,
                  int *launches)
@@ -831,24 +857,7 @@ static int run_c(hl_handle *h, const hl_geom &g, int linesmax,
     prof_mark(h, 3, s);
 
     hl_final_args fa;
-    fa.imgs = nullptr;
-    fa.img0.keys = h->d_keys;
-    fa.img0.ncand = h->d_counters + 0;
-    fa.img0.cap = pa.img0.cap;
-    fa.img0.rho_min = g.rho_min;
-    fa.img0.ref_numrho = g.ref_numrho;
-    fa.img0.pad = 0;
-    fa.T = h->T;
-    fa.detheta = h->p.detheta;
-    fa.thresdis = h->p.thresdis;
-    fa.thresang = h->p.thresang;
-    fa.linesmax = linesmax;
-    fa.hdr = reinterpret_cast<hl_result_hdr *>(h->d_result);
-    fa.img0.lines = lines_dev ? lines_dev
-                              : reinterpret_cast<hl_line *>(h->d_result +
-                                                            sizeof(hl_result_hdr));
-    fa.status = h->d_counters + 1;
-    fa.img0.count_out = count_dev;
+    final_args(h, g, linesmax, lines_dev, count_dev, &fa);
     CK(hl_launch_finalize(&fa, 1, s));
     (*launches)++;
     prof_mark(h, 4, s);
@@ -905,6 +914,28 @@ static int plain_launch(hl_handle *h, const hl_image_desc *img, int linesmax,
         return rc;
     int launches = 0;
     h->last_batch = 0;
+    if (!h->win_rows_override && !h->threads_override && !h->prof &&
+        hl_small_fits(h->T, h->Tp, g.numrho)) {
+        /* a small image: the whole path in one cluster launch, the
+         * accumulator in shared memory only */
+        hl_small_args sa;
+        memset(&sa, 0, sizeof(sa));
+        sa.roi = roi;
+        sa.pts = reinterpret_cast<float2 *>(h->d_pts);
+        sa.cosv = h->d_cos;
+        sa.sinv = h->d_sin;
+        sa.T = h->T;
+        sa.Tp = h->Tp;
+        sa.R = g.numrho;
+        sa.rho_min = g.rho_min;
+        sa.irho = (float)(1.0 / h->p.derho);   /* okano_3_0/HoughLine.cu:107 */
+        sa.threshold = h->p.threshold;
+        final_args(h, g, linesmax, lines_dev, count_dev, &sa.fin);
+        sa.scale = (float)(1.0 / (h->T + 2));  /* :882-883 */
+        CK(hl_launch_small(&sa, s));
+        h->last_launches = 1;
+        return HL_NO_ERROR;
+    }
     if ((rc = run_ab(h, roi, g, s, &launches)) != HL_NO_ERROR)
         return rc;
     rc = run_c(h, g, linesmax, lines_dev, count_dev, s, &launches);

@@ -218,6 +218,23 @@ typedef struct hl_final_args {
     int *status;              /* read; reset to 0 when hdr is set */
 } hl_final_args;
 
+/* The whole plain path of one small image in one cluster launch (see
+ * hl_small_kernel): usable when Tp / 32 <= HL_SMALL_MAX_CTAS and the R x 32
+ * accumulator slice plus its dump row fit one CTA's shared memory. */
+#define HL_SMALL_MAX_CTAS 8
+typedef struct hl_small_args {
+    hl_roi roi;
+    float2 *pts;              /* w * h entries of scratch (global) */
+    const float *cosv, *sinv; /* [Tp] */
+    int T, Tp, R, rho_min;
+    float irho;
+    int threshold;
+    hl_final_args fin;        /* keys, counters, result records */
+    float scale;              /* (float)(1 / (T + 2)), the reference decode */
+} hl_small_args;
+int hl_small_fits(int T, int Tp, int R);
+cudaError_t hl_launch_small(const hl_small_args *a, cudaStream_t s);
+
 /* launchers (return cudaGetLastError() after the launch) */
 cudaError_t hl_launch_trig(float *cosv, float *sinv, int T, int Tp,
                            double detheta, cudaStream_t s);

@@ -19,6 +19,7 @@
  * (:853-873) is unstable, so ties are ordered by index here.
  */
 #include "hl_internal.h"
+#include "hl_device.cuh"
 
 #include <math.h>
 
@@ -669,6 +670,280 @@ cudaError_t hl_launch_finalize(const hl_final_args *a, int nimg, cudaStream_t s)
         return e;
     return hl_launch_pdl(hl_finalize_kernel, dim3(nimg), dim3(FIN_THREADS), smem, s, false, *a,
                          scale);
+}
+
+/* ---- one small image in one launch ----------------------------------------
+ * A cluster of Tp / 32 CTAs (1024 threads each), CTA c owning theta slice c
+ * and the whole rho range of it in shared memory (R rows x 32 columns plus a
+ * dump row), so no accumulator goes to HBM:
+ *   1. CTA c compacts the ROI rows [c h / C, (c + 1) h / C) into its part of
+ *      one global point list (ROI-local float (x, y); a count pass, the
+ *      counts exchanged through distributed shared memory after a cluster
+ *      barrier, then a write pass at the CTA's offset from the first pass's
+ *      edge masks, kept in registers when a thread has one batch of chunks;
+ *      the order inside the list is free, the counts do not depend on it);
+ *   2. after a second cluster barrier every CTA votes every point of the list
+ *      into its slice with the vote kernel's diagonal schedule (the vote rule
+ *      of okano_3_0/HoughLine.cu:86-130, exact float -> integer conversion);
+ *   3. after a third barrier the peak rule (:168-213, bounds-checked, zero
+ *      outside the accumulator) runs on the slice in shared memory, the
+ *      neighbours across a slice edge read from the next CTA's shared memory
+ *      (distributed shared memory loads), peaks appended as keys;
+ *   4. after a fourth barrier (no CTA reads another's slice any more) CTA 0
+ *      reuses its shared memory for the tail (rank, decode, merge, truncate:
+ *      finalize_cta) and writes the result.
+ * The four cluster barriers are the only waits. */
+#define SMALL_THREADS 1024
+
+/* 4-bit mask of the bytes of w equal to 0xFF (bit b = byte b) */
+__device__ __forceinline__ uint32_t eq255_mask4(uint32_t w)
+{
+    const uint32_t m = __vcmpeq4(w, 0xffffffffu) & 0x80808080u;
+    return ((m >> 7) | (m >> 14) | (m >> 21) | (m >> 28)) & 15u;
+}
+
+static inline size_t small_smem(int R)
+{
+    const size_t acc = (size_t)(R + 1) * HL_SLICE * sizeof(int);
+    return acc > sizeof(FinSmem) ? acc : sizeof(FinSmem);
+}
+
+int hl_small_fits(int T, int Tp, int R)
+{
+    const int C = Tp / HL_SLICE;
+    return T > 0 && C >= 1 && C <= HL_SMALL_MAX_CTAS && R > 0 &&
+           small_smem(R) <= 227u * 1024u;
+}
+
+/* Edge masks of this thread's four 16-pixel chunks c, c + SMALL_THREADS, ...
+ * of the rows [y0, ...) (bit b = pixel x + b is 255; 0 past nch) */
+__device__ __forceinline__ void small_chunk_masks(const hl_roi &roi, int y0, int cw, int nch,
+                                                  int w, int c, uint32_t mm[4])
+{
+    uint4 v[4];
+    bool vec[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+        const int cc = c + u * SMALL_THREADS;
+        const int y = y0 + cc / cw, x = (cc % cw) * 16;
+        const uint8_t *pp = roi.base + (size_t)y * roi.pitch + x;
+        vec[u] = cc < nch && x + 16 <= w && (((uintptr_t)pp) & 15u) == 0;
+        v[u] = vec[u] ? __ldcs(reinterpret_cast<const uint4 *>(pp)) : make_uint4(0, 0, 0, 0);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+        const int cc = c + u * SMALL_THREADS;
+        uint32_t m = 0;
+        if (vec[u]) {
+            m = eq255_mask4(v[u].x) | (eq255_mask4(v[u].y) << 4) |
+                (eq255_mask4(v[u].z) << 8) | (eq255_mask4(v[u].w) << 12);
+        } else if (cc < nch) {
+            const int y = y0 + cc / cw, x = (cc % cw) * 16;
+            const uint8_t *pp = roi.base + (size_t)y * roi.pitch + x;
+            const int lim = min(16, w - x);
+            for (int b = 0; b < lim; b++)
+                m |= (uint32_t)(pp[b] == 255) << b;
+        }
+        mm[u] = m;
+    }
+}
+
+template <bool UNIT>
+__global__ void __launch_bounds__(SMALL_THREADS, 1)
+hl_small_kernel(hl_small_args a)
+{
+    extern __shared__ __align__(16) unsigned char small_raw[];
+    int *acc = reinterpret_cast<int *>(small_raw);
+    __shared__ int s_cnt, s_wr;
+    cg::cluster_group cl = cg::this_cluster();
+    const int C = (int)cl.num_blocks(), rank = (int)cl.block_rank();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nwarps = SMALL_THREADS / 32;
+    const int w = a.roi.w, h = a.roi.h;
+
+    /* 1. compaction of this CTA's rows in two passes over 16-pixel chunks
+     * (four 16-byte loads in flight per thread; byte loads where a chunk is
+     * unaligned or runs past the ROI's right edge): count, exchange the
+     * counts across the cluster, then write the points at this CTA's offset
+     * of one contiguous list (the second pass reads the rows from L2).  The
+     * slice is cleared meanwhile. */
+    for (int i = tid; i < (a.R + 1) * HL_SLICE; i += SMALL_THREADS)
+        acc[i] = 0;
+    if (tid == 0) {
+        s_cnt = 0;
+        s_wr = 0;
+    }
+    __syncthreads();
+    const int y0 = (int)((long long)h * rank / C), y1 = (int)((long long)h * (rank + 1) / C);
+    const int cw = (w + 15) >> 4;
+    const int nch = (y1 - y0) * cw;
+    int mycnt = 0;
+    const bool one_batch = nch <= 4 * SMALL_THREADS;   /* masks kept in registers */
+    uint32_t kept[4] = {0u, 0u, 0u, 0u};
+    for (int c0 = 0; c0 < nch; c0 += 4 * SMALL_THREADS) {
+        uint32_t mm[4];
+        small_chunk_masks(a.roi, y0, cw, nch, w, c0 + tid, mm);
+        mycnt += __popc(mm[0]) + __popc(mm[1]) + __popc(mm[2]) + __popc(mm[3]);
+        if (one_batch) {
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                kept[u] = mm[u];
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        mycnt += __shfl_xor_sync(FULL, mycnt, o);
+    if (lane == 0 && mycnt)
+        atomicAdd(&s_cnt, mycnt);
+    cl.sync();
+    int start = 0, ntot = 0;
+    for (int r = 0; r < C; r++) {
+        const int n = *cl.map_shared_rank(&s_cnt, r);
+        start += r < rank ? n : 0;
+        ntot += n;
+    }
+    for (int c0 = 0; c0 < nch; c0 += 4 * SMALL_THREADS) {
+        uint32_t mm[4];
+        if (one_batch) {
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                mm[u] = kept[u];
+        } else {
+            small_chunk_masks(a.roi, y0, cw, nch, w, c0 + tid, mm);
+        }
+        const int cnt = __popc(mm[0]) + __popc(mm[1]) + __popc(mm[2]) + __popc(mm[3]);
+        int pos = cnt ? start + atomicAdd(&s_wr, cnt) : 0;
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int c = c0 + tid + u * SMALL_THREADS;
+            const float y = (float)(y0 + c / cw);
+            const int x = (c % cw) * 16;
+            for (uint32_t m = mm[u]; m; m &= m - 1)
+                a.pts[pos++] = make_float2((float)(x + __ffs(m) - 1), y);
+        }
+    }
+    __threadfence();
+    cl.sync();
+
+    /* 2. every point voted into this slice, rounds of 8 points, four
+     * rounds' loads in flight per warp (the points come from L2) */
+    const int k0 = rank * HL_SLICE;
+    DiagTab tab;
+    diag_table(tab, a.cosv + k0, a.sinv + k0, (unsigned)__cvta_generic_to_shared(acc), lane);
+    const f2x ir = f2_pack(a.irho, a.irho);
+    const int p = lane & 7;
+    for (int g0 = warp * 8; g0 < ntot; g0 += 4 * nwarps * 8) {
+        float2 q[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int gi = g0 + u * nwarps * 8 + p;
+            q[u] = gi < ntot ? a.pts[gi] : make_float2(1e30f, 0.0f);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (g0 + u * nwarps * 8 < ntot)
+                diag_point<UNIT, CV_SIGN>(q[u].x, q[u].y, tab, ir, RHO_MAGIC_BITS + a.rho_min,
+                                          (unsigned)a.R);
+    }
+    cl.sync();
+
+    /* 3. peaks of the slice: v > thr, v > W, v >= E, v > N, v >= S */
+    const int *accL = rank > 0 ? cl.map_shared_rank(acc, rank - 1) : nullptr;
+    const int *accR = rank + 1 < C ? cl.map_shared_rank(acc, rank + 1) : nullptr;
+    const hl_final_img &im = a.fin.img0;
+    const int4 *acc4 = reinterpret_cast<const int4 *>(acc);
+    const int n4 = a.R * (HL_SLICE / 4);
+    /* a uniform trip count for every warp (the warp collectives below) */
+    for (int b4 = 0; b4 < n4; b4 += SMALL_THREADS) {
+        const int i4 = b4 + tid;
+        const int4 q4 = i4 < n4 ? acc4[i4] : make_int4(0, 0, 0, 0);
+        const int mx = max(max(q4.x, q4.y), max(q4.z, q4.w));
+        unsigned found = 0;   /* bit e: bin 4 i4 + e is a peak */
+        if (i4 < n4 && mx > a.threshold) {
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int i = 4 * i4 + e;
+                const int row = i >> 5, j = i & 31, k = k0 + j;
+                const int v = e == 0 ? q4.x : e == 1 ? q4.y : e == 2 ? q4.z : q4.w;
+                if (k < a.T && v > a.threshold) {
+                    const int W = j > 0 ? acc[i - 1] : (accL ? accL[row * HL_SLICE + 31] : 0);
+                    const int E = k + 1 >= a.T ? 0
+                                  : (j < 31 ? acc[i + 1] : accR[row * HL_SLICE]);
+                    const int N = row > 0 ? acc[i - HL_SLICE] : 0;
+                    const int S = row + 1 < a.R ? acc[i + HL_SLICE] : 0;
+                    if (v > W && v >= E && v > N && v >= S)
+                        found |= 1u << e;
+                }
+            }
+        }
+        const int cnt = __popc(found);
+        const unsigned any = __ballot_sync(FULL, cnt > 0);
+        if (!any)
+            continue;
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o)
+                incl += t;
+        }
+        int base = 0;
+        if (lane == 31)
+            base = atomicAdd(im.ncand, incl);
+        base = __shfl_sync(FULL, base, 31);
+        int pos = base + incl - cnt;
+        for (unsigned f = found; f; f &= f - 1) {
+            const int e = __ffs(f) - 1;
+            const int i = 4 * i4 + e;
+            const int row = i >> 5, k = k0 + (i & 31);
+            const int v = e == 0 ? q4.x : e == 1 ? q4.y : e == 2 ? q4.z : q4.w;
+            if (pos < im.cap) {
+                const unsigned idx = (unsigned)row * (unsigned)a.T + (unsigned)k;
+                const_cast<unsigned long long *>(im.keys)[pos] =
+                    ((unsigned long long)(unsigned)v << 32) | (unsigned)(~idx);
+            }
+            pos++;
+        }
+    }
+    __threadfence();
+    cl.sync();
+
+    /* 4. the tail on CTA 0, in the shared memory the slice used */
+    if (rank != 0)
+        return;
+    FinSmem &sm = *reinterpret_cast<FinSmem *>(small_raw);
+    finalize_cta(a.fin, im, a.scale, sm);
+}
+
+cudaError_t hl_launch_small(const hl_small_args *a, cudaStream_t s)
+{
+    const int C = a->Tp / HL_SLICE;
+    const size_t smem = small_smem(a->R);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)C);
+    cfg.blockDim = dim3(SMALL_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaError_t e;
+    if (a->irho == 1.0f) {
+        e = cudaFuncSetAttribute(hl_small_kernel<true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess)
+            return e;
+        return cudaLaunchKernelEx(&cfg, hl_small_kernel<true>, *a);
+    }
+    e = cudaFuncSetAttribute(hl_small_kernel<false>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    return cudaLaunchKernelEx(&cfg, hl_small_kernel<false>, *a);
 }
 
 /* acc[R][Tp] -> acc[R][T] */

@@ -63,18 +63,6 @@
  * every tile to an even number of points, 16 bytes) */
 #define SLOT_CAP HL_VOTE_CHUNK
 
-/* Float -> integer without the conversion pipe (16 results per SM-clock).
- * M = 1.5 * 2^23: for |v| < 2^22 the sum v + M lies in [2^23, 2^24), where
- * floats are spaced 1 apart, so the sum rounded toward zero is M + floor(v)
- * and rounded up is M + ceil(v), and its bit pattern is bits(M) plus that
- * integer.  Truncation equals floor for v >= 0 and ceil for v < 0, so a rho
- * window whose rows are all >= 1 may use floor (a negative v then lands below
- * the window either way), one whose rows are all <= -1 may use ceil, and only
- * the window holding row 0 needs the exact conversion. */
-#define RHO_MAGIC 12582912.0f
-#define RHO_MAGIC_BITS 0x4B400000
-enum { CV_EXACT = 0, CV_FLOOR = 1, CV_CEIL = 2 };
-
 /* ---- mbarrier + bulk copy ---------------------------------------------- */
 __device__ __forceinline__ unsigned smem_u32(const void *p)
 {
@@ -128,121 +116,6 @@ __device__ __forceinline__ bool mbar_wait_sleep(unsigned long long *bar,
             return true;
     }
     return false;
-}
-
-/* one vote, no returned value */
-__device__ __forceinline__ void red_smem(unsigned addr)
-{
-    asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(addr));
-}
-
-/* ---- packed f32x2 arithmetic ------------------------------------------ *
- * Two lanes of a 64-bit register pair per instruction.  The products are
- * formed as fma.rn(a, b, +0): exactly fl(a*b) for the finite operands here
- * (a -0 product becomes +0, which no later sum or truncation can tell
- * apart).  A plain mul.rn.f32x2 followed by add.rn.f32x2 is contracted by
- * ptxas into one fused multiply-add, which changes rho in a small fraction
- * of votes; the fma form is never contracted (checked on the GPU against
- * the scalar __fmul_rn/__fadd_rn rule for every (x, y) of a 4096 x 4096
- * image at T = 720: no difference). */
-typedef unsigned long long f2x;
-__device__ __forceinline__ f2x f2_pack(float a, float b)
-{
-    f2x r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-__device__ __forceinline__ void f2_unpack(f2x r, unsigned &a, unsigned &b)
-{
-    asm("mov.b64 {%0, %1}, %2;" : "=r"(a), "=r"(b) : "l"(r));
-}
-__device__ __forceinline__ f2x f2_mul(f2x a, f2x b)
-{
-    f2x d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(0ull));
-    return d;
-}
-__device__ __forceinline__ f2x f2_add(f2x a, f2x b)
-{
-    f2x d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ f2x f2_add_rz(f2x a, f2x b)
-{
-    f2x d;
-    asm("add.rz.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ f2x f2_add_rp(f2x a, f2x b)
-{
-    f2x d;
-    asm("add.rp.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-
-/* Diagonal vote schedule.  A consumer warp votes 8 points at a time, each
- * point on 4 lanes: lane = p + 8 j (point p, theta group j).  At step i the
- * lane votes theta column 8 j + (p + i) % 8 of the slice, so at every step
- * the 32 lanes address 32 different columns -- 32 different banks, whatever
- * rows their points reach -- and over the 8 steps every point votes all 32
- * thetas.  A lane loads its point once per 8 votes (one shared-memory
- * wavefront for the warp's 8 points), where a broadcast load per point
- * would cost as many wavefronts as the atomics themselves: the shared
- * pipe serves loads, shuffles and reductions alike at about one wavefront
- * per SM-clock.  Each lane keeps its 8 columns' cos/sin as f32x2 pairs of
- * consecutive steps and the columns' shared-memory addresses. */
-struct DiagTab {
-    f2x c[4], s[4];        /* cos / sin of the lane's columns, steps (2i, 2i + 1) */
-    unsigned col[8];       /* address of the lane's column at step i, row 0 */
-};
-
-__device__ __forceinline__ void diag_table(DiagTab &t, const float *cs, const float *sn,
-                                           unsigned acc_base, int lane)
-{
-    const int p = lane & 7, j = lane >> 3;
-#pragma unroll
-    for (int i = 0; i < 8; i += 2) {
-        const int c0 = 8 * j + ((p + i) & 7), c1 = 8 * j + ((p + i + 1) & 7);
-        t.c[i / 2] = f2_pack(cs[c0], cs[c1]);
-        t.s[i / 2] = f2_pack(sn[c0], sn[c1]);
-        t.col[i] = acc_base + 4u * (unsigned)c0;
-        t.col[i + 1] = acc_base + 4u * (unsigned)c1;
-    }
-}
-
-/* The 8 steps of one point (x, y) on this lane.  rho per the vote rule
- * (okano_3_0/HoughLine.cu:115-121), the row relative to the window clamped
- * to the dump row `lim`; float -> integer by the magic constant (CV_FLOOR /
- * CV_CEIL, see RHO_MAGIC) or by the exact conversion (CV_EXACT). */
-template <bool UNIT, int CV>
-__device__ __forceinline__ void diag_point(float x, float y, const DiagTab &t, f2x ir,
-                                           int base, unsigned lim)
-{
-    const f2x X = f2_pack(x, x), Y = f2_pack(y, y);
-    const f2x M = f2_pack(RHO_MAGIC, RHO_MAGIC);
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        f2x a = f2_mul(X, t.c[i]), b = f2_mul(Y, t.s[i]);
-        if (!UNIT) {
-            a = f2_mul(a, ir);
-            b = f2_mul(b, ir);
-        }
-        const f2x v = f2_add(a, b);
-        unsigned r0, r1;
-        if (CV == CV_FLOOR) {
-            f2_unpack(f2_add_rz(v, M), r0, r1);
-        } else if (CV == CV_CEIL) {
-            f2_unpack(f2_add_rp(v, M), r0, r1);
-        } else {
-            unsigned u0, u1;
-            f2_unpack(v, u0, u1);
-            r0 = (unsigned)__float2int_rz(__uint_as_float(u0));
-            r1 = (unsigned)__float2int_rz(__uint_as_float(u1));
-        }
-        red_smem(t.col[2 * i] + 128u * min(r0 - (unsigned)base, lim));
-        red_smem(t.col[2 * i + 1] + 128u * min(r1 - (unsigned)base, lim));
-    }
 }
 
 /* A consumer warp's share of a slot: points [0, m) of pts, m <= 64, 8 per

@@ -258,3 +258,37 @@ def test_trig_table_matches_golden(hl_mod):
         c, s = HoughLine(detheta=det).trig_table()
         T = len(c)
         assert np.array_equal(c, z[f"cos_T{T}"]) and np.array_equal(s, z[f"sin_T{T}"])
+
+
+@pytest.mark.parametrize("w,h,det,derho,noise,roi", [
+    (512, 512, math.pi / 180, 1.0, 10000, None),          # the 512 x 512 configuration
+    (640, 480, math.pi / 180, 1.0, 20000, (7, 3, 631, 470)),
+    (333, 127, math.pi / 90, 1.0, 30000, None),            # 3 CTAs of 32 thetas
+    (600, 600, math.pi / 256, 1.0, 8000, None),            # 8 CTAs, the most a cluster takes
+    (512, 384, math.pi / 180, 2.0, 10000, None),           # rho step 2 (irho = 0.5)
+    (1, 1, math.pi / 180, 1.0, 0, None),
+])
+def test_small_image_single_launch(hl_mod, w, h, det, derho, noise, roi):
+    """Small images take one cluster launch (compaction, vote, peaks and the
+    tail, the accumulator in shared memory only); its lines must equal the
+    multi-launch pipeline's (forced by a vote shape) and the oracle's."""
+    HoughLine, Image = hl_mod
+    img = cases.synth_custom(w, h, 6, 20, max(w, h) // 2 + 20, noise, w + h)
+    if w == 1:
+        img[:] = 255
+    thr = 30 if w > 1 else 0
+    dev = Image.from_host(img, roi)
+    hl = HoughLine(detheta=det, derho=derho, threshold=thr)
+    rc, small = hl.houghLine(dev, None, 24)
+    assert rc == 0 and hl.last_launch_count() == 1
+    ref = HoughLine(detheta=det, derho=derho, threshold=thr)
+    assert ref.set_vote_shape(1000, 1024) == 0
+    rc, multi = ref.houghLine(dev, None, 24)
+    assert rc == 0 and ref.last_launch_count() > 1
+    x1, y1, x2, y2 = roi if roi else (0, 0, w, h)
+    want, _, _ = _oracle_lines(hl, img[y1:y2, x1:x2], thr, 24, det, derho)
+    assert [l.astuple() for l in small] == want
+    assert [l.astuple() for l in multi] == want
+    # a second call on the same handle reuses the cleared candidate counter
+    rc, again = hl.houghLine(dev, None, 24)
+    assert rc == 0 and [l.astuple() for l in again] == want
