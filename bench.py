@@ -733,6 +733,17 @@ def run_gb300(args):
             print(json.dumps({"circle": out}))
         return 0
 
+    if args.batched_only:
+        stream = torch.cuda.current_stream(dev)
+        sp = C.c_void_p(stream.cuda_stream)
+        atom = C.c_double()
+        _lib.check(L.hl_measure_smem_atomic_peak(2000, C.byref(atom), sp), "atomic peak")
+        out = batched_workload(L, HoughLine, Image, dev, sp, max(args.steps, 5), atom.value,
+                               ws == 1 and not args.no_cpu_baseline)
+        if rank == 0:
+            print(json.dumps({"batched": out}))
+        return 0
+
     imgs_host = make_images(rank, 4)
     hl = HoughLine(detheta=DETHETA, threshold=THRESHOLD)
     g = hl.geometry(W, H)
@@ -961,6 +972,8 @@ def main():
                     help="skip the HoughCircle measurement")
     ap.add_argument("--circle-only", action="store_true",
                     help="only the HoughCircle measurement (its own JSON line)")
+    ap.add_argument("--batched-only", action="store_true",
+                    help="only the batched 256-image measurement (its own JSON line)")
     ap.add_argument("--no-proposal", action="store_true",
                     help="skip the proposal-guided measurements")
     args = ap.parse_args()
