@@ -162,10 +162,11 @@ static inline long long hl_slot4(int win_rows, int part16)
 /* Tiles the allocation-free compaction entry point can serve. */
 #define HL_NOALLOC_MAX_TILES 65536
 
-/* Vote-kernel staging: points per ring slot (a batch is 64 points per
- * consumer warp, at most 31 warps), ring slots, tiles per coarse-filter
+/* Vote-kernel staging: points per consumer warp per batch, points per ring
+ * slot (at most 31 consumer warps), ring slots, tiles per coarse-filter
  * group. */
-#define HL_VOTE_CHUNK 2048
+#define HL_VOTE_PPW 64
+#define HL_VOTE_CHUNK (HL_VOTE_PPW * 32)
 #define HL_VOTE_SLOTS 3
 #define HL_VOTE_TG 4096
 /* largest rho window (rows) one CTA can hold next to its staging */

@@ -25,11 +25,11 @@
  * aligned because the compaction pads every tile to an even number of
  * float2 entries.  The runs, laid end to end, form the item's point stream.
  * It publishes the item as a segment (double-buffered descriptor) and
- * streams it: a batch is 64 points per consumer warp, batch b the stream
+ * streams it: a batch is HL_VOTE_PPW points per consumer warp, batch b the stream
  * range [b*B, (b+1)*B); the producer's lanes each copy one run's part of it
  * into a ring of HL_VOTE_SLOTS shared-memory slots with cp.async.bulk (TMA
  * bulk copies completing on the slot's full barrier), so a slot holds its
- * batch gap-free; consumer warp i votes points [64i, 64i + 64) of the slot
+ * batch gap-free; consumer warp i votes points [PPW i, PPW i + PPW) of the slot
  * straight from shared memory and arrives on the slot's empty barrier, which
  * the producer waits on before refilling it.  The producer moves on to the
  * next item as soon as the current one is issued, so its setup and first
@@ -118,16 +118,16 @@ __device__ __forceinline__ bool mbar_wait_sleep(unsigned long long *bar,
     return false;
 }
 
-/* A consumer warp's share of a slot: points [0, m) of pts, m <= 64, 8 per
- * round.  Entries past m (stale ring data) vote as the sentinel (1e30, 0),
- * whose rows lie outside every window and go to the dump row. */
+/* A consumer warp's share of a slot: points [0, m) of pts, m <= HL_VOTE_PPW,
+ * 8 per round.  Entries past m (stale ring data) vote as the sentinel
+ * (1e30, 0), whose rows lie outside every window and go to the dump row. */
 template <bool UNIT, int CV>
 __device__ __forceinline__ void vote_share(const float2 *pts, int m, const DiagTab &t,
                                            f2x ir, int base, unsigned lim, int p)
 {
-    if (m >= 64) {
+    if (m >= HL_VOTE_PPW) {
 #pragma unroll 2
-        for (int r = 0; r < 64; r += 8) {
+        for (int r = 0; r < HL_VOTE_PPW; r += 8) {
             const float2 q = pts[r + p];
             diag_point<UNIT, CV>(q.x, q.y, t, ir, base, lim);
         }
@@ -496,8 +496,8 @@ hl_vote_kernel(hl_vote_args a)
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nthr = blockDim.x, nwarps = nthr >> 5;
     const int ncons = nwarps - 1;               /* consumer warps 1..nwarps-1 */
-    /* points per batch: 64 per consumer warp (at most SLOT_CAP) */
-    const int batch = 64 * ncons;
+    /* points per batch: HL_VOTE_PPW per consumer warp (at most SLOT_CAP) */
+    const int batch = HL_VOTE_PPW * ncons;
     const int nslices = a.Tp / HL_SLICE;
 
     hl_pdl_begin();
@@ -583,9 +583,9 @@ hl_vote_kernel(hl_vote_args a)
                               a.status))
                 return;
             seq++;
-            /* this warp's share: points [64 cw, 64 cw + 64) */
-            const int m = min(64, total - b * batch - 64 * cw);
-            const float2 *pts = sm.raw[slot] + 64 * cw;
+            /* this warp's share: points [PPW cw, PPW cw + PPW) */
+            const int m = min(HL_VOTE_PPW, total - b * batch - HL_VOTE_PPW * cw);
+            const float2 *pts = sm.raw[slot] + HL_VOTE_PPW * cw;
             if (cv == CV_FLOOR)
                 vote_share<UNIT, CV_FLOOR>(pts, m, tab, ir, vbase, lrows, pl);
             else if (cv == CV_CEIL)
