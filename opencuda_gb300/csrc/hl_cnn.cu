@@ -216,38 +216,46 @@ hl_conv3x3_kernel(hl_conv_args a)
     for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
         /* A operand: row m = output pixel tile * 128 + m */
         if (CIN == 32) {
-            /* one 16-byte cp.async per (row, K group): every copy of the
-             * tile in flight at once, zero-filled outside the image */
-            for (int e = tid; e < CNN_TILE_M * KG; e += CNN_THREADS) {
-                const int m = e / KG, q = e % KG;
-                const int p = tile * CNN_TILE_M + m;
-                bool ok = false;
-                const __nv_bfloat16 *src = a.x;
-                if (p < a.B * HWo) {
-                    const int bimg = p / HWo, r = p % HWo;
-                    const int oy = r / a.Wo, ox = r % a.Wo;
-                    /* K group q = tap q / 4, channels (q % 4) * 8 .. +7 */
-                    const int tap = q >> 2, c0 = (q & 3) * 8;
-                    const int ky = tap / 3, kx = tap % 3;
-                    int iy, ix;
-                    if (MODE == GATHER_CONV) {
-                        iy = oy * a.stride - 1 + ky;
-                        ix = ox * a.stride - 1 + kx;
-                        ok = iy >= 0 && ix >= 0 && iy < a.H && ix < a.W;
-                    } else {
-                        const int ty = oy + 1 - ky, tx = ox + 1 - kx;
-                        iy = ty >> 1;
-                        ix = tx >> 1;
-                        ok = ty >= 0 && tx >= 0 && !(ty & 1) && !(tx & 1) &&
-                             iy < a.H && ix < a.W;
-                    }
-                    if (ok)
-                        src = a.x + (((size_t)bimg * a.H + iy) * a.W + ix) * 32 + c0;
+            /* thread m gathers row m (one output pixel): its coordinates once,
+             * then one 16-byte cp.async per K group (tap q / 4, channels
+             * (q % 4) * 8 .. +7) with compile-time tap offsets; every copy of
+             * the tile in flight at once, zero-filled outside the image */
+            static_assert(CNN_THREADS == CNN_TILE_M, "one thread per tile row");
+            const int m = tid;
+            const int p = tile * CNN_TILE_M + m;
+            const bool row_ok = p < a.B * HWo;
+            int bimg = 0, oy = 0, ox = 0;
+            if (row_ok) {
+                bimg = p / HWo;
+                const int r = p - bimg * HWo;
+                oy = r / a.Wo;
+                ox = r - oy * a.Wo;
+            }
+            const __nv_bfloat16 *ximg = a.x + (size_t)bimg * a.H * a.W * 32;
+            const unsigned arow = cnn_smem_u32(&sm.a[m >> 3][0][(m & 7) * 16]);
+#pragma unroll
+            for (int tap = 0; tap < 9; tap++) {
+                const int ky = tap / 3, kx = tap % 3;
+                int iy, ix;
+                bool ok;
+                if (MODE == GATHER_CONV) {
+                    iy = oy * a.stride - 1 + ky;
+                    ix = ox * a.stride - 1 + kx;
+                    ok = row_ok && iy >= 0 && ix >= 0 && iy < a.H && ix < a.W;
+                } else {
+                    const int ty = oy + 1 - ky, tx = ox + 1 - kx;
+                    iy = ty >> 1;
+                    ix = tx >> 1;
+                    ok = row_ok && ty >= 0 && tx >= 0 && !(ty & 1) && !(tx & 1) &&
+                         iy < a.H && ix < a.W;
                 }
-                asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
-                             ::"r"(cnn_smem_u32(&sm.a[m >> 3][q][(m & 7) * 16])),
-                             "l"(src), "r"(ok ? 16 : 0)
-                             : "memory");
+                const __nv_bfloat16 *src = ok ? ximg + ((size_t)iy * a.W + ix) * 32 : a.x;
+#pragma unroll
+                for (int c = 0; c < 4; c++)
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
+                                 ::"r"(arow + (unsigned)((tap * 4 + c) * 128)),
+                                 "l"(src + c * 8), "r"(ok ? 16 : 0)
+                                 : "memory");
             }
             asm volatile("cp.async.wait_all;" ::: "memory");
         } else {
