@@ -45,6 +45,16 @@
 #define CT_WARPS (CT_THREADS / 32)
 #define CT_ROWS 256   /* compaction-tile rows of the halo taken per pass */
 
+#ifndef CT_SEG
+#define CT_SEG 4            /* lanes (segments of the walk) per point */
+#endif
+#define CT_QN (32 / CT_SEG) /* points per walk */
+struct CtSeg {
+    int nloop;                        /* steps of the longest segment */
+    int len[CT_SEG];                  /* steps of each segment */
+    int x[CT_SEG], y[CT_SEG], d[CT_SEG];   /* the state where it starts */
+};
+
 struct CircleTileSmem {
     int cnt[CT_CELLS];        /* the tile and its apron, row-major */
     int pre[CT_ROWS + 1];     /* points of the halo rows before each row */
@@ -54,6 +64,7 @@ struct CircleTileSmem {
     int2 left[CT_WARPS * 32];                /* the warps' last, partial queues */
     int nleft;
     int nextb;                               /* next candidate batch of the pass */
+    CtSeg seg;                              /* the segments of this CTA's walk */
 };
 
 /* one vote at the shared-memory word addr when p holds: a predicated
@@ -65,18 +76,29 @@ __device__ __forceinline__ void ct_red(unsigned addr, bool p)
                  :: "r"(addr), "r"((int)p) : "memory");
 }
 
-/* Each lane walks the midpoint circle of radius r around its point (x0, y0)
- * (okano_3_0/HoughCircle.cu:214-243) and votes the octant points that fall in
- * [0, xw) x [0, yh); pbase is the shared address of that region's origin.
- * The warp's lanes share r, so the loop and its d < y branch are uniform. */
-__device__ __forceinline__ void ct_walk(int x0, int y0, int r, int xw, int yh, unsigned pbase)
+/* A lane's votes: its point (x0, y0) walks (part of) the midpoint circle of
+ * radius r (okano_3_0/HoughCircle.cu:214-243) and votes the octant points
+ * that fall in [0, xw) x [0, yh); pbase is the shared address of that
+ * region's origin.  The warp's lanes share r, so the loop is uniform. */
+/* The walk of one radius split into CT_SEG segments on CT_SEG lanes.  The
+ * midpoint recurrence (x, y, d) depends on r only, so the state where each
+ * segment starts is the same for every point: lane l walks segment l / CT_QN
+ * of point l % CT_QN.  A walk covers CT_QN points in about 1 / CT_SEG of the
+ * steps of a whole walk, so the CTA's walks are CT_SEG times as many and as
+ * short, and the warps finish closer together. */
+__device__ __forceinline__ void ct_walk_seg(int x0, int y0, const CtSeg &hw, int seg,
+                                            int xw, int yh, unsigned pbase)
 {
-    int x = 0, y = r, d = 3 - 2 * r;
-    while (x < y) {
+    int x = hw.x[seg], y = hw.y[seg], d = hw.d[seg];
+    const int mylen = hw.len[seg], nloop = hw.nloop;
+    for (int it = 0; it < nloop; it++) {
+        const bool act = it < mylen;
         const int xa = x0 + x, xb = x0 - x, xc = x0 + y, xd = x0 - y;
         const int ya = y0 + y, yb = y0 - y, yc = y0 + x, yd = y0 - x;
-        const bool fxa = (unsigned)xa < (unsigned)xw, fxb = (unsigned)xb < (unsigned)xw;
-        const bool fxc = (unsigned)xc < (unsigned)xw, fxd = (unsigned)xd < (unsigned)xw;
+        const bool fxa = act && (unsigned)xa < (unsigned)xw;
+        const bool fxb = act && (unsigned)xb < (unsigned)xw;
+        const bool fxc = act && (unsigned)xc < (unsigned)xw;
+        const bool fxd = act && (unsigned)xd < (unsigned)xw;
         const bool fya = (unsigned)ya < (unsigned)yh, fyb = (unsigned)yb < (unsigned)yh;
         const bool fyc = (unsigned)yc < (unsigned)yh, fyd = (unsigned)yd < (unsigned)yh;
         const unsigned ra = pbase + 4u * (unsigned)(ya * CT_AW);
@@ -92,7 +114,6 @@ __device__ __forceinline__ void ct_walk(int x0, int y0, int r, int xw, int yh, u
         ct_red(rd + 4u * (unsigned)xc, fxc && fyd);
         ct_red(rc + 4u * (unsigned)xd, fxd && fyc);
         ct_red(rd + 4u * (unsigned)xd, fxd && fyd);
-        /* d < y: d += 4x + 6; else d += 4(x - y) + 10, y - 1 (as selects) */
         const bool up = d < y;
         d += up ? 4 * x + 6 : 4 * (x - y) + 10;
         y -= up ? 0 : 1;
@@ -152,6 +173,42 @@ hl_circle_tile_kernel(hl_circle_tile_args a0)
     /* counted cells, image coordinates: the tile and its apron within the ROI */
     const int cx0 = max(tx0 - 1, 0), cy0 = max(ty0 - 1, 0);
     const int cx1 = min(tx0 + HL_CIRCLE_TW + 1, a.w), cy1 = min(ty0 + HL_CIRCLE_TH + 1, a.h);
+    if (tid == 0 && r > 0) {
+        /* the midpoint recurrence of radius r (okano_3_0/HoughCircle.cu:
+         * 214-243): its step count, and the state where each segment starts */
+        int x = 0, y = r, d = 3 - 2 * r, n = 0;
+        while (x < y) {
+            const bool up = d < y;
+            d += up ? 4 * x + 6 : 4 * (x - y) + 10;
+            y -= up ? 0 : 1;
+            x++;
+            n++;
+        }
+        /* segment k: steps [k n / CT_SEG, (k + 1) n / CT_SEG) */
+        CtSeg hw;
+        x = 0;
+        y = r;
+        d = 3 - 2 * r;
+        int step = 0;
+        for (int k = 0; k < CT_SEG; k++) {
+            const int b0 = k * n / CT_SEG, b1 = (k + 1) * n / CT_SEG;
+            while (step < b0) {
+                const bool up = d < y;
+                d += up ? 4 * x + 6 : 4 * (x - y) + 10;
+                y -= up ? 0 : 1;
+                x++;
+                step++;
+            }
+            hw.x[k] = x;
+            hw.y[k] = y;
+            hw.d[k] = d;
+            hw.len[k] = b1 - b0;
+        }
+        hw.nloop = 0;
+        for (int k = 0; k < CT_SEG; k++)
+            hw.nloop = max(hw.nloop, hw.len[k]);
+        sm.seg = hw;
+    }
     __syncthreads();
     if (r > 0) {
         const int xlo = cx0 - tx0 + CT_OX, xw = cx1 - cx0;
@@ -234,42 +291,43 @@ hl_circle_tile_kernel(hl_circle_tile_args a0)
                 if (ok)
                     sm.rank_lane[warp][__popc(vm & ((1u << lane) - 1u))] = (unsigned char)lane;
                 __syncwarp();
-                /* slots [qn, qn + take) take the first ranks */
-                const int take = min(32 - qn, nv);
-                const bool fill = lane >= qn && lane - qn < take;
-                int src = fill ? sm.rank_lane[warp][lane - qn] : lane;
-                int nx = __shfl_sync(FULL, cx, src), ny = __shfl_sync(FULL, cy, src);
-                if (fill) {
-                    qx = nx;
-                    qy = ny;
-                }
-                qn += take;
-                if (qn == 32) {
-                    ct_walk(qx, qy, r, xw, yh, pbase);
-                    /* the ranks left over start the next queue */
-                    const int rem = nv - take;
-                    const bool f2 = lane < rem;
-                    src = f2 ? sm.rank_lane[warp][take + lane] : lane;
-                    nx = __shfl_sync(FULL, cx, src);
-                    ny = __shfl_sync(FULL, cy, src);
-                    qx = f2 ? nx : CT_NOWHERE;
-                    qy = f2 ? ny : CT_NOWHERE;
-                    qn = rem;
+                /* the queue is lanes [0, CT_QN); slots [qn, qn + take) take
+                 * the next ranks, and a full queue walks its circles at once,
+                 * CT_SEG lanes a point */
+                for (int done = 0; done < nv;) {
+                    const int take = min(CT_QN - qn, nv - done);
+                    const bool fill = lane >= qn && lane < qn + take;
+                    const int src = fill ? sm.rank_lane[warp][done + lane - qn] : lane;
+                    const int nx = __shfl_sync(FULL, cx, src), ny = __shfl_sync(FULL, cy, src);
+                    if (fill) {
+                        qx = nx;
+                        qy = ny;
+                    }
+                    qn += take;
+                    done += take;
+                    if (qn == CT_QN) {
+                        const int px = __shfl_sync(FULL, qx, lane % CT_QN);
+                        const int py = __shfl_sync(FULL, qy, lane % CT_QN);
+                        ct_walk_seg(px, py, sm.seg, lane / CT_QN, xw, yh, pbase);
+                        qx = CT_NOWHERE;
+                        qy = CT_NOWHERE;
+                        qn = 0;
+                    }
                 }
                 __syncwarp();   /* rank_lane is rewritten by the next batch */
             }
             __syncthreads();   /* before the next pass rewrites pre / start */
         }
-        /* the partial queues left in every warp are pooled and walked 32 at
-         * a time, not as up to 16 part-empty walks */
+        /* the partial queues left in every warp are pooled and walked CT_QN
+         * points at a time, not as up to 32 part-empty walks */
         if (lane < qn)
             sm.left[atomicAdd(&sm.nleft, 1)] = make_int2(qx, qy);
         __syncthreads();
         const int nl = sm.nleft;
-        for (int b0 = warp * 32; b0 < nl; b0 += CT_THREADS) {
-            const int k = b0 + lane;
+        for (int b0 = warp * CT_QN; b0 < nl; b0 += CT_WARPS * CT_QN) {
+            const int k = b0 + lane % CT_QN;
             const int2 q = k < nl ? sm.left[k] : make_int2(CT_NOWHERE, CT_NOWHERE);
-            ct_walk(q.x, q.y, r, xw, yh, pbase);
+            ct_walk_seg(q.x, q.y, sm.seg, lane / CT_QN, xw, yh, pbase);
         }
     }
     __syncthreads();
