@@ -848,7 +848,11 @@ static int run_c(hl_handle *h, const hl_geom &g, int linesmax,
     pa.img0.threshold = h->p.threshold;
     pa.img0.pad = 0;
     pa.chunks = nullptr;
-    pa.nchunks = (g.numrho + HL_PEAK_ROWS - 1) / HL_PEAK_ROWS;
+    /* units of HL_PEAK_FLAT int4; the kernel indexes the accumulator's int4
+     * in 32 bits */
+    if ((long long)g.numrho * (h->Tp / 4) >= (1LL << 32))
+        return HL_OP_OVERFLOW;
+    pa.nchunks = (int)(((long long)g.numrho * (h->Tp / 4) + HL_PEAK_FLAT - 1) / HL_PEAK_FLAT);
     pa.T = h->T;
     pa.Tp = h->Tp;
     pa.status = h->d_counters + 1;

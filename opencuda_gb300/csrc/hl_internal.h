@@ -182,15 +182,19 @@ typedef struct hl_peak_img {
     int pad;
 } hl_peak_img;
 
-/* rows of an accumulator one peak-pass chunk covers */
+/* rows of an accumulator one peak-pass chunk covers (several images), int4
+ * of a unit of one image's accumulator, threads of a peak-pass CTA */
 #define HL_PEAK_ROWS 16
+#define HL_PEAK_FLAT 1024
+#define HL_PEAK_THREADS 256
+#define HL_PEAK_CTAS_PER_SM 6
 
 typedef struct hl_peak_args {
     const hl_peak_img *imgs;  /* per image, or NULL: the one image img0 */
     hl_peak_img img0;
     const int2 *chunks;       /* {image, first row}, HL_PEAK_ROWS rows each;
-                                 NULL: chunk c is rows c * HL_PEAK_ROWS.. of
-                                 img0 */
+                                 NULL: unit c is int4 c * HL_PEAK_FLAT.. of
+                                 img0's accumulator */
     int nchunks;
     int T, Tp;
     int *status;

@@ -33,123 +33,116 @@ namespace cg = cooperative_groups;
 #define FIN_CHUNK 1024
 #define FIN_SCACHE 1024
 
-/* Chunks of HL_PEAK_ROWS accumulator rows of one image each, taken
- * grid-stride; one thread per 4 consecutive bins of a row (one 16-byte
- * streaming load).  The neighbours are read only for bins above the
- * threshold, which are rare, so the pass is one read of every accumulator
- * at HBM speed. */
-__global__ void __launch_bounds__(256) hl_peaks_kernel(hl_peak_args a)
+/* The peak rule (okano_3_0/HoughLine.cu:195-199, bounds-checked: zero
+ * outside the accumulator) for bin k of row `row` (p points at it), which
+ * exceeds the threshold; a peak is appended as its key.  Scalar loads: the
+ * bins are rare, and the kernel keeps few registers. */
+__device__ __forceinline__ void peak_bin(const int32_t *p, unsigned long long *keys, int *ncand,
+                                         int R, int cap, int T, int Tp, int row, int k,
+                                         int *status)
 {
+    const int x = p[0];
+    const int W = k > 0 ? p[-1] : 0;
+    const int E = k + 1 < T ? p[1] : 0;
+    const int N = row > 0 ? p[-Tp] : 0;
+    const int S = row + 1 < R ? p[Tp] : 0;
+    if (x > W && x >= E && x > N && x >= S) {
+        const unsigned idx = (unsigned)row * (unsigned)T + (unsigned)k;
+        const int pos = atomicAdd(ncand, 1);
+        if (pos < cap)
+            keys[pos] = ((unsigned long long)(unsigned)x << 32) | (unsigned)(~idx);
+        else
+            atomicOr(status, HL_ST_CAND_OVERFLOW);
+    }
+}
+
+/* One read of every accumulator at the memory system's speed.  Work units
+ * are taken grid-stride: with several images (chunks != NULL) a unit is
+ * HL_PEAK_ROWS rows of one image, with one image it is HL_PEAK_FLAT
+ * consecutive int4 of its accumulator (a unit need not start a row: each
+ * int4 finds its row).  A step of a unit is four int4 per thread, loaded at
+ * once (streaming loads) and compared with the threshold; an int4 holding
+ * a bin above it -- rare -- is noted in shared memory, and a step that
+ * noted any (one barrier tells) applies the peak rule to its notes.  The
+ * loop keeps few registers, so HL_PEAK_CTAS_PER_SM CTAs fit an SM and many
+ * loads are in flight. */
+__global__ void __launch_bounds__(HL_PEAK_THREADS, HL_PEAK_CTAS_PER_SM) hl_peaks_kernel(hl_peak_args a)
+{
+    __shared__ unsigned s_note[4 * HL_PEAK_THREADS];   /* step offset << 4 | bins */
+    __shared__ int s_nnote;
     const int q4 = a.Tp >> 2;
+    const int tid = (int)threadIdx.x;
+    if (tid == 0)
+        s_nnote = 0;
+    __syncthreads();
     hl_pdl_begin();
     for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
-        const int2 ch = a.chunks ? a.chunks[c] : make_int2(0, c * HL_PEAK_ROWS);
-        const hl_peak_img im = a.imgs ? a.imgs[ch.x] : a.img0;
-        const int row0 = ch.y;
-        const int nrow = min(HL_PEAK_ROWS, im.R - row0);
-        const int total = nrow * q4;
-        const int4 *src = reinterpret_cast<const int4 *>(im.acc) + (size_t)row0 * q4;
-        /* four 16-byte loads in flight per thread; the common case (no
-         * value above the threshold in the warp) is 16 compares and one
-         * vote, the neighbour reads and the key append run out of line */
-        for (int e0 = 0; e0 < total; e0 += 4 * blockDim.x) {
+        /* the unit: n int4 of image img from (row_lo, int4 column col_lo)
+         * on; only what the loop needs stays in registers */
+        int img = 0, row_lo, col_lo, n, thr;
+        const int4 *src;
+        if (a.chunks) {
+            const int2 ch = a.chunks[c];
+            const hl_peak_img &im = a.imgs[ch.x];
+            img = ch.x;
+            row_lo = ch.y;
+            col_lo = 0;
+            n = (min(ch.y + HL_PEAK_ROWS, im.R) - ch.y) * q4;
+            thr = im.threshold;
+            src = reinterpret_cast<const int4 *>(im.acc) + (size_t)row_lo * q4;
+        } else {
+            /* the host keeps R * Tp / 4 below 2^32 */
+            const unsigned e_lo = (unsigned)c * HL_PEAK_FLAT;
+            row_lo = (int)(e_lo / (unsigned)q4);
+            col_lo = (int)(e_lo - (unsigned)row_lo * (unsigned)q4);
+            n = (int)min((unsigned)HL_PEAK_FLAT, (unsigned)a.img0.R * (unsigned)q4 - e_lo);
+            thr = a.img0.threshold;
+            src = reinterpret_cast<const int4 *>(a.img0.acc) + e_lo;
+        }
+        for (int l0 = 0; l0 < n; l0 += 4 * HL_PEAK_THREADS) {
             int4 v4[4];
 #pragma unroll
             for (int u = 0; u < 4; u++) {
-                const int e = e0 + u * blockDim.x + threadIdx.x;
-                v4[u] = (e < total) ? __ldcs(src + e) : make_int4(0, 0, 0, 0);
+                const int l = l0 + u * HL_PEAK_THREADS + tid;
+                v4[u] = (l < n) ? __ldcs(src + l) : make_int4(0, 0, 0, 0);
             }
-            unsigned cand = 0u;
+            bool noted = false;
 #pragma unroll
             for (int u = 0; u < 4; u++) {
-                cand |= (unsigned)(v4[u].x > im.threshold) << (4 * u);
-                cand |= (unsigned)(v4[u].y > im.threshold) << (4 * u + 1);
-                cand |= (unsigned)(v4[u].z > im.threshold) << (4 * u + 2);
-                cand |= (unsigned)(v4[u].w > im.threshold) << (4 * u + 3);
-            }
-            if (!__any_sync(FULL, cand != 0u))
-                continue;
-            /* rare path: the neighbours of every candidate -- the int4 rows
-             * above and below and the two edge bins -- loaded two groups at
-             * a time, the peak rule (okano_3_0/HoughLine.cu:195-199) from
-             * registers, then one aggregated append for the warp */
-            unsigned peak = 0u;
-#pragma unroll
-            for (int h = 0; h < 4; h += 2) {
-                int4 up[2], dn[2];
-                int wv[2], ev[2];
-#pragma unroll
-                for (int g = 0; g < 2; g++) {
-                    const int u = h + g;
-                    const int e = e0 + u * blockDim.x + threadIdx.x;
-                    const int rl = e / q4, row = row0 + rl, kq = (e - rl * q4) * 4;
-                    const bool any = ((cand >> (4 * u)) & 15u) != 0u;
-                    const int32_t *p = im.acc + (size_t)row * a.Tp + kq;
-                    up[g] = (any && row > 0) ? *reinterpret_cast<const int4 *>(p - a.Tp)
-                                             : make_int4(0, 0, 0, 0);
-                    dn[g] = (any && row + 1 < im.R) ? *reinterpret_cast<const int4 *>(p + a.Tp)
-                                                   : make_int4(0, 0, 0, 0);
-                    wv[g] = (any && kq > 0) ? p[-1] : 0;
-                    ev[g] = (any && kq + 4 < a.T) ? p[4] : 0;
-                }
-#pragma unroll
-                for (int g = 0; g < 2; g++) {
-                    const int u = h + g;
-                    const int e = e0 + u * blockDim.x + threadIdx.x;
-                    const int rl = e / q4, kq = (e - rl * q4) * 4;
-                    const int xv[4] = {v4[u].x, v4[u].y, v4[u].z, v4[u].w};
-                    const int nv[4] = {up[g].x, up[g].y, up[g].z, up[g].w};
-                    const int sv[4] = {dn[g].x, dn[g].y, dn[g].z, dn[g].w};
-#pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        const int k = kq + q;
-                        if (((cand >> (4 * u + q)) & 1u) && k < a.T) {
-                            const int x = xv[q];
-                            const int W = k > 0 ? (q > 0 ? xv[q - 1] : wv[g]) : 0;
-                            const int E = k + 1 < a.T ? (q < 3 ? xv[q + 1] : ev[g]) : 0;
-                            if (x > W && x >= E && x > nv[q] && x >= sv[q])
-                                peak |= 1u << (4 * u + q);
-                        }
-                    }
+                const unsigned bits = (unsigned)(v4[u].x > thr) |
+                                      ((unsigned)(v4[u].y > thr) << 1) |
+                                      ((unsigned)(v4[u].z > thr) << 2) |
+                                      ((unsigned)(v4[u].w > thr) << 3);
+                if (bits) {
+                    s_note[atomicAdd(&s_nnote, 1)] =
+                        ((unsigned)(u * HL_PEAK_THREADS + tid) << 4) | bits;
+                    noted = true;
                 }
             }
-            /* append: one atomic per warp, each lane writes its keys */
-            const int lane = threadIdx.x & 31;
-            const int cnt = __popc(peak);
-            int incl = cnt;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int t = __shfl_up_sync(FULL, incl, o);
-                if (lane >= o)
-                    incl += t;
-            }
-            const int wtot = __shfl_sync(FULL, incl, 31);
-            if (wtot == 0)
-                continue;
-            int base = 0;
-            if (lane == 31)
-                base = atomicAdd(im.ncand, wtot);
-            base = __shfl_sync(FULL, base, 31) + incl - cnt;
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-                if (!((peak >> (4 * u)) & 15u))
-                    continue;
-                const int e = e0 + u * blockDim.x + threadIdx.x;
-                const int rl = e / q4;
-                const int row = row0 + rl, kq = (e - rl * q4) * 4;
-                const int xv[4] = {v4[u].x, v4[u].y, v4[u].z, v4[u].w};
-#pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    if ((peak >> (4 * u + q)) & 1u) {
-                        const unsigned idx = (unsigned)row * (unsigned)a.T + (unsigned)(kq + q);
-                        if (base < im.cap)
-                            im.keys[base] = ((unsigned long long)(unsigned)xv[q] << 32) |
-                                            (unsigned)(~idx);
-                        else
-                            atomicOr(a.status, HL_ST_CAND_OVERFLOW);
-                        base++;
-                    }
+            if (__syncthreads_or(noted)) {
+                const int32_t *acc = a.chunks ? a.imgs[img].acc : a.img0.acc;
+                unsigned long long *keys = a.chunks ? a.imgs[img].keys : a.img0.keys;
+                int *ncand = a.chunks ? a.imgs[img].ncand : a.img0.ncand;
+                const int R = a.chunks ? a.imgs[img].R : a.img0.R;
+                const int cap = a.chunks ? a.imgs[img].cap : a.img0.cap;
+                const int nn = s_nnote;
+                /* a note per bin of the noted int4 */
+                for (int j = tid; j < 4 * nn; j += HL_PEAK_THREADS) {
+                    const unsigned e = s_note[j >> 2];
+                    const int q = j & 3;
+                    if (!((e >> q) & 1u))
+                        continue;
+                    const int t = col_lo + l0 + (int)(e >> 4);
+                    const int dr = t / q4;
+                    const int row = row_lo + dr, k = (t - dr * q4) * 4 + q;
+                    if (k < a.T)
+                        peak_bin(acc + (size_t)row * a.Tp + k, keys, ncand, R, cap, a.T, a.Tp,
+                                 row, k, a.status);
                 }
+                __syncthreads();
+                if (tid == 0)
+                    s_nnote = 0;
+                __syncthreads();
             }
         }
     }
@@ -160,8 +153,8 @@ cudaError_t hl_launch_peaks(const hl_peak_args *a, cudaStream_t s)
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int blocks = std::max(1, std::min(a->nchunks, sms * 8));
-    return hl_launch_pdl(hl_peaks_kernel, dim3(blocks), dim3(256), 0, s, false, *a);
+    const int blocks = std::max(1, std::min(a->nchunks, sms * HL_PEAK_CTAS_PER_SM));
+    return hl_launch_pdl(hl_peaks_kernel, dim3(blocks), dim3(HL_PEAK_THREADS), 0, s, false, *a);
 }
 
 /* ------------------------------------------------------------------ */
@@ -177,10 +170,7 @@ struct FinSmem {
      * on consecutive candidates hit different banks */
     unsigned pred[FIN_CHUNK][FIN_CHUNK / 32 + 1];
     unsigned removed[FIN_CHUNK / 32];
-    unsigned dec[FIN_CHUNK / 32];    /* decided candidates */
-    unsigned alive[FIN_CHUNK / 32];  /* decided survivors */
-    unsigned ndec[FIN_CHUNK / 32];
-    unsigned nalive[FIN_CHUNK / 32];
+    unsigned alive[FIN_CHUNK / 32];  /* kept candidates */
     int surv[FIN_CHUNK];
     float sang[FIN_SCACHE];
     int sdist[FIN_SCACHE];
@@ -245,19 +235,22 @@ __device__ __forceinline__ void decode(unsigned long long key, int T,
  * j < i are built: entry (i, wd) for 32 wd < i, enumerated word by word.
  * Four adjacent threads share an entry (8 tests each, OR-ed by shuffles);
  * the threads of a warp mostly share wd and read the word's candidates with
- * broadcast loads.  Threads t0, t0 + step, ... (step a multiple of 32) take
- * the entries; pred may be another CTA's shared memory of the cluster. */
+ * broadcast loads.  Of nsub CTAs (a cluster) CTA sub takes every nsub-th
+ * entry, so the CTAs share the work evenly; pred may be another CTA's
+ * shared memory of the cluster. */
 __device__ __forceinline__ void build_pred(const FinSmem &sm, int m, const hl_final_args &a,
-                                           int t0, int step,
+                                           int sub, int nsub,
                                            unsigned (*pred)[FIN_CHUNK / 32 + 1])
 {
     const int W = (m + 31) >> 5;
     int nent = 0;
     for (int wd = 0; wd < W; wd++)
         nent += max(0, m - 32 * wd - 1);
-    const int span = (4 * nent + 31) & ~31;
-    for (int e = t0; e < span; e += step) {
-        const int q = e & 3, en = e >> 2;
+    const int q = threadIdx.x & 3;
+    const int estep = (int)(blockDim.x >> 2) * nsub;
+    /* a whole number of passes: every lane of a warp runs the same trips */
+    const int span = (nent + estep - 1) / estep * estep;
+    for (int en = (int)(threadIdx.x >> 2) * nsub + sub; en < span; en += estep) {
         unsigned bits = 0u;
         int i = 0, wd = 0, jn = 0;
         if (en < nent) {
@@ -352,55 +345,45 @@ __device__ int greedy_chunk(FinSmem &sm, const hl_final_img &im, int m, int K, i
     const int W = (m + 31) >> 5;
     /* The greedy pass of okano_3_0/HoughLine.cu:900-927 keeps candidate i
      * iff it was not removed by an earlier chunk and no earlier kept
-     * candidate is similar to it.  Resolved in rounds: an undecided
-     * candidate with a kept predecessor is dropped, one whose
-     * predecessors are all decided (none kept) is kept.  Each round
-     * decides at least the first undecided candidate; in practice a few
-     * rounds decide them all. */
+     * candidate is similar to it.  One warp resolves it a 32-candidate word
+     * at a time, in order: lane j of word w (candidate i = 32 w + j) is
+     * dropped by a kept candidate of an earlier word (its predecessor words
+     * against the kept bits, all loads independent), then the word is
+     * settled in rounds -- a candidate whose earlier in-word predecessors
+     * are all decided is kept iff none of them is kept; each round settles
+     * at least the lowest undecided lane, in practice one or two rounds
+     * settle the word. */
     if (tid < 32) {
-        unsigned d = (tid < W) ? sm.removed[tid] : 0xffffffffu;
-        if (tid == W - 1 && (m & 31))
-            d |= ~((1u << (m & 31)) - 1u);
-        sm.dec[tid] = d;
-        sm.alive[tid] = 0u;
-        sm.ndec[tid] = 0u;
-        sm.nalive[tid] = 0u;
+        const int lane = tid;
+        if (lane >= W)
+            sm.alive[lane] = 0u;   /* words past the chunk keep nobody */
+        __syncwarp();
+        for (int w = 0; w < W; w++) {
+            const int i = 32 * w + lane;
+            const bool valid = i < m;
+            unsigned kill = valid ? (sm.removed[w] >> lane) & 1u : 1u;
+            unsigned pin = 0u;
+            if (valid) {
+                for (int v = 0; v < w; v++)
+                    kill |= sm.pred[i][v] & sm.alive[v];
+                /* the in-word entry holds bits below the lane only (none
+                 * was built for lane 0) */
+                pin = lane ? sm.pred[i][w] & ((1u << lane) - 1u) : 0u;
+            }
+            unsigned und = __ballot_sync(FULL, kill == 0u);
+            unsigned alive = 0u;
+            while (und) {
+                const bool in = (und >> lane) & 1u;
+                const unsigned ready = __ballot_sync(FULL, in && !(pin & und));
+                alive |= __ballot_sync(FULL, ((ready >> lane) & 1u) && !(pin & alive));
+                und &= ~ready;
+            }
+            if (lane == 0)
+                sm.alive[w] = alive;
+            __syncwarp();
+        }
     }
     __syncthreads();
-    for (int round = 0; round < m; round++) {
-        for (int i = tid; i < m; i += blockDim.x) {
-            const int iw = i >> 5;
-            const unsigned ib = 1u << (i & 31);
-            if (sm.dec[iw] & ib)
-                continue;
-            bool all = true, kill = false;
-            for (int w = 0; w < ((i + 31) >> 5); w++) {
-                const unsigned pw = sm.pred[i][w];
-                all = all && !(pw & ~sm.dec[w]);
-                kill = kill || (pw & sm.alive[w]);
-            }
-            if (kill) {
-                atomicOr(&sm.ndec[iw], ib);
-            } else if (all) {
-                atomicOr(&sm.ndec[iw], ib);
-                atomicOr(&sm.nalive[iw], ib);
-            }
-        }
-        __syncthreads();
-        if (tid < 32) {
-            const unsigned d = sm.dec[tid] | sm.ndec[tid];
-            sm.dec[tid] = d;
-            sm.alive[tid] |= sm.nalive[tid];
-            sm.ndec[tid] = 0u;
-            sm.nalive[tid] = 0u;
-            const bool done = __all_sync(FULL, d == 0xffffffffu);
-            if (tid == 0)
-                sm.misc[4] = done;
-        }
-        __syncthreads();
-        if (sm.misc[4])
-            break;
-    }
     /* survivors in rank order, at most room of them */
     {
         const int room = K - S;
@@ -568,7 +551,7 @@ __device__ void finalize_cta(const hl_final_args &a, const hl_final_img &im, flo
                 atomicOr(&sm.removed[i >> 5], 1u << (i & 31));
         }
         __syncthreads();
-        build_pred(sm, m, a, tid, blockDim.x, sm.pred);
+        build_pred(sm, m, a, 0, 1, sm.pred);
         __syncthreads();
         S += greedy_chunk(sm, im, m, K, S);
     }
@@ -639,7 +622,7 @@ hl_finalize_cluster_kernel(hl_final_args a, float scale)
         for (int i = tid; i < 32; i += blockDim.x)
             sm.removed[i] = 0u;
     __syncthreads();
-    build_pred(sm, m, a, rank * (int)blockDim.x + tid, FIN_CLUSTER * (int)blockDim.x,
+    build_pred(sm, m, a, rank, FIN_CLUSTER,
                reinterpret_cast<unsigned (*)[FIN_CHUNK / 32 + 1]>(
                    cl.map_shared_rank(&sm.pred[0][0], 0)));
     cl.sync();

@@ -500,14 +500,15 @@ hl_vote_kernel(hl_vote_args a)
     const int batch = HL_VOTE_PPW * ncons;
     const int nslices = a.Tp / HL_SLICE;
 
-    hl_pdl_begin();
-    /* the block and its dump row start at zero; after each item the
-     * consumers clear what it used */
+    /* the block and its dump row start at zero (before the wait for the
+     * previous launch: shared memory only); after each item the consumers
+     * clear what it used */
     {
         int4 *z = reinterpret_cast<int4 *>(s_acc);
         for (int i = tid; i < (a.win_rows + 1) * (HL_SLICE / 4); i += nthr)
             z[i] = make_int4(0, 0, 0, 0);
     }
+    hl_pdl_begin();
     if (tid == 0) {
         for (int i = 0; i < HL_VOTE_SLOTS; i++) {
             mbar_init(&sm.full[i], 1);
