@@ -567,7 +567,7 @@ static int vote_items(hl_handle *h, int w, int hh, int rho_min, int R,
             const int w0 = (b / slices) * rows, k0 = (b % slices) * HL_SLICE;
             const long long off = (long long)w0 * h->Tp + k0;
             slot0[b] = nslots;
-            merge.push_back({off / 4, std::min(rows, R - w0), k0, nslots, pieces[b], {0, 0}});
+            merge.push_back({off / 4, std::min(rows, R - w0), k0, nslots, pieces[b], w0, 0, {0, 0}});
             nslots += pieces[b];
         }
         const int n = (int)parts.size();
@@ -631,6 +631,19 @@ static int ensure_image(hl_handle *h, const hl_geom &g, int w, int hh)
                                 cap2 / sizeof(int));
     }
     return HL_NO_ERROR;
+}
+
+/* Peak candidates (batches): the list and its room; a threshold that only
+ * peaks-to-be clear leaves a few hundred per image, and past the room the
+ * peak pass scans the accumulators instead.  A null list: no noting. */
+static hl_cand_list cand_list(unsigned long long *e, size_t cap_bytes, int *count)
+{
+    hl_cand_list c;
+    c.e = e;
+    c.count = count;
+    c.cap = (int)std::min(cap_bytes / sizeof(unsigned long long), (size_t)0x7fffffff);
+    c.pad = 0;
+    return c;
 }
 
 static int ensure_acc(hl_handle *h, int R, int linesmax)
@@ -742,7 +755,7 @@ static int run_ab(hl_handle *h, const hl_roi &roi, const hl_geom &g,
     va.img0.h = roi.h;
     va.img0.rho_min = g.rho_min;
     va.img0.R = g.numrho;
-    va.img0.pad = 0;
+    va.img0.threshold = h->p.threshold;
     va.img0.acc = h->d_acc;
     va.cosv = h->d_cos;
     va.sinv = h->d_sin;
@@ -753,6 +766,9 @@ static int run_ab(hl_handle *h, const hl_roi &roi, const hl_geom &g,
     va.irho = (float)(1.0 / h->p.derho);   /* okano_3_0/HoughLine.cu:107 */
     va.status = h->d_counters + 1;
     va.part16 = hl_part16_ok(h->p.derho, roi.w, roi.h);
+    /* one image: no candidate list (the peak pass scans the accumulator,
+     * which is still in L2; noting measured slower on the whole step) */
+    va.cand = cand_list(nullptr, 0, nullptr);
     /* persistent CTAs: as many as fit (one per SM at 1024 threads) */
     const size_t smem = hl_vote_smem_bytes(va.win_rows);
     const int per_sm = std::max(1, std::min(2048 / threads,
@@ -800,6 +816,9 @@ static int run_ab(hl_handle *h, const hl_roi &roi, const hl_geom &g,
         ma.regs = h->d_merge;
         ma.nreg = h->order_nmerge;
         ma.part16 = va.part16;
+        ma.pimgs = nullptr;
+        ma.thr0 = h->p.threshold;
+        ma.cand = va.cand;
         CK(hl_launch_merge(&ma, va.win_rows, s));
         (*launches)++;
     }
@@ -856,6 +875,7 @@ static int run_c(hl_handle *h, const hl_geom &g, int linesmax,
     pa.T = h->T;
     pa.Tp = h->Tp;
     pa.status = h->d_counters + 1;
+    pa.cand = cand_list(nullptr, 0, nullptr);
     CK(hl_launch_peaks(&pa, s));
     (*launches)++;
     prof_mark(h, 3, s);
@@ -1323,7 +1343,8 @@ extern "C" int hl_real_line(hl_handle *h, const hl_image_desc *img, int x1,
 /* ==================================================================== */
 
 /* Counters of a batch call, cleared at its start: [0] compaction ticket,
- * [1] vote work counter, [2] status word, [3] total points. */
+ * [1] vote work counter, [2] status word, [3] total points, [8] noted peak
+ * candidates. */
 #define BW_NCNT 16
 
 struct hl_batch_ws {
@@ -1337,6 +1358,8 @@ struct hl_batch_ws {
     size_t cap_acc;
     unsigned long long *d_keys;
     size_t cap_keys;
+    unsigned long long *d_cand;    /* noted peak candidates; counter d_cnt[8] */
+    size_t cap_cand;
     int4 *d_scratch;               /* split parts' slots: win_rows x HL_SLICE */
     size_t cap_scratch;
     unsigned *d_tmask;             /* every image's admitted-tile masks */
@@ -1400,7 +1423,7 @@ static void batch_ws_free(hl_batch_ws *b)
 {
     if (!b)
         return;
-    void *dp[] = {b->d_pts, b->d_state, b->d_tile_off, b->d_acc, b->d_keys,
+    void *dp[] = {b->d_pts, b->d_state, b->d_tile_off, b->d_acc, b->d_keys, b->d_cand,
                   b->d_ncand, b->d_cnt, b->d_tab, b->d_lines, b->d_counts,
                   b->d_scratch, b->d_tmask};
     for (void *q : dp)
@@ -1597,7 +1620,7 @@ static int batch_plan(hl_handle *h, hl_batch_ws *b, const hl_image_desc *imgs,
             const long long off = (long long)b->acc_off[im] + (long long)w0 * h->Tp + k0;
             slot0[q] = nslots;
             b->merge.push_back({off / 4, std::min(rows, b->R[im] - w0), k0, nslots, pieces[q],
-                                {0, 0}});
+                                w0, im, {0, 0}});
             nslots += pieces[q];
         }
         b->items.resize(parts.size());
@@ -1640,6 +1663,8 @@ static int batch_plan(hl_handle *h, hl_batch_ws *b, const hl_image_desc *imgs,
         (rc = grow((void **)&b->d_tile_off, &b->cap_tile_off,
                    sizeof(int) * ((size_t)b->ntiles + 1))) != HL_NO_ERROR ||
         (rc = grow((void **)&b->d_acc, &b->cap_acc, sizeof(int32_t) * b->acc_ints)) != HL_NO_ERROR ||
+        (rc = grow((void **)&b->d_cand, &b->cap_cand,
+                   sizeof(unsigned long long) * (65536 + b->acc_ints / 128))) != HL_NO_ERROR ||
         (rc = grow((void **)&b->d_keys, &b->cap_keys,
                    sizeof(unsigned long long) * b->nkeys)) != HL_NO_ERROR ||
         (rc = grow((void **)&b->d_tab, &b->cap_tab, b->tab_bytes)) != HL_NO_ERROR ||
@@ -1690,7 +1715,7 @@ static int batch_plan(hl_handle *h, hl_batch_ws *b, const hl_image_desc *imgs,
         vi[i].rho_min = g.rho_min;
         vi[i].R = g.numrho;
         vi[i].nwin = b->nwin[i];
-        vi[i].pad = 0;
+        vi[i].threshold = thr ? thr[i] : h->p.threshold;
         vi[i].tmask = b->d_tmask + b->tmask_off[i];
         vi[i].acc = b->d_acc + b->acc_off[i];
         pi[i].acc = b->d_acc + b->acc_off[i];
@@ -1766,6 +1791,8 @@ static int batch_enqueue_vote_peaks(hl_handle *h, hl_batch_ws *b, cudaStream_t s
     va.nitems = b->nitems;
     va.scratch = b->d_scratch;
     va.part16 = b->part16;
+    /* the counter is cleared with the others at the start of every call */
+    va.cand = cand_list(b->d_cand, b->cap_cand, b->d_cnt + 8);
     va.work = reinterpret_cast<unsigned *>(b->d_cnt + 1);
     va.work_base = 0;
     CK(hl_launch_vote(&va, b->threads, b->grid, s));
@@ -1779,6 +1806,9 @@ static int batch_enqueue_vote_peaks(hl_handle *h, hl_batch_ws *b, cudaStream_t s
         ma.regs = reinterpret_cast<const hl_merge_region *>(dt + b->off_merge);
         ma.nreg = (int)b->merge.size();
         ma.part16 = b->part16;
+        ma.pimgs = reinterpret_cast<const hl_peak_img *>(dt + b->off_pimg);
+        ma.thr0 = 0;
+        ma.cand = va.cand;
         CK(hl_launch_merge(&ma, b->win_rows, s));
     }
     prof_mark(h, 2, s);
@@ -1791,6 +1821,7 @@ static int batch_enqueue_vote_peaks(hl_handle *h, hl_batch_ws *b, cudaStream_t s
     pa.T = h->T;
     pa.Tp = h->Tp;
     pa.status = b->d_cnt + 2;
+    pa.cand = va.cand;
     CK(hl_launch_peaks(&pa, s));
     prof_mark(h, 3, s);
     return HL_NO_ERROR;
@@ -1886,6 +1917,7 @@ static int batch_run_ws(hl_handle *h, hl_batch_ws **pb, const hl_image_desc *img
         gk.push_back((long long)(uintptr_t)b->d_keys);
         gk.push_back((long long)(uintptr_t)b->d_tmask);
         gk.push_back((long long)(uintptr_t)b->d_scratch);
+        gk.push_back((long long)(uintptr_t)b->d_cand);
         if (!b->gexec || gk != b->gkey) {
             if (b->gexec) {
                 cudaGraphExecDestroy(b->gexec);

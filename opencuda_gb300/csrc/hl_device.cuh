@@ -202,4 +202,33 @@ __device__ __forceinline__ void diag_point(float x, float y, const DiagTab &t, f
     }
 }
 
+
+/* Notes the bins of one int4 of counts whose bit is set in bits (bin
+ * idx0 + j for bit j, j < 4) as peak candidates of image img; once the list
+ * is full (the peak pass then scans every accumulator) a bin costs one
+ * load. */
+__device__ __forceinline__ void note_cands(const hl_cand_list &c, int img, unsigned idx0,
+                                           unsigned bits)
+{
+    if (*(volatile int *)c.count >= c.cap)
+        return;
+    while (bits) {
+        const int j = __ffs(bits) - 1;
+        bits &= bits - 1;
+        const int pos = atomicAdd(c.count, 1);
+        if (pos < c.cap)
+            c.e[pos] = ((unsigned long long)(unsigned)img << 32) | (idx0 + (unsigned)j);
+    }
+}
+
+/* bits of the bins of v above thr, bins kq + j >= T (padding) left out */
+__device__ __forceinline__ unsigned above4(const int4 &v, int thr, int kq, int T)
+{
+    unsigned b = (unsigned)(v.x > thr) | ((unsigned)(v.y > thr) << 1) |
+                 ((unsigned)(v.z > thr) << 2) | ((unsigned)(v.w > thr) << 3);
+    if (kq + 3 >= T)
+        b &= (T > kq) ? (1u << (T - kq)) - 1u : 0u;
+    return b;
+}
+
 #endif

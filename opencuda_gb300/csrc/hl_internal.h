@@ -91,9 +91,22 @@ typedef struct hl_vote_img {
     int w, h;                 /* ROI size (tile clipping) */
     int rho_min, R;
     int nwin;                 /* rho windows of win_rows rows */
-    int pad;
+    int threshold;            /* peak threshold: bins above it are noted */
     int32_t *acc;             /* [R][Tp] */
 } hl_vote_img;
+
+/* Peak candidates of a launch: every accumulator bin above its image's
+ * threshold, noted as image << 32 | (row * T + theta) when its final count
+ * is stored (the vote's block store, the merge of a split block).  A
+ * counter past cap means some were not noted: the peak pass then scans
+ * every accumulator instead.  The counter is zero at the vote's start (the
+ * batch clears it with its other counters); e == NULL: nothing is noted. */
+typedef struct hl_cand_list {
+    unsigned long long *e;
+    int *count;               /* cleared by the compaction launch */
+    int cap;
+    int pad;
+} hl_cand_list;
 
 typedef struct hl_vote_args {
     const hl_vote_img *imgs;  /* per image, or NULL: the one image img0 */
@@ -119,6 +132,7 @@ typedef struct hl_vote_args {
     /* nonzero: a slot holds 16-bit counts (two per word; the host sets it
      * when no bin can reach 2^16 votes, see hl_part16_ok), half the bytes */
     int part16;
+    hl_cand_list cand;
 } hl_vote_args;
 
 /* A split vote block: its accumulator region (rows x 8 int4 from off4, rows
@@ -128,8 +142,12 @@ typedef struct hl_merge_region {
     long long off4;
     int rows, k0;
     int slot0, nparts;
+    int w0;                   /* first row of the block in its image */
+    int img;                  /* its image */
     int pad[2];
 } hl_merge_region;
+
+struct hl_peak_img;
 
 typedef struct hl_merge_args {
     int4 *acc;
@@ -140,6 +158,10 @@ typedef struct hl_merge_args {
     const hl_merge_region *regs;
     int nreg;
     int part16;               /* slots hold 16-bit counts (hl_vote_args) */
+    /* the peak threshold of region r: pimgs[r.img].threshold, or thr0 */
+    const struct hl_peak_img *pimgs;
+    int thr0;
+    hl_cand_list cand;
 } hl_merge_args;
 
 /* Can a split part's counts be kept in 16 bits?  A bin of one rho bin width
@@ -198,6 +220,9 @@ typedef struct hl_peak_args {
     int nchunks;
     int T, Tp;
     int *status;
+    /* the bins above the threshold, noted by the vote and the merge; when
+     * they all fit, only they are tested (no scan of the accumulators) */
+    hl_cand_list cand;
 } hl_peak_args;
 
 /* One image of a finalize launch (one CTA per image). */

@@ -56,8 +56,11 @@ __device__ __forceinline__ void peak_bin(const int32_t *p, unsigned long long *k
     }
 }
 
-/* One read of every accumulator at the memory system's speed.  Work units
- * are taken grid-stride: with several images (chunks != NULL) a unit is
+/* The peak rule for every bin above the threshold.  When the vote and the
+ * merge noted all of them (the usual case: they are rare), each thread
+ * takes noted bins and reads only their neighbours -- no accumulator is
+ * read as a whole.  Otherwise one read of every accumulator at the memory
+ * system's speed.  Work units are taken grid-stride: with several images (chunks != NULL) a unit is
  * HL_PEAK_ROWS rows of one image, with one image it is HL_PEAK_FLAT
  * consecutive int4 of its accumulator (a unit need not start a row: each
  * int4 finds its row).  A step of a unit is four int4 per thread, loaded at
@@ -76,6 +79,23 @@ __global__ void __launch_bounds__(HL_PEAK_THREADS, HL_PEAK_CTAS_PER_SM) hl_peaks
         s_nnote = 0;
     __syncthreads();
     hl_pdl_begin();
+    if (a.cand.e) {
+        const int nc = *a.cand.count;
+        if (nc <= a.cand.cap) {
+            for (int j = blockIdx.x * HL_PEAK_THREADS + tid; j < nc;
+                 j += gridDim.x * HL_PEAK_THREADS) {
+                const unsigned long long e = a.cand.e[j];
+                const int img = (int)(e >> 32);
+                const unsigned idx = (unsigned)e;
+                const int row = (int)(idx / (unsigned)a.T), k = (int)(idx % (unsigned)a.T);
+                const hl_peak_img &im = a.chunks ? a.imgs[img] : a.img0;
+                if (row < im.R)
+                    peak_bin(im.acc + (size_t)row * a.Tp + k, im.keys, im.ncand, im.R, im.cap,
+                             a.T, a.Tp, row, k, a.status);
+            }
+            return;
+        }
+    }
     for (int c = blockIdx.x; c < a.nchunks; c += gridDim.x) {
         /* the unit: n int4 of image img from (row_lo, int4 column col_lo)
          * on; only what the loop needs stays in registers */

@@ -179,6 +179,8 @@ struct VoteSeg {
     int b_lo, b_hi;                    /* this part's batches of them */
     int first, last;                   /* first / last segment of the item */
     float c[HL_SLICE], s[HL_SLICE];    /* cos / sin of the slice's thetas */
+    int img;                           /* the image (in the tail padding: the
+                                          layout measured fastest is kept) */
 };
 
 struct VoteSmem {
@@ -258,6 +260,7 @@ __device__ __forceinline__ bool cons_sync(VoteSmem &sm, unsigned &par,
  * segment and streams its batches into the ring.  It runs ahead of the
  * consumers by up to the ring's depth, so the next item's setup and first
  * copies overlap the current item's last votes. */
+template <bool NOTE>
 __device__ __forceinline__ void vote_producer(const hl_vote_args &a,
                                               VoteSmem &sm, int batch)
 {
@@ -404,6 +407,8 @@ __device__ __forceinline__ void vote_producer(const hl_vote_args &a,
                 g.part = part;
                 g.nparts = nparts;
                 g.slot = it.z;
+                if (NOTE)
+                    g.img = a.imgs ? (int)((unsigned)it.x >> 16) : 0;
                 g.rho_min = im.rho_min;
                 g.R = im.R;
                 g.total = total;
@@ -486,7 +491,9 @@ __device__ __forceinline__ void vote_producer(const hl_vote_args &a,
     }
 }
 
-template <bool UNIT>
+/* NOTE: note the bins above the threshold as peak candidates (a.cand);
+ * without, the code is the plain vote and store */
+template <bool UNIT, bool NOTE>
 __global__ void __launch_bounds__(1024, 1)
 hl_vote_kernel(hl_vote_args a)
 {
@@ -526,7 +533,7 @@ hl_vote_kernel(hl_vote_args a)
      * consumers meet on mbarriers, every wait bounded */
     __syncthreads();
     if (warp == 0) {
-        vote_producer(a, sm, batch);
+        vote_producer<NOTE>(a, sm, batch);
         return;
     }
 
@@ -544,6 +551,7 @@ hl_vote_kernel(hl_vote_args a)
     unsigned lrows = 0;
     int32_t *acc_g = nullptr;
     int nparts = 1, pslot = 0;
+    int img = 0;   /* the item's image (noting candidates only) */
     while (true) {
         const int ds = (int)(nseg & 1u);
         if (!mbar_wait_ab(&sm.seg_full[ds], (nseg >> 1) & 1u, &sm.abort, a.status))
@@ -570,6 +578,8 @@ hl_vote_kernel(hl_vote_args a)
             acc_g = g.acc;
             nparts = g.nparts;
             pslot = g.slot;
+            if (NOTE)
+                img = g.img;
         }
         __syncwarp();
         if (lane == 0)
@@ -605,14 +615,17 @@ hl_vote_kernel(hl_vote_args a)
         if (!cons_sync(sm, cpar, a.status))
             return;
         /* a whole block goes to acc (the padding columns, thetas >= T,
-         * hold dumped votes and are stored as zero), a part of a split
-         * block to its scratch slot as it is; each thread stores and
+         * hold dumped votes and are stored as zero; bins above the
+         * image's threshold are noted as peak candidates), a part of a
+         * split block to its scratch slot as it is; each thread stores and
          * clears the same elements */
         const int tp4 = a.Tp >> 2;
         const int n4 = rows * (HL_SLICE / 4);
         int4 *dst4 = nparts == 1 ? reinterpret_cast<int4 *>(acc_g) + (size_t)w0 * tp4 + (k0 >> 2)
                                  : a.scratch + (size_t)pslot * hl_slot4(a.win_rows, a.part16);
         const bool pack = nparts > 1 && a.part16;
+        /* the image's peak threshold, read once (noting candidates only) */
+        const int thr = NOTE ? (a.imgs ? a.imgs[img].threshold : a.img0.threshold) : 0;
         for (int i = ctid; i < n4 + HL_SLICE / 4; i += nct) {
             if (i < n4) {
                 const int rr = i >> 3, q = i & 7;
@@ -626,6 +639,14 @@ hl_vote_kernel(hl_vote_args a)
                         if (kq + 3 >= a.T) v.w = 0;
                     }
                     dst4[(size_t)rr * tp4 + q] = v;
+                    if (NOTE) {
+                        const unsigned bits = above4(v, thr, k0 + 4 * q, a.T);
+                        if (bits)
+                            note_cands(a.cand, img,
+                                       (unsigned)(w0 + rr) * (unsigned)a.T +
+                                           (unsigned)(k0 + 4 * q),
+                                       bits);
+                    }
                 } else if (pack) {
                     reinterpret_cast<int2 *>(dst4)[i] =
                         make_int2((v.x & 0xffff) | (v.y << 16), (v.z & 0xffff) | (v.w << 16));
@@ -641,10 +662,12 @@ hl_vote_kernel(hl_vote_args a)
 }
 
 /* The blocks voted in parts: block region = sum of its parts' scratch
- * slots, the padding columns (thetas >= T) stored as zero.  A
+ * slots, the padding columns (thetas >= T) stored as zero, the bins above
+ * the image's threshold noted as peak candidates.  A
  * thread takes 16 bytes of every part of its region (grid.y = region): two
  * output int4 when the parts hold 16-bit counts, one otherwise; every slot
  * is read once, from L2 where the vote launch just wrote it. */
+template <bool NOTE>
 __global__ void __launch_bounds__(256)
 hl_merge_kernel(hl_merge_args a)
 {
@@ -731,6 +754,13 @@ hl_merge_kernel(hl_merge_args a)
             if (kq + 3 >= a.T) v.w = 0;
         }
         a.acc[r.off4 + (size_t)rr * a.pitch4 + q] = v;
+        if (NOTE) {
+            const unsigned bits =
+                above4(v, a.pimgs ? a.pimgs[r.img].threshold : a.thr0, r.k0 + 4 * q, a.T);
+            if (bits)
+                note_cands(a.cand, r.img,
+                           (unsigned)(r.w0 + rr) * (unsigned)a.T + (unsigned)(r.k0 + 4 * q), bits);
+        }
     }
 }
 
@@ -741,8 +771,11 @@ cudaError_t hl_launch_merge(const hl_merge_args *a, int max_rows, cudaStream_t s
     const int per_thread = a->part16 ? 2 : 1;   /* output int4 per thread */
     const unsigned gx =
         (unsigned)((max_rows * (HL_SLICE / 4) / per_thread + 255) / 256);
-    return hl_launch_pdl(hl_merge_kernel, dim3(gx, (unsigned)a->nreg), dim3(256), 0, s, false,
-                         *a);
+    if (a->cand.e)
+        return hl_launch_pdl(hl_merge_kernel<true>, dim3(gx, (unsigned)a->nreg), dim3(256), 0, s,
+                             false, *a);
+    return hl_launch_pdl(hl_merge_kernel<false>, dim3(gx, (unsigned)a->nreg), dim3(256), 0, s,
+                         false, *a);
 }
 
 cudaError_t hl_launch_tile_masks(const hl_vote_args *a, int nimg, size_t max_words,
@@ -757,28 +790,29 @@ cudaError_t hl_launch_tile_masks(const hl_vote_args *a, int nimg, size_t max_wor
     return cudaGetLastError();
 }
 
+template <bool UNIT, bool NOTE>
+static cudaError_t launch_vote_t(const hl_vote_args *a, int threads, int grid, size_t smem,
+                                 cudaStream_t s)
+{
+    const cudaError_t e = cudaFuncSetAttribute(hl_vote_kernel<UNIT, NOTE>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    return hl_launch_pdl(hl_vote_kernel<UNIT, NOTE>, dim3(grid), dim3(threads), smem, s, false,
+                         *a);
+}
+
 cudaError_t hl_launch_vote(const hl_vote_args *a, int threads, int grid,
                            cudaStream_t s)
 {
     const size_t smem = hl_vote_smem_bytes(a->win_rows);
-    cudaError_t e;
-    if (a->irho == 1.0f) {
-        e = cudaFuncSetAttribute(hl_vote_kernel<true>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem);
-        if (e != cudaSuccess)
-            return e;
-        return hl_launch_pdl(hl_vote_kernel<true>, dim3(grid), dim3(threads), smem, s, false,
-                             *a);
-    } else {
-        e = cudaFuncSetAttribute(hl_vote_kernel<false>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem);
-        if (e != cudaSuccess)
-            return e;
-        return hl_launch_pdl(hl_vote_kernel<false>, dim3(grid), dim3(threads), smem, s, false,
-                             *a);
-    }
+    const bool note = a->cand.e != nullptr;
+    if (a->irho == 1.0f)
+        return note ? launch_vote_t<true, true>(a, threads, grid, smem, s)
+                    : launch_vote_t<true, false>(a, threads, grid, smem, s);
+    return note ? launch_vote_t<false, true>(a, threads, grid, smem, s)
+                : launch_vote_t<false, false>(a, threads, grid, smem, s);
 }
 
 size_t hl_vote_points_smem_bytes(int win_rows)

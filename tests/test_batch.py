@@ -180,3 +180,26 @@ def test_tiled_cells_one_launch(hl_mod):
             want, _, _ = O.houghline(img[y1:y2, x1:x2], c, s, math.pi / 180, 1.0, 40,
                                      hl.getThresAng(), hl.getThresDis(), 24)
             assert got == want
+
+
+def test_batch_peak_candidates_and_their_overflow(hl_mod):
+    """The batched vote and merge note every bin above its image's
+    threshold, and the peak pass then tests only those; past the list's
+    room it scans every accumulator.  A 4096 x 4096 image (split blocks,
+    merged by the merge launch) with uneven ones, first with thresholds that
+    only peaks-to-be clear, then with one image at threshold 0 (millions of
+    bins: the list overflows), give hl_plain's lines image by image."""
+    HoughLine, Image = hl_mod
+    imgs = [cases.synth(2, 1234, 0)] + [cases.synth(3, 77, i) for i in range(3)]
+    dev = [Image.from_host(im) for im in imgs]
+    hl = HoughLine(detheta=DEG05)
+    ref = HoughLine(detheta=DEG05)
+    for thr in ([300] + [int(0.15 * max(im.shape)) for im in imgs[1:]],
+                [300, 0] + [int(0.15 * max(im.shape)) for im in imgs[2:]]):
+        rc, res = hl.houghLineBatch(dev, 24, thr)
+        assert rc == 0 and len(res) == len(imgs)
+        for i in range(len(imgs)):
+            ref.setThreshold(thr[i])
+            rc, single = ref.houghLine(dev[i], None, 24)
+            assert rc == 0
+            assert [l.astuple() for l in res[i]] == [l.astuple() for l in single], (thr, i)
