@@ -207,8 +207,9 @@ typedef struct hl_peak_img {
 /* rows of an accumulator one peak-pass chunk covers (several images), int4
  * of a unit of one image's accumulator, threads of a peak-pass CTA */
 #define HL_PEAK_ROWS 16
-#define HL_PEAK_FLAT 1024
 #define HL_PEAK_THREADS 256
+#define HL_PEAK_LOADS 4           /* 16-byte loads in flight per thread */
+#define HL_PEAK_FLAT (HL_PEAK_LOADS * HL_PEAK_THREADS)
 #define HL_PEAK_CTAS_PER_SM 6
 
 typedef struct hl_peak_args {

@@ -63,15 +63,15 @@ __device__ __forceinline__ void peak_bin(const int32_t *p, unsigned long long *k
  * system's speed.  Work units are taken grid-stride: with several images (chunks != NULL) a unit is
  * HL_PEAK_ROWS rows of one image, with one image it is HL_PEAK_FLAT
  * consecutive int4 of its accumulator (a unit need not start a row: each
- * int4 finds its row).  A step of a unit is four int4 per thread, loaded at
- * once (streaming loads) and compared with the threshold; an int4 holding
+ * int4 finds its row).  A step of a unit is HL_PEAK_LOADS int4 per thread,
+ * loaded at once (streaming loads) and compared with the threshold; an int4 holding
  * a bin above it -- rare -- is noted in shared memory, and a step that
  * noted any (one barrier tells) applies the peak rule to its notes.  The
  * loop keeps few registers, so HL_PEAK_CTAS_PER_SM CTAs fit an SM and many
  * loads are in flight. */
 __global__ void __launch_bounds__(HL_PEAK_THREADS, HL_PEAK_CTAS_PER_SM) hl_peaks_kernel(hl_peak_args a)
 {
-    __shared__ unsigned s_note[4 * HL_PEAK_THREADS];   /* step offset << 4 | bins */
+    __shared__ unsigned s_note[HL_PEAK_LOADS * HL_PEAK_THREADS];   /* step offset << 4 | bins */
     __shared__ int s_nnote;
     const int q4 = a.Tp >> 2;
     const int tid = (int)threadIdx.x;
@@ -119,16 +119,16 @@ __global__ void __launch_bounds__(HL_PEAK_THREADS, HL_PEAK_CTAS_PER_SM) hl_peaks
             thr = a.img0.threshold;
             src = reinterpret_cast<const int4 *>(a.img0.acc) + e_lo;
         }
-        for (int l0 = 0; l0 < n; l0 += 4 * HL_PEAK_THREADS) {
-            int4 v4[4];
+        for (int l0 = 0; l0 < n; l0 += HL_PEAK_LOADS * HL_PEAK_THREADS) {
+            int4 v4[HL_PEAK_LOADS];
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
+            for (int u = 0; u < HL_PEAK_LOADS; u++) {
                 const int l = l0 + u * HL_PEAK_THREADS + tid;
                 v4[u] = (l < n) ? __ldcs(src + l) : make_int4(0, 0, 0, 0);
             }
             bool noted = false;
 #pragma unroll
-            for (int u = 0; u < 4; u++) {
+            for (int u = 0; u < HL_PEAK_LOADS; u++) {
                 const unsigned bits = (unsigned)(v4[u].x > thr) |
                                       ((unsigned)(v4[u].y > thr) << 1) |
                                       ((unsigned)(v4[u].z > thr) << 2) |
