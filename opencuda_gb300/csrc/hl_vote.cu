@@ -666,7 +666,8 @@ hl_vote_kernel(hl_vote_args a)
  * the image's threshold noted as peak candidates.  A
  * thread takes 16 bytes of every part of its region (grid.y = region): two
  * output int4 when the parts hold 16-bit counts, one otherwise; every slot
- * is read once, from L2 where the vote launch just wrote it. */
+ * is read once, from L2 where the vote launch just wrote it; the parts'
+ * loads go four at a time, all in flight. */
 template <bool NOTE>
 __global__ void __launch_bounds__(256)
 hl_merge_kernel(hl_merge_args a)
@@ -678,19 +679,19 @@ hl_merge_kernel(hl_merge_args a)
     int o;   /* first output int4 of this thread */
     if (a.part16) {
         /* one 16-byte load per part: eight 16-bit counts, output int4 o and
-         * o + 1 (a row holds 8, so both lie in one row); up to four parts'
-         * loads in flight at once */
+         * o + 1 (a row holds 8, so both lie in one row); the parts' loads
+         * four at a time, all four in flight (the last group predicated) */
         const int j = blockIdx.x * 256 + threadIdx.x;
         o = 2 * j;
         if (o >= n4)
             return;
         const int4 *src = a.scratch + (size_t)r.slot0 * a.slot4 + j;
-        int p = 0;
-        for (; p + 4 <= r.nparts; p += 4) {
+        for (int p = 0; p < r.nparts; p += 4) {
             int4 q[4];
 #pragma unroll
             for (int u = 0; u < 4; u++)
-                q[u] = __ldcg(src + (size_t)(p + u) * a.slot4);
+                q[u] = p + u < r.nparts ? __ldcg(src + (size_t)(p + u) * a.slot4)
+                                        : make_int4(0, 0, 0, 0);
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 v0.x += q[u].x & 0xffff;
@@ -703,28 +704,17 @@ hl_merge_kernel(hl_merge_args a)
                 v1.w += (unsigned)q[u].w >> 16;
             }
         }
-        for (; p < r.nparts; p++) {
-            const int4 q = __ldcg(src + (size_t)p * a.slot4);
-            v0.x += q.x & 0xffff;
-            v0.y += (unsigned)q.x >> 16;
-            v0.z += q.y & 0xffff;
-            v0.w += (unsigned)q.y >> 16;
-            v1.x += q.z & 0xffff;
-            v1.y += (unsigned)q.z >> 16;
-            v1.z += q.w & 0xffff;
-            v1.w += (unsigned)q.w >> 16;
-        }
     } else {
         o = blockIdx.x * 256 + threadIdx.x;
         if (o >= n4)
             return;
         const int4 *src = a.scratch + (size_t)r.slot0 * a.slot4 + o;
-        int p = 0;
-        for (; p + 4 <= r.nparts; p += 4) {
+        for (int p = 0; p < r.nparts; p += 4) {
             int4 q[4];
 #pragma unroll
             for (int u = 0; u < 4; u++)
-                q[u] = __ldcg(src + (size_t)(p + u) * a.slot4);
+                q[u] = p + u < r.nparts ? __ldcg(src + (size_t)(p + u) * a.slot4)
+                                        : make_int4(0, 0, 0, 0);
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 v0.x += q[u].x;
@@ -732,13 +722,6 @@ hl_merge_kernel(hl_merge_args a)
                 v0.z += q[u].z;
                 v0.w += q[u].w;
             }
-        }
-        for (; p < r.nparts; p++) {
-            const int4 q = __ldcg(src + (size_t)p * a.slot4);
-            v0.x += q.x;
-            v0.y += q.y;
-            v0.z += q.z;
-            v0.w += q.w;
         }
     }
     const int nout = a.part16 ? 2 : 1;

@@ -192,14 +192,17 @@ def test_batch_peak_candidates_and_their_overflow(hl_mod):
     HoughLine, Image = hl_mod
     imgs = [cases.synth(2, 1234, 0)] + [cases.synth(3, 77, i) for i in range(3)]
     dev = [Image.from_host(im) for im in imgs]
-    hl = HoughLine(detheta=DEG05)
-    ref = HoughLine(detheta=DEG05)
-    for thr in ([300] + [int(0.15 * max(im.shape)) for im in imgs[1:]],
-                [300, 0] + [int(0.15 * max(im.shape)) for im in imgs[2:]]):
-        rc, res = hl.houghLineBatch(dev, 24, thr)
-        assert rc == 0 and len(res) == len(imgs)
-        for i in range(len(imgs)):
-            ref.setThreshold(thr[i])
-            rc, single = ref.houghLine(dev[i], None, 24)
-            assert rc == 0
-            assert [l.astuple() for l in res[i]] == [l.astuple() for l in single], (thr, i)
+    for derho in (1.0, 2.0):   # the vote's unit and scaled rho forms
+        hl = HoughLine(detheta=DEG05)
+        ref = HoughLine(detheta=DEG05)
+        assert hl.setDeRho(derho) == 0 and ref.setDeRho(derho) == 0
+        for thr in ([300] + [int(0.15 * max(im.shape)) for im in imgs[1:]],
+                    [300, 0] + [int(0.15 * max(im.shape)) for im in imgs[2:]]):
+            rc, res = hl.houghLineBatch(dev, 24, thr)
+            assert rc == 0 and len(res) == len(imgs)
+            for i in range(len(imgs)):
+                ref.setThreshold(thr[i])
+                rc, single = ref.houghLine(dev[i], None, 24)
+                assert rc == 0
+                assert [l.astuple() for l in res[i]] == [l.astuple() for l in single], \
+                    (derho, thr, i)
