@@ -433,8 +433,9 @@ def proposal_workload(L, HoughLine, Image, dev, sp, kind: int, n: int, reps: int
     (local maxima of the coarse heatmap, the 64 best grown by one cell, and
     the confidence fall-back whose threshold was calibrated on held-out
     scenes for 99% top-32 recall) and `no_fallback` (the same selection, no
-    fall-back).  Timed with CUDA events around whole batch calls (the
-    proposal call synchronises once to decide its fall-back set); recall =
+    fall-back).  Timed with CUDA events around whole batch calls through the
+    C ABI, device buffers made once, like the plain call (the proposal call
+    synchronises once to decide its fall-back set); recall =
     plain top-32 lines the proposal path also reports, over all images.
     With check_counts, every line the calibrated run reports is checked
     against the plain accumulator of its image (untimed)."""
@@ -488,8 +489,17 @@ def proposal_workload(L, HoughLine, Image, dev, sp, kind: int, n: int, reps: int
            "network": sel.get("network", ""), "selection": base,
            "calibration": sel.get("calibration")}
     for name, opts in points.items():
-        def prop(opts=opts):
-            rc, _, st = proposal_batch(hl, net, imgs, K, thr, stream=sp, **opts)
+        # timed through the C ABI like the plain call (device buffers made
+        # once, no statistics counted); the Python wrapper below, untimed,
+        # gives the lines and the statistics
+        copts = _lib.hl_proposal_opts(opts["p_cut"], opts["max_props"], opts["dilate_theta"],
+                                      opts["dilate_rho"], 0, opts["top_m"],
+                                      1 if opts["nms"] else 0, opts["p_conf"])
+
+        def prop(copts=copts):
+            rc = L.hl_proposal_batch(hl.handle, net.handle, descs, n, th, K, C.byref(copts),
+                                     C.c_void_p(lines.data_ptr()),
+                                     C.c_void_p(counts.data_ptr()), None, sp)
             if rc != 0:
                 raise RuntimeError(f"hl_proposal_batch returned {rc}")
         t_prop = timed(prop)
@@ -731,6 +741,16 @@ def run_gb300(args):
                               ws == 1 and not args.no_cpu_baseline)
         if rank == 0:
             print(json.dumps({"circle": out}))
+        return 0
+
+    if args.proposal_only:
+        stream = torch.cuda.current_stream(dev)
+        sp = C.c_void_p(stream.cuda_stream)
+        out = {"proposal": [proposal_workload(L, HoughLine, Image, dev, sp, 4, 128, 5, False),
+                            proposal_workload(L, HoughLine, Image, dev, sp, 5, 1024, 3, True)],
+               "proposal_single": proposal_single_image(L, HoughLine, Image, dev, sp, 50)}
+        if rank == 0:
+            print(json.dumps(out))
         return 0
 
     if args.batched_only:
@@ -976,6 +996,8 @@ def main():
                     help="only the batched 256-image measurement (its own JSON line)")
     ap.add_argument("--no-proposal", action="store_true",
                     help="skip the proposal-guided measurements")
+    ap.add_argument("--proposal-only", action="store_true",
+                    help="only the proposal-guided measurements (their own JSON line)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

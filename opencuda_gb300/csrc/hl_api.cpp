@@ -2251,6 +2251,7 @@ extern "C" int hl_proposal_batch(hl_handle *h, hl_net *net,
     const size_t off_geo = align16(sizeof(hl_pool_img) * nimg);
     const size_t tab = off_geo + sizeof(hl_head_geom) * nimg;
     size_t max_bins = 1;
+    int nk_fast = 0;
     std::vector<char> force((size_t)nimg, 0);
     if (!b->tab_event) {
         CK(cudaEventCreateWithFlags(&b->tab_read, cudaEventDisableTiming));
@@ -2286,7 +2287,10 @@ extern "C" int hl_proposal_batch(hl_handle *h, hl_net *net,
         hg[i].pad = 0;
         const int nk = (h->T + HL_COARSE_T - 1) / HL_COARSE_T + 2;
         const int nj = (b->R[i] + HL_COARSE_R - 1) / HL_COARSE_R + 2;
-        max_bins = std::max(max_bins, (size_t)nk * nj);
+        /* columns of nj rows plus a dump row; the branch-free vote for at
+         * most 6 or 10 thetas writes that many columns */
+        nk_fast = nk <= 6 ? 6 : (nk <= 10 ? 10 : 0);
+        max_bins = std::max(max_bins, (size_t)std::max(nk, nk_fast) * (size_t)(nj + 1));
         const int ntiles = ((w + HL_TILE_W - 1) / HL_TILE_W) * ((hh + HL_TILE_H - 1) / HL_TILE_H);
         if (ntiles > HL_WIN_MAXTILES)
             force[i] = 1;
@@ -2342,6 +2346,7 @@ extern "C" int hl_proposal_batch(hl_handle *h, hl_net *net,
     wa.irho = (float)(1.0 / h->p.derho);
     wa.votes = stats ? reinterpret_cast<unsigned long long *>(pw->d_cnt + 2) : nullptr;
     wa.status = pw->d_cnt + 1;
+    wa.nk_fast = nk_fast;
     CK(hl_launch_window_vote(&wa, (int)max_bins, std::max(1, h->sms) * 6, s));
     if ((rc = batch_enqueue_finalize(h, b, nimg, K, s)) != HL_NO_ERROR)
         return rc;

@@ -22,6 +22,8 @@
 #include "hl_internal.h"
 #include "hl_window.h"
 
+#include <algorithm>
+
 #define FULL 0xffffffffu
 
 #define NCELL (HL_COARSE_T * HL_COARSE_R)
@@ -204,13 +206,159 @@ __device__ __forceinline__ void fine_range(int c, int n, int m, int *lo, int *hi
     *hi = (int)(((long long)(c + 1) * m + n - 1) / n);
 }
 
+/* The votes of one point into a window's haloed bins (nk thetas of
+ * cos/sin s_c/s_s, nj rows from the row whose rho bits are `base`): the
+ * plain method's rule (okano_3_0/HoughLine.cu:115-121) with the float ->
+ * integer step by the window's conversion (CV_FLOOR / CV_CEIL: the magic
+ * constant, see RHO_MAGIC; CV_EXACT: the conversion instruction).  The lane
+ * starts at theta kk0 and walks the thetas round, so at a time the warp's
+ * lanes vote about 32 / nk lanes per theta: points of one line (which
+ * share a bin at its theta) collide in groups of that size, not 32. */
+template <bool UNIT, int CV>
+__device__ __forceinline__ void window_point(float x, float y, const float *s_c,
+                                             const float *s_s, int nk, int kk0, int base,
+                                             int nj, unsigned acc_base, float irho)
+{
+    int kk = kk0;
+    for (int st = 0; st < nk; st++) {
+        const float v = rho_f<UNIT>(x, y, s_c[kk], s_s[kk], irho);
+        int j;
+        if (CV == CV_FLOOR)
+            j = __float_as_int(__fadd_rz(v, RHO_MAGIC)) - base;
+        else if (CV == CV_CEIL)
+            j = __float_as_int(__fadd_ru(v, RHO_MAGIC)) - base;
+        else
+            j = __float2int_rz(v) - base;
+        if ((unsigned)j < (unsigned)nj)
+            red_smem(acc_base + (unsigned)(kk * (nj + 1) + j) * 4u);
+        if (++kk == nk)
+            kk = 0;
+    }
+}
+
+/* The points of the window's hit tiles: with the hit tiles listed (nhit of
+ * them, at most HL_WIN_HITS), warp w takes hits w, w + 8, ... -- the hits of
+ * a strip bunch in a few mask words, so taking whole mask words left most
+ * warps idle -- else warp w takes mask words w, w + 8, ... */
+template <bool UNIT, int CV>
+__device__ __forceinline__ void window_tiles(const hl_vote_img &im, const unsigned *tmask,
+                                             int ntl, const unsigned short *hits, int nhit,
+                                             const float *s_c, const float *s_s, int nk,
+                                             int base, int nj, unsigned acc_base, float irho)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nw = blockDim.x >> 5;
+    const int kk0 = lane % nk;
+    if (nhit <= HL_WIN_HITS) {
+        for (int h = warp; h < nhit; h += nw) {
+            const int tl = hits[h];
+            const int p0 = im.tile_off[tl], p1 = im.tile_off[tl + 1];
+            for (int p = p0 + lane; p < p1; p += 32) {
+                const float2 xy = im.pts[p];
+                window_point<UNIT, CV>(xy.x, xy.y, s_c, s_s, nk, kk0, base, nj, acc_base,
+                                       irho);
+            }
+        }
+        return;
+    }
+    for (int wd = warp; wd < (ntl + 31) / 32; wd += nw) {
+        unsigned m = tmask[wd];
+        while (m) {
+            const int tl = wd * 32 + __ffs(m) - 1;
+            m &= m - 1;
+            const int p0 = im.tile_off[tl], p1 = im.tile_off[tl + 1];
+            for (int p = p0 + lane; p < p1; p += 32) {
+                const float2 xy = im.pts[p];
+                window_point<UNIT, CV>(xy.x, xy.y, s_c, s_s, nk, kk0, base, nj, acc_base,
+                                       irho);
+            }
+        }
+    }
+}
+
+/* float -> integer of the window's conversion (RHO_MAGIC), as bits */
+template <int CV>
+__device__ __forceinline__ int conv_bits(float v)
+{
+    if (CV == CV_FLOOR)
+        return __float_as_int(__fadd_rz(v, RHO_MAGIC));
+    if (CV == CV_CEIL)
+        return __float_as_int(__fadd_ru(v, RHO_MAGIC));
+    return __float2int_rz(v);
+}
+
+/* The common case, at most NK thetas (NK a compile-time bound): the
+ * thetas' cos / sin and column addresses in registers, every lane votes its
+ * point for theta 0, 1, ... with no branch -- a row outside the window
+ * goes to the column's dump row nj (rows are nj + 1 apart), a theta past
+ * the window's nk to a column of its own that nothing reads (cos = sin =
+ * 0).  Warp w takes the listed hit tiles w, w + 8, ... */
+template <bool UNIT, int CV, int NK>
+__device__ __forceinline__ void window_tiles_nk(const hl_vote_img &im, const unsigned short *hits,
+                                                int nhit, const float *s_c, const float *s_s,
+                                                int base, int nj, unsigned acc_base, float irho)
+{
+    float c[NK], sn[NK];
+    unsigned kb[NK];
+#pragma unroll
+    for (int k = 0; k < NK; k++) {
+        c[k] = s_c[k];
+        sn[k] = s_s[k];
+        kb[k] = acc_base + (unsigned)(k * (nj + 1)) * 4u;
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nw = blockDim.x >> 5;
+    for (int h = warp; h < nhit; h += nw) {
+        const int tl = hits[h];
+        const int p0 = im.tile_off[tl], p1 = im.tile_off[tl + 1];
+        for (int p = p0 + lane; p < p1; p += 32) {
+            const float2 xy = im.pts[p];
+#pragma unroll
+            for (int k = 0; k < NK; k++) {
+                const int j = conv_bits<CV>(rho_f<UNIT>(xy.x, xy.y, c[k], sn[k], irho)) - base;
+                red_smem(kb[k] + min((unsigned)j, (unsigned)nj) * 4u);
+            }
+        }
+    }
+}
+
+template <bool UNIT, int NK>
+__device__ __forceinline__ void window_tiles_cv(int cv, const hl_vote_img &im,
+                                                const unsigned short *hits, int nhit,
+                                                const float *s_c, const float *s_s, int base,
+                                                int nj, unsigned acc_base, float irho)
+{
+    if (cv == CV_FLOOR)
+        window_tiles_nk<UNIT, CV_FLOOR, NK>(im, hits, nhit, s_c, s_s, base, nj, acc_base, irho);
+    else if (cv == CV_CEIL)
+        window_tiles_nk<UNIT, CV_CEIL, NK>(im, hits, nhit, s_c, s_s, base, nj, acc_base, irho);
+    else
+        window_tiles_nk<UNIT, CV_EXACT, NK>(im, hits, nhit, s_c, s_s, base, nj, acc_base, irho);
+}
+
+/* windows with more thetas than the shared table: the same walk, cos/sin
+ * from global memory, exact conversion */
+template <bool UNIT>
+__device__ __noinline__ void window_tiles_wide(const hl_vote_img &im, const unsigned *tmask,
+                                               int ntl, const unsigned short *hits, int nhit,
+                                               const float *c, const float *s, int nk,
+                                               int base, int nj, unsigned acc_base, float irho)
+{
+    window_tiles<UNIT, CV_EXACT>(im, tmask, ntl, hits, nhit, c, s, nk, base, nj, acc_base,
+                                 irho);
+}
+
 template <bool UNIT>
 __global__ void __launch_bounds__(256)
 hl_window_vote_kernel(hl_window_args a)
 {
-    extern __shared__ int wacc[];            /* [nk][nj] haloed window */
+    extern __shared__ int wacc[];            /* [nk][nj + 1] haloed window, dump row nj */
     __shared__ unsigned tmask[HL_WIN_MAXTILES / 32];
+    __shared__ float s_c[HL_WIN_MAXK], s_s[HL_WIN_MAXK];   /* its cos / sin */
+    __shared__ unsigned short s_hit[HL_WIN_HITS];           /* its hit tiles */
+    __shared__ int s_nhit;
     __shared__ int4 cur;
+    const unsigned acc_base = (unsigned)__cvta_generic_to_shared(wacc);
     const int nwin = min(*a.nwin, a.cap);
     for (int wi = blockIdx.x; wi < nwin; wi += gridDim.x) {
         __syncthreads();
@@ -229,8 +377,12 @@ hl_window_vote_kernel(hl_window_args a)
         const int hk0 = max(k_lo - 1, 0), hk1 = min(k_hi + 1, a.T);
         const int hj0 = max(j_lo - 1, 0), hj1 = min(j_hi + 1, im.R);
         const int nk = hk1 - hk0, nj = hj1 - hj0;
-        for (int i = threadIdx.x; i < nk * nj; i += blockDim.x)
+        for (int i = threadIdx.x; i < nk * (nj + 1); i += blockDim.x)
             wacc[i] = 0;
+        for (int i = threadIdx.x; i < HL_WIN_MAXK; i += blockDim.x) {
+            s_c[i] = i < nk ? a.cosv[hk0 + i] : 0.0f;   /* past nk: a column nothing reads */
+            s_s[i] = i < nk ? a.sinv[hk0 + i] : 0.0f;
+        }
         /* tile filter over the image's tiles (one bit each) */
         const float c0 = a.cosv[hk0], s0 = a.sinv[hk0];
         const float c1 = a.cosv[hk1 - 1], s1 = a.sinv[hk1 - 1];
@@ -246,24 +398,60 @@ hl_window_vote_kernel(hl_window_args a)
                 tmask[(base + threadIdx.x) >> 5] = m;
         }
         __syncthreads();
-        /* vote: each warp takes hit tiles in turn, its lanes the tile's points */
-        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        for (int wd = warp; wd < (ntl + 31) / 32; wd += blockDim.x >> 5) {
-            unsigned m = tmask[wd];
-            while (m) {
-                const int tl = wd * 32 + __ffs(m) - 1;
-                m &= m - 1;
-                const int p0 = im.tile_off[tl], p1 = im.tile_off[tl + 1];
-                for (int p = p0 + lane; p < p1; p += 32) {
-                    const float2 xy = im.pts[p];
-                    for (int k = hk0; k < hk1; k++) {
-                        const int j = rho_of<UNIT>(xy.x, xy.y, a.cosv[k], a.sinv[k],
-                                                   a.irho) - im.rho_min - hj0;
-                        if ((unsigned)j < (unsigned)nj)
-                            atomicAdd(&wacc[(k - hk0) * nj + j], 1);
-                    }
+        /* the hit tiles listed in order (warp 0: a word per lane, prefix of
+         * the counts, each lane writes its word's tiles) */
+        if (threadIdx.x < 32) {
+            const int lane = threadIdx.x, nwd = (ntl + 31) / 32;
+            int tot = 0;
+            for (int w0 = 0; w0 < nwd; w0 += 32) {
+                unsigned m = w0 + lane < nwd ? tmask[w0 + lane] : 0u;
+                const int cnt = __popc(m);
+                int incl = cnt;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int t = __shfl_up_sync(FULL, incl, o);
+                    if (lane >= o)
+                        incl += t;
                 }
+                int pos = tot + incl - cnt;
+                while (m) {
+                    const int bb = __ffs(m) - 1;
+                    m &= m - 1;
+                    if (pos < HL_WIN_HITS)
+                        s_hit[pos] = (unsigned short)((w0 + lane) * 32 + bb);
+                    pos++;
+                }
+                tot += __shfl_sync(FULL, incl, 31);
             }
+            if (lane == 0)
+                s_nhit = tot;
+        }
+        __syncthreads();
+        /* vote: each warp takes hit tiles in turn, its lanes the tile's
+         * points; the float -> integer step by the magic constant unless the
+         * window holds rho 0 (or has more thetas than the table) */
+        {
+            const int row_lo = im.rho_min + hj0, row_hi = im.rho_min + hj1 - 1;
+            const int cv = row_lo >= 1 ? CV_FLOOR : (row_hi <= -1 ? CV_CEIL : CV_EXACT);
+            const int base = cv == CV_EXACT ? row_lo : RHO_MAGIC_BITS + row_lo;
+            if (s_nhit <= HL_WIN_HITS && nk <= 6 && a.nk_fast == 6)
+                window_tiles_cv<UNIT, 6>(cv, im, s_hit, s_nhit, s_c, s_s, base, nj, acc_base,
+                                         a.irho);
+            else if (s_nhit <= HL_WIN_HITS && nk <= 10 && a.nk_fast == 10)
+                window_tiles_cv<UNIT, 10>(cv, im, s_hit, s_nhit, s_c, s_s, base, nj, acc_base,
+                                          a.irho);
+            else if (nk <= HL_WIN_MAXK && row_lo >= 1)
+                window_tiles<UNIT, CV_FLOOR>(im, tmask, ntl, s_hit, s_nhit, s_c, s_s, nk,
+                                             RHO_MAGIC_BITS + row_lo, nj, acc_base, a.irho);
+            else if (nk <= HL_WIN_MAXK && row_hi <= -1)
+                window_tiles<UNIT, CV_CEIL>(im, tmask, ntl, s_hit, s_nhit, s_c, s_s, nk,
+                                            RHO_MAGIC_BITS + row_lo, nj, acc_base, a.irho);
+            else if (nk <= HL_WIN_MAXK)
+                window_tiles<UNIT, CV_EXACT>(im, tmask, ntl, s_hit, s_nhit, s_c, s_s, nk,
+                                             row_lo, nj, acc_base, a.irho);
+            else
+                window_tiles_wide<UNIT>(im, tmask, ntl, s_hit, s_nhit, a.cosv + hk0,
+                                        a.sinv + hk0, nk, row_lo, nj, acc_base, a.irho);
         }
         __syncthreads();
         /* peaks among the owned bins */
@@ -271,13 +459,13 @@ hl_window_vote_kernel(hl_window_args a)
         for (int i = threadIdx.x; i < ok * oj; i += blockDim.x) {
             const int k = k_lo + i / oj, j = j_lo + i % oj;
             const int lk = k - hk0, lj = j - hj0;
-            const int v = wacc[lk * nj + lj];
+            const int v = wacc[lk * (nj + 1) + lj];
             bool is = false;
             if (v > pk.threshold) {
-                const int W = (k > 0) ? wacc[(lk - 1) * nj + lj] : 0;
-                const int E = (k + 1 < a.T) ? wacc[(lk + 1) * nj + lj] : 0;
-                const int N = (j > 0) ? wacc[lk * nj + lj - 1] : 0;
-                const int S = (j + 1 < im.R) ? wacc[lk * nj + lj + 1] : 0;
+                const int W = (k > 0) ? wacc[(lk - 1) * (nj + 1) + lj] : 0;
+                const int E = (k + 1 < a.T) ? wacc[(lk + 1) * (nj + 1) + lj] : 0;
+                const int N = (j > 0) ? wacc[lk * (nj + 1) + lj - 1] : 0;
+                const int S = (j + 1 < im.R) ? wacc[lk * (nj + 1) + lj + 1] : 0;
                 /* okano_3_0/HoughLine.cu:195-199 */
                 is = v > W && v >= E && v > N && v >= S;
             }
@@ -308,23 +496,29 @@ hl_window_vote_kernel(hl_window_args a)
     }
 }
 
+template <bool UNIT>
+static cudaError_t launch_window_t(const hl_window_args *a, size_t smem, int grid, cudaStream_t s)
+{
+    cudaError_t e = cudaFuncSetAttribute(hl_window_vote_kernel<UNIT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    /* the CTAs take windows grid-stride: as many as are resident at once */
+    int dev = 0, sms = 1, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hl_window_vote_kernel<UNIT>, 256,
+                                                      smem) == cudaSuccess &&
+        per_sm > 0)
+        grid = std::min(grid, per_sm * sms);
+    hl_window_vote_kernel<UNIT><<<grid, 256, smem, s>>>(*a);
+    return cudaGetLastError();
+}
+
 cudaError_t hl_launch_window_vote(const hl_window_args *a, int max_win_bins, int grid,
                                   cudaStream_t s)
 {
     const size_t smem = sizeof(int) * (size_t)max_win_bins;
-    cudaError_t e;
-    if (a->irho == 1.0f) {
-        e = cudaFuncSetAttribute(hl_window_vote_kernel<true>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess)
-            return e;
-        hl_window_vote_kernel<true><<<grid, 256, smem, s>>>(*a);
-    } else {
-        e = cudaFuncSetAttribute(hl_window_vote_kernel<false>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess)
-            return e;
-        hl_window_vote_kernel<false><<<grid, 256, smem, s>>>(*a);
-    }
-    return cudaGetLastError();
+    return a->irho == 1.0f ? launch_window_t<true>(a, smem, grid, s)
+                           : launch_window_t<false>(a, smem, grid, s);
 }

@@ -12,6 +12,10 @@
 #define HL_COARSE_R 128
 /* tiles one window may filter (64 Mpixel ROIs) */
 #define HL_WIN_MAXTILES 16384
+/* thetas of a window whose cos / sin the vote keeps in shared memory */
+#define HL_WIN_MAXK 64
+/* hit tiles of a window listed for the warps (more: taken by mask word) */
+#define HL_WIN_HITS 4096
 
 typedef struct hl_select_args {
     const float *logits;   /* [nimg][90][128] */
@@ -41,6 +45,10 @@ typedef struct hl_window_args {
     float irho;
     unsigned long long *votes;   /* executed votes, or NULL */
     int *status;
+    /* 6 or 10: every window has at most that many thetas and the vote may
+     * take the branch-free path compiled for it (its accumulator has room
+     * for that many columns); 0: the general path */
+    int nk_fast;
 } hl_window_args;
 
 cudaError_t hl_launch_select(const hl_select_args *a, int nimg, cudaStream_t s);
