@@ -512,6 +512,7 @@ def proposal_workload(L, HoughLine, Image, dev, sp, kind: int, n: int, reps: int
                      "fallback_rate": st["fallback"] / n,
                      "fallback_confidence": st["fallback_conf"] / n,
                      "windows_per_image": st["windows"] / n,
+                     "cells_per_image": st["cells"] / n,
                      "executed_votes_per_image": st["votes"] / n}
         if check_counts and name == "calibrated":
             # every reported line is a peak bin of the plain accumulator with

@@ -112,12 +112,14 @@ typedef struct hl_proposal_opts {
 
 typedef struct hl_proposal_stats {
     int fallback;        /* images that ran the plain method instead */
-    int windows;         /* coarse windows voted */
+    int windows;         /* windows voted (runs of up to 8 coarse cells) */
     int judged;          /* images also run through the plain method */
     int judged_lines;    /* lines the plain method gave them */
     int judged_found;    /* of those, reported by the proposal path */
     int fallback_conf;   /* of the fall-backs, decided by the confidence test */
     long long votes;     /* executed votes of the windows */
+    int cells;           /* coarse cells the windows cover */
+    int pad;
 } hl_proposal_stats;
 
 int hl_proposal_batch(hl_handle *h, hl_net *net, const hl_image_desc *imgs,

@@ -87,7 +87,8 @@ class hl_proposal_opts(C.Structure):
 class hl_proposal_stats(C.Structure):
     _fields_ = [("fallback", C.c_int), ("windows", C.c_int), ("judged", C.c_int),
                 ("judged_lines", C.c_int), ("judged_found", C.c_int),
-                ("fallback_conf", C.c_int), ("votes", C.c_longlong)]
+                ("fallback_conf", C.c_int), ("votes", C.c_longlong), ("cells", C.c_int),
+                ("pad", C.c_int)]
 
 
 class hl_tune_entry(C.Structure):

@@ -2159,7 +2159,7 @@ struct hl_prop_ws {
     size_t cap_htab;
     int4 *d_win;
     size_t cap_win;
-    int *d_cnt;                    /* [0] windows [1] status [2..3] votes */
+    int *d_cnt;                    /* [0] windows [1] status [2..3] votes [4] cells */
     int *d_fb;                     /* per-image fall-back flags */
     size_t cap_fb;
     int *h_fb;                     /* pinned copy */
@@ -2286,7 +2286,7 @@ extern "C" int hl_proposal_batch(hl_handle *h, hl_net *net,
         hg[i].qw = ((w + f - 1) / f + 3) / 4;
         hg[i].pad = 0;
         const int nk = (h->T + HL_COARSE_T - 1) / HL_COARSE_T + 2;
-        const int nj = (b->R[i] + HL_COARSE_R - 1) / HL_COARSE_R + 2;
+        const int nj = HL_WIN_RUN * ((b->R[i] + HL_COARSE_R - 1) / HL_COARSE_R) + 2;
         /* columns of nj rows plus a dump row; the branch-free vote for at
          * most 6 or 10 thetas writes that many columns */
         nk_fast = nk <= 6 ? 6 : (nk <= 10 ? 10 : 0);
@@ -2330,6 +2330,7 @@ extern "C" int hl_proposal_batch(hl_handle *h, hl_net *net,
     sa.fallback = pw->d_fb;
     sa.win = pw->d_win;
     sa.nwin = pw->d_cnt + 0;
+    sa.ncells = pw->d_cnt + 4;
     sa.cap = cap_win;
     sa.status = pw->d_cnt + 1;
     CK(hl_launch_select(&sa, nimg, s));
@@ -2353,7 +2354,7 @@ extern "C" int hl_proposal_batch(hl_handle *h, hl_net *net,
     CK(cudaEventRecord(b->tab_read, s));
 
     /* fall-back and judged images run the plain method */
-    int st_host[4] = {0, 0, 0, 0};
+    int st_host[5] = {0, 0, 0, 0, 0};
     CK(cudaMemcpyAsync(pw->h_fb, pw->d_fb, sizeof(int) * nimg, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(st_host, pw->d_cnt, sizeof(st_host), cudaMemcpyDeviceToHost, s));
     int nst = 0;
@@ -2465,6 +2466,8 @@ extern "C" int hl_proposal_batch(hl_handle *h, hl_net *net,
         unsigned long long v = 0;
         memcpy(&v, &st_host[2], sizeof(v));
         stats->votes = (long long)v;
+        stats->cells = st_host[4];
+        stats->pad = 0;
     }
     return HL_NO_ERROR;
 }

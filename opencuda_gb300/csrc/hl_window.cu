@@ -7,9 +7,10 @@
  * sees more likely lines than that (count and confidence tests), grows the
  * kept cells by the dilation and appends one window per cell.
  *
- * hl_window_vote_kernel: one CTA per window.  A coarse cell (t, r) owns the
- * fine thetas k with floor(90 k / T) = t and the rho rows j with
- * floor(128 j / R) = r; the CTA votes those bins plus a one-bin halo with
+ * hl_window_vote_kernel: one CTA per window, a run of up to HL_WIN_RUN
+ * marked coarse cells (t, r .. r1) at one theta cell.  A coarse cell (t, r)
+ * owns the fine thetas k with floor(90 k / T) = t and the rho rows j with
+ * floor(128 j / R) = r; the CTA votes the run's bins plus a one-bin halo with
  * the plain method's rule (okano_3_0/HoughLine.cu:86-130) from every point of
  * the tiles that can reach them, then applies the peak rule (:168-213) to the
  * owned bins with the halo as their neighbours (bins outside the accumulator
@@ -167,22 +168,25 @@ hl_select_kernel(hl_select_args a)
         }
     }
     __syncthreads();
+    /* one window per run of marked cells along rho at one theta (a mask
+     * word holds 32 consecutive rho cells of one theta cell), at most
+     * HL_WIN_RUN cells: the run's points are read once for all its cells */
     for (int wd = threadIdx.x; wd < NCELL / 32; wd += blockDim.x) {
         unsigned m = mark[wd];
-        if (!m)
-            continue;
-        const int n = __popc(m);
-        const int base = atomicAdd(a.nwin, n);
-        int q = 0;
+        if (m)
+            atomicAdd(a.ncells, __popc(m));
         while (m) {
             const int bit = __ffs(m) - 1;
-            m &= m - 1;
+            const unsigned ones = ~(m >> bit);            /* the run ends at its first 0 */
+            const int len = min(ones ? __ffs(ones) - 1 : 32 - bit, HL_WIN_RUN);
+            m &= ~(((len == 32 ? 0u : (1u << len)) - 1u) << bit);
             const int c = wd * 32 + bit;
-            if (base + q < a.cap)
-                a.win[base + q] = make_int4(b, c / HL_COARSE_R, c % HL_COARSE_R, 0);
+            const int q = atomicAdd(a.nwin, 1);
+            if (q < a.cap)
+                a.win[q] = make_int4(b, c / HL_COARSE_R, c % HL_COARSE_R,
+                                     c % HL_COARSE_R + len - 1);
             else
                 atomicOr(a.status, HL_ST_CAND_OVERFLOW);
-            q++;
         }
     }
 }
@@ -365,12 +369,13 @@ hl_window_vote_kernel(hl_window_args a)
         if (threadIdx.x == 0)
             cur = a.win[wi];
         __syncthreads();
-        const int b = cur.x, t = cur.y, r = cur.z;
+        const int b = cur.x, t = cur.y, r = cur.z, r1 = cur.w;   /* rho cells r .. r1 */
         const hl_vote_img im = a.vimgs[b];
         const hl_peak_img pk = a.pimgs[b];
-        int k_lo, k_hi, j_lo, j_hi;
+        int k_lo, k_hi, j_lo, j_hi, unused;
         fine_range(t, HL_COARSE_T, a.T, &k_lo, &k_hi);
-        fine_range(r, HL_COARSE_R, im.R, &j_lo, &j_hi);
+        fine_range(r, HL_COARSE_R, im.R, &j_lo, &unused);
+        fine_range(r1, HL_COARSE_R, im.R, &unused, &j_hi);
         if (k_hi <= k_lo || j_hi <= j_lo)
             continue;
         /* haloed ranges, clipped to the accumulator */

@@ -16,6 +16,8 @@
 #define HL_WIN_MAXK 64
 /* hit tiles of a window listed for the warps (more: taken by mask word) */
 #define HL_WIN_HITS 4096
+/* rho cells one window may span (a run of marked cells at one theta) */
+#define HL_WIN_RUN 8
 
 typedef struct hl_select_args {
     const float *logits;   /* [nimg][90][128] */
@@ -28,8 +30,9 @@ typedef struct hl_select_args {
     int use_conf;          /* confidence test on (zconf) */
     float zconf;           /* fall back when the best unselected candidate is above */
     int *fallback;         /* out [nimg]: 0, 1 (count test) or 2 (confidence test) */
-    int4 *win;             /* out: {image, t, r, 0} */
+    int4 *win;             /* out: {image, t, r, r1}: rho cells r .. r1 */
     int *nwin;             /* window counter (zeroed before) */
+    int *ncells;           /* marked coarse cells (zeroed before) */
     int cap;
     int *status;
 } hl_select_args;

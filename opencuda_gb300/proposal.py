@@ -155,5 +155,5 @@ def proposal_batch(hl, net: HoughNet, images, linesmax: int, thresholds=None,
             out.append(LineParam(a, int(raw[i, j, 1]), int(raw[i, j, 2])))
         res.append(out)
     stats = {k: getattr(st, k) for k in ("fallback", "windows", "judged", "judged_lines",
-                                         "judged_found", "fallback_conf", "votes")}
+                                         "judged_found", "fallback_conf", "votes", "cells")}
     return rc, res, stats

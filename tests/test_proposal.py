@@ -45,7 +45,9 @@ def test_all_cells_proposed_equals_plain(env):
     assert rc == 0 and st["fallback"] == 0
     assert [[l.astuple() for l in r] for r in got] == want
     assert st["judged"] == len(imgs) and st["judged_found"] == st["judged_lines"]
-    assert st["windows"] == len(imgs) * 90 * 128
+    assert st["cells"] == len(imgs) * 90 * 128
+    # a window is a run of up to 8 rho cells at one theta cell
+    assert st["windows"] == len(imgs) * 90 * 128 // 8
 
 
 def test_forced_fallback_is_plain(env):
@@ -132,10 +134,10 @@ def test_trained_network_gains_over_untrained(env):
         rc, got, st = proposal_batch(hl, net, imgs, 32, thr, p_cut=0.999, max_props=11520,
                                      dilate_theta=1, dilate_rho=1, top_m=32, nms=True)
         assert rc == 0 and st["fallback"] == 0
-        res[name] = (_recall(plain, got), st["windows"], st["votes"])
+        res[name] = (_recall(plain, got), st["cells"], st["votes"])
     (rt, wt, vt), (ru, wu, vu) = res["trained"], res["untrained"]
-    print(f"\nablation: trained recall {rt:.3f} ({wt} windows, {vt} votes), "
-          f"untrained {ru:.3f} ({wu} windows, {vu} votes)")
+    print(f"\nablation: trained recall {rt:.3f} ({wt} cells, {vt} votes), "
+          f"untrained {ru:.3f} ({wu} cells, {vu} votes)")
     assert rt > ru + 0.25
     assert wt <= 1.3 * wu
 
