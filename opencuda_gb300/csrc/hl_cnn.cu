@@ -406,9 +406,17 @@ __global__ void hl_pool_kernel(const hl_pool_img *imgs, int nimg, int side,
         const int f = im.factor;
         int cnt = 0;
         const int y0 = i * f, x0 = j * f;
+        const int x1 = min(x0 + f, im.w);
         for (int y = y0; y < min(y0 + f, im.h); y++) {
             const uint8_t *row = im.base + (size_t)y * im.pitch;
-            for (int x = x0; x < min(x0 + f, im.w); x++)
+            int x = x0;
+            /* four bytes a load where the row allows it (255-bytes counted
+             * with one byte-wise compare), the rest byte by byte */
+            if ((((uintptr_t)(row + x)) & 3u) == 0)
+                for (; x + 4 <= x1; x += 4)
+                    cnt += __popc(__vcmpeq4(*reinterpret_cast<const unsigned *>(row + x),
+                                            0xffffffffu)) >> 3;
+            for (; x < x1; x++)
                 cnt += row[x] == 255;
         }
         out[e] = __float2bfloat16((float)cnt / (float)(f * f));

@@ -169,3 +169,35 @@ def test_network_gradients_match_oracle(lib):
             assert rel < 0.05, (o, n, rel)
             o += n
     assert np.allclose(g[o:], gref[o:], rtol=1e-3, atol=1e-6)
+
+
+def test_occupancy_matches_numpy(lib):
+    """The network's input: the fraction of 255-pixels in every f x f cell
+    (f = ceil(max(w, h) / 256)), as BF16, for ROIs of odd sizes and offsets
+    (rows not 4-byte aligned) and whole images."""
+    import math
+    import torch
+    from opencuda_gb300.houghline import HoughLine, Image
+    from opencuda_gb300.proposal import HoughNet
+    rng = np.random.default_rng(12)
+    cases = []
+    for (h, w, roi) in ((517, 333, None), (1030, 2047, (3, 5, 3 + 1999, 5 + 1001)),
+                        (4096, 4093, None), (700, 701, (1, 2, 1 + 613, 2 + 597))):
+        img = np.where(rng.random((h, w)) < 0.07, 255, rng.integers(0, 255, (h, w))).astype(np.uint8)
+        cases.append((img, roi))
+    hl = HoughLine(detheta=math.pi / 360)
+    net = HoughNet(seed=1)
+    dev = [Image.from_host(im, roi) if roi else Image.from_host(im) for im, roi in cases]
+    occ, _ = net.occupancy(hl, dev)
+    got = occ.cpu().numpy().view(np.uint16)
+    for b, (img, roi) in enumerate(cases):
+        sub = img if roi is None else img[roi[1]:roi[3], roi[0]:roi[2]]
+        h, w = sub.shape
+        f = max(1, (max(w, h) + 255) // 256)
+        want = np.zeros((256, 256), np.float32)
+        edge = (sub == 255).astype(np.int64)
+        for i in range(min(256, (h + f - 1) // f)):
+            for j in range(min(256, (w + f - 1) // f)):
+                want[i, j] = edge[i * f:(i + 1) * f, j * f:(j + 1) * f].sum() / float(f * f)
+        wb = CO.bf16_bits(want).view(np.uint16)
+        assert np.array_equal(got[b], wb), b
