@@ -315,8 +315,12 @@ __device__ __forceinline__ void window_tiles_nk(const hl_vote_img &im, const uns
     for (int h = warp; h < nhit; h += nw) {
         const int tl = hits[h];
         const int p0 = im.tile_off[tl], p1 = im.tile_off[tl + 1];
+        /* the next point's load issued before this one's votes */
+        float2 nxt = p0 + lane < p1 ? im.pts[p0 + lane] : make_float2(0.0f, 0.0f);
         for (int p = p0 + lane; p < p1; p += 32) {
-            const float2 xy = im.pts[p];
+            const float2 xy = nxt;
+            if (p + 32 < p1)
+                nxt = im.pts[p + 32];
 #pragma unroll
             for (int k = 0; k < NK; k++) {
                 const int j = conv_bits<CV>(rho_f<UNIT>(xy.x, xy.y, c[k], sn[k], irho)) - base;
