@@ -5,15 +5,19 @@
  * The reference finds peaks with _findlocalMaxKer (okano_3_0/HoughLine.cu:
  * 168-213, racy and unchecked at its edges), copies two accumulator-sized
  * arrays to the host and ranks / merges there (:781-948).  Here:
- *   hl_peaks_kernel   -- bounds-checked peak rule over acc[R][Tp], peaks
- *                        appended as 64-bit keys (votes << 32 | ~index) with
- *                        warp-aggregated atomics (HBM-bound: one read of acc);
+ *   hl_peaks_kernel   -- bounds-checked peak rule, peaks appended as
+ *                        64-bit keys (votes << 32 | ~index): over the bins
+ *                        the vote noted above the threshold (batches), or one
+ *                        read of acc[R][Tp] (one image; HBM / L2 bound);
  *   hl_finalize_kernel -- one CTA: top-M selection (MSD radix select when the
  *                        peaks exceed one 1024-key chunk), rank sort of the
  *                        chunk (keys are unique), the reference's float
  *                        decode, the pairwise predecessor bitmask, and the
- *                        greedy merge resolved in parallel rounds;
- *                        writes min(survivors, linesmax) LineParam records.
+ *                        greedy merge resolved by one warp word by word;
+ *                        writes min(survivors, linesmax) LineParam records
+ *                        (hl_finalize_cluster_kernel: the same for one image
+ *                        with the sort and the bitmask spread over a
+ *                        cluster).
  * Ranking is canonical: votes descending, then the reference raster index
  * (rho-major, theta-minor) ascending -- the reference's Shell sort
  * (:853-873) is unstable, so ties are ordered by index here.
